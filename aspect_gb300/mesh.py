@@ -1,0 +1,261 @@
+"""Level meshes, DoF maps and constraints handed to the solver through the C ABI.
+
+This module is the caller side of the boundary: it produces exactly the arrays
+that ASPECT's ``setup_dofs`` produces through deal.II
+(source/simulator/solver/stokes_matrix_free_global_coarsening.cc:1456-1732 builds
+one DoFHandler plus AffineConstraints per level of a global-coarsening
+hierarchy): per level, the cell-to-DoF maps of the Q2 velocity and Q1 pressure,
+the cell geometry, the constraint lines (no-normal-flux, Dirichlet, hanging
+nodes) and the parent/child relation to the next coarser level.
+
+Conventions (shared with ``include/gb_gmg.h``):
+
+* cells of a level are numbered 0..n_cells-1; local DoFs are lexicographic,
+  velocity components blocked (``c * 3**dim + node``);
+* geometry kind 0 (``GEOM_BOX``): per cell ``[x0.., h..]`` (lower corner and
+  edge lengths of an axis-aligned box); kind 1 (``GEOM_Q2``): the 3**dim Q2
+  support points of the cell mapping, ``[node][dim]``;
+* a constraint line is ``x[row] = sum_k w_k x[col_k] + inhomogeneity``; a line
+  with no entries is a Dirichlet constraint (zero in the homogeneous operators);
+* child index of a fine cell = sum_d bit_d << d, bit_d = which half of the
+  parent's reference cell the child occupies in direction d.
+"""
+from __future__ import annotations
+
+import dataclasses
+import itertools
+import numpy as np
+
+GEOM_BOX = 0
+GEOM_Q2 = 1
+
+
+@dataclasses.dataclass
+class Constraints:
+    """Closed AffineConstraints of one block, in CSR form."""
+
+    rows: np.ndarray  # int32 [n_lines]
+    ptr: np.ndarray  # int32 [n_lines+1]
+    cols: np.ndarray  # int32 [nnz]
+    weights: np.ndarray  # float64 [nnz]
+    inhom: np.ndarray  # float64 [n_lines]
+
+    @staticmethod
+    def empty() -> "Constraints":
+        return Constraints(np.zeros(0, np.int32), np.zeros(1, np.int32), np.zeros(0, np.int32),
+                           np.zeros(0), np.zeros(0))
+
+    @staticmethod
+    def from_dict(lines: dict) -> "Constraints":
+        """``lines``: row -> (list[(col, weight)], inhomogeneity)."""
+        rows = np.array(sorted(lines), dtype=np.int32)
+        ptr = [0]
+        cols, ws, inh = [], [], []
+        for r in rows:
+            ent, b = lines[int(r)]
+            for c, w in ent:
+                cols.append(c)
+                ws.append(w)
+            ptr.append(len(cols))
+            inh.append(b)
+        return Constraints(rows, np.array(ptr, np.int32), np.array(cols, np.int32),
+                           np.array(ws, float), np.array(inh, float))
+
+    @property
+    def n_lines(self) -> int:
+        return len(self.rows)
+
+    def constrained_mask(self, n: int) -> np.ndarray:
+        m = np.zeros(n, bool)
+        m[self.rows] = True
+        return m
+
+    def distribute(self, x: np.ndarray) -> None:
+        """x[row] = sum w x[col] + b (AffineConstraints::distribute)."""
+        for i, r in enumerate(self.rows):
+            a, b = self.ptr[i], self.ptr[i + 1]
+            x[r] = np.dot(self.weights[a:b], x[self.cols[a:b]]) + self.inhom[i]
+
+    def set_zero(self, x: np.ndarray) -> None:
+        x[self.rows] = 0.0
+
+    def condense(self, f: np.ndarray) -> None:
+        """Move rhs entries of constrained rows to their masters, then zero them."""
+        for i, r in enumerate(self.rows):
+            a, b = self.ptr[i], self.ptr[i + 1]
+            if b > a:
+                np.add.at(f, self.cols[a:b], self.weights[a:b] * f[r])
+        f[self.rows] = 0.0
+
+
+@dataclasses.dataclass
+class LevelMesh:
+    dim: int
+    n_cells: int
+    n_u: int
+    n_p: int
+    cell_dofs_u: np.ndarray  # int32 [n_cells, dim*3**dim]
+    cell_dofs_p: np.ndarray  # int32 [n_cells, 2**dim]
+    geom_kind: int
+    geometry: np.ndarray  # float64, see module doc
+    constraints_u: Constraints
+    constraints_p: Constraints
+    parent: np.ndarray | None = None  # int32 [n_cells] into the next coarser level
+    child_index: np.ndarray | None = None  # uint8 [n_cells]
+    # Position of each velocity / pressure DoF (for boundary conditions and
+    # function interpolation); velocity DoF positions repeat per component.
+    dof_points_u: np.ndarray | None = None
+    dof_component_u: np.ndarray | None = None
+    dof_points_p: np.ndarray | None = None
+    # Optional extra information used by the harness only.
+    cell_level: np.ndarray | None = None
+
+    def q2_support_points(self) -> np.ndarray:
+        """Q2 mapping support points per cell, shape (n_cells, 3**dim, dim)."""
+        from . import fe
+        if self.geom_kind == GEOM_Q2:
+            return self.geometry.reshape(self.n_cells, 3 ** self.dim, self.dim)
+        ref = fe.tensor_points(self.dim, fe.Q2_NODES)
+        g = self.geometry.reshape(self.n_cells, 2 * self.dim)
+        return g[:, None, :self.dim] + ref[None, :, :] * g[:, None, self.dim:]
+
+    def map_points(self, ref_pts: np.ndarray) -> np.ndarray:
+        """Real coordinates of reference points in every cell: (n_cells, n_pts, dim)."""
+        from . import fe
+        if self.geom_kind == GEOM_BOX:
+            g = self.geometry.reshape(self.n_cells, 2 * self.dim)
+            return g[:, None, :self.dim] + ref_pts[None, :, :] * g[:, None, self.dim:]
+        phi = fe.shape_values(self.dim, fe.Q2_NODES, ref_pts)
+        X = self.q2_support_points()
+        return np.einsum("qn,cnd->cqd", phi, X)
+
+    def jacobians(self, ref_pts: np.ndarray) -> np.ndarray:
+        """dx/dxi at reference points: (n_cells, n_pts, dim, dim) [x-comp, xi-dir]."""
+        from . import fe
+        if self.geom_kind == GEOM_BOX:
+            g = self.geometry.reshape(self.n_cells, 2 * self.dim)
+            J = np.zeros((self.n_cells, len(ref_pts), self.dim, self.dim))
+            for d in range(self.dim):
+                J[:, :, d, d] = g[:, None, self.dim + d]
+            return J
+        dphi = fe.shape_grads(self.dim, fe.Q2_NODES, ref_pts)
+        X = self.q2_support_points()
+        return np.einsum("qne,cnd->cqde", dphi, X)
+
+
+def _lex(idx: tuple, shape: tuple) -> int:
+    out, stride = 0, 1
+    for i, n in zip(idx, shape):
+        out += i * stride
+        stride *= n
+    return out
+
+
+def box_level(dim: int, ncells: tuple, extent: tuple, origin: tuple | None = None,
+              free_slip: bool = True) -> LevelMesh:
+    """Uniform axis-aligned box with lexicographic cells, component-blocked
+    Q2 velocity numbering and lexicographic Q1 pressure numbering.
+
+    ``free_slip``: no-normal-flux on every face (the normal component is a
+    Dirichlet-zero line), as ``Tangential velocity boundary indicators`` gives
+    on a box (VectorTools::compute_no_normal_flux_constraints on axis-aligned
+    faces)."""
+    origin = origin or (0.0,) * dim
+    ncells = tuple(ncells)
+    h = tuple(extent[d] / ncells[d] for d in range(dim))
+    nn = tuple(2 * n + 1 for n in ncells)  # Q2 nodes per direction
+    npn = tuple(n + 1 for n in ncells)  # Q1 nodes per direction
+    n_nodes = int(np.prod(nn))
+    n_pnodes = int(np.prod(npn))
+    n_cells = int(np.prod(ncells))
+
+    # cell multi-indices, x fastest
+    cidx = np.stack(np.meshgrid(*[np.arange(n) for n in ncells], indexing="ij"), -1)
+    cidx = cidx.transpose(*reversed(range(dim)), dim).reshape(-1, dim)  # x fastest
+    loc = np.array(list(itertools.product(range(3), repeat=dim)))[:, ::-1]  # x fastest
+    locp = np.array(list(itertools.product(range(2), repeat=dim)))[:, ::-1]
+
+    strides = np.cumprod((1,) + nn[:-1])
+    pstrides = np.cumprod((1,) + npn[:-1])
+    node = ((2 * cidx[:, None, :] + loc[None, :, :]) * strides).sum(-1)  # (n_cells, 3^d)
+    pnode = ((cidx[:, None, :] + locp[None, :, :]) * pstrides).sum(-1)
+    cell_dofs_u = np.concatenate([node + c * n_nodes for c in range(dim)], axis=1).astype(np.int32)
+    cell_dofs_p = pnode.astype(np.int32)
+
+    geom = np.zeros((n_cells, 2 * dim))
+    for d in range(dim):
+        geom[:, d] = origin[d] + cidx[:, d] * h[d]
+        geom[:, dim + d] = h[d]
+
+    # DoF positions
+    nidx = np.stack(np.meshgrid(*[np.arange(n) for n in nn], indexing="ij"), -1)
+    nidx = nidx.transpose(*reversed(range(dim)), dim).reshape(-1, dim)
+    pts_u = np.array([origin[d] + nidx[:, d] * 0.5 * h[d] for d in range(dim)]).T
+    pidx = np.stack(np.meshgrid(*[np.arange(n) for n in npn], indexing="ij"), -1)
+    pidx = pidx.transpose(*reversed(range(dim)), dim).reshape(-1, dim)
+    pts_p = np.array([origin[d] + pidx[:, d] * h[d] for d in range(dim)]).T
+
+    lines = {}
+    if free_slip:
+        for c in range(dim):
+            on_face = (nidx[:, c] == 0) | (nidx[:, c] == nn[c] - 1)
+            for nd in np.nonzero(on_face)[0]:
+                lines[int(nd + c * n_nodes)] = ([], 0.0)
+    cu = Constraints.from_dict(lines)
+
+    return LevelMesh(dim=dim, n_cells=n_cells, n_u=dim * n_nodes, n_p=n_pnodes,
+                     cell_dofs_u=cell_dofs_u, cell_dofs_p=cell_dofs_p, geom_kind=GEOM_BOX,
+                     geometry=geom, constraints_u=cu, constraints_p=Constraints.empty(),
+                     dof_points_u=np.tile(pts_u, (dim, 1)),
+                     dof_component_u=np.repeat(np.arange(dim), n_nodes),
+                     dof_points_p=pts_p)
+
+
+def box_hierarchy(dim: int, n_fine: int, extent=None, n_coarse: int = 1,
+                  free_slip: bool = True) -> list[LevelMesh]:
+    """Global-coarsening hierarchy of uniform boxes: level l has n_coarse*2**l
+    cells per direction, up to n_fine on the finest level."""
+    extent = tuple(extent or (1.0,) * dim)
+    levels = []
+    n = n_coarse
+    while n <= n_fine:
+        levels.append(box_level(dim, (n,) * dim, extent, free_slip=free_slip))
+        n *= 2
+    assert levels and n // 2 == n_fine, "n_fine must be n_coarse * 2**k"
+    for l in range(1, len(levels)):
+        nc = n_coarse * 2 ** l
+        cidx = np.stack(np.meshgrid(*[np.arange(nc)] * dim, indexing="ij"), -1)
+        cidx = cidx.transpose(*reversed(range(dim)), dim).reshape(-1, dim)
+        par = cidx // 2
+        pstr = np.cumprod((1,) + (nc // 2,) * (dim - 1))
+        levels[l].parent = (par * pstr).sum(-1).astype(np.int32)
+        levels[l].child_index = ((cidx % 2) << np.arange(dim)).sum(-1).astype(np.uint8)
+    return levels
+
+
+def permute_dofs(level: LevelMesh, seed: int) -> tuple[LevelMesh, np.ndarray, np.ndarray]:
+    """Return a copy with randomly renumbered DoFs (tests that the library does not
+    depend on the caller's numbering). Returns (mesh, perm_u, perm_p) where
+    new_index = perm[old_index]."""
+    rng = np.random.default_rng(seed)
+    pu = rng.permutation(level.n_u).astype(np.int32)
+    pp = rng.permutation(level.n_p).astype(np.int32)
+
+    def remap(c: Constraints, perm):
+        lines = {}
+        for i, r in enumerate(c.rows):
+            a, b = c.ptr[i], c.ptr[i + 1]
+            lines[int(perm[r])] = ([(int(perm[cc]), float(w)) for cc, w in
+                                    zip(c.cols[a:b], c.weights[a:b])], float(c.inhom[i]))
+        return Constraints.from_dict(lines)
+
+    inv_u = np.argsort(pu)
+    inv_p = np.argsort(pp)
+    out = dataclasses.replace(
+        level, cell_dofs_u=pu[level.cell_dofs_u].astype(np.int32),
+        cell_dofs_p=pp[level.cell_dofs_p].astype(np.int32),
+        constraints_u=remap(level.constraints_u, pu), constraints_p=remap(level.constraints_p, pp),
+        dof_points_u=level.dof_points_u[inv_u] if level.dof_points_u is not None else None,
+        dof_component_u=level.dof_component_u[inv_u] if level.dof_component_u is not None else None,
+        dof_points_p=level.dof_points_p[inv_p] if level.dof_points_p is not None else None)
+    return out, pu, pp

@@ -1,0 +1,236 @@
+"""Synthetic Stokes problems and the caller-side steps around one solve.
+
+These functions stand in for the parts of ASPECT that sit *around* the
+matrix-free solver and stay on the caller's side of the C ABI:
+
+* right-hand side ``rho g . phi_u`` (source/simulator/assemblers/stokes.cc:285-400),
+  condensed with the constraints as ``distribute_local_to_global`` does;
+* pressure scaling = volume-weighted geometric mean viscosity at cell
+  midpoints / length scale (source/simulator/helper_functions.cc:255-345;
+  box length scale 0.01 * x-extent, source/geometry_model/box.cc:252-255);
+* viscosity averaging (include/aspect/material_model/interface.h:818-831);
+* surface pressure normalisation (source/simulator/helper_functions.cc:765-880);
+* error norms of the SolCx postprocessor (benchmarks/solcx/solcx.h:3106-3190,
+  QGauss(degree_v+2)).
+
+Random inputs use one SplitMix64 stream per seed; the default seed of the
+benchmark workloads is 20261204 + workload index.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+import numpy as np
+
+from . import fe
+from .mesh import LevelMesh, box_hierarchy
+
+BASE_SEED = 20261204
+
+
+class SplitMix64:
+    def __init__(self, seed: int):
+        self.state = seed & 0xFFFFFFFFFFFFFFFF
+
+    def next_u64(self) -> int:
+        self.state = (self.state + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+        z = self.state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+        return z ^ (z >> 31)
+
+    def uniform(self, n: int = 1) -> np.ndarray:
+        return np.array([(self.next_u64() >> 11) * (1.0 / 9007199254740992.0) for _ in range(n)])
+
+    def normal(self, n: int) -> np.ndarray:
+        u1 = np.maximum(self.uniform(n), 1e-300)
+        u2 = self.uniform(n)
+        return np.sqrt(-2 * np.log(u1)) * np.cos(2 * np.pi * u2)
+
+
+@dataclasses.dataclass
+class StokesProblem:
+    """Everything one solve needs, in the caller's (deal.II-like) numbering."""
+
+    name: str
+    levels: list
+    eta: np.ndarray            # finest level: [n_cells] (averaged) or [n_cells, n_q]
+    projection: int            # 0: DGQ0 level tables, 1: DGQ1 (project to Q1)
+    pressure_scaling: float
+    rhs: np.ndarray            # [n_u + n_p], condensed
+    gravity_dir: int           # for reporting only
+    extra: dict = dataclasses.field(default_factory=dict)
+
+    @property
+    def fine(self) -> LevelMesh:
+        return self.levels[-1]
+
+    @property
+    def n_dofs(self) -> int:
+        return self.fine.n_u + self.fine.n_p
+
+
+def q_points_real(level: LevelMesh, n1d: int = 3) -> tuple[np.ndarray, np.ndarray]:
+    """Real quadrature points (n_cells, n_q, dim) and JxW (n_cells, n_q)."""
+    pts, w = fe.quadrature(level.dim, n1d)
+    x = level.map_points(pts)
+    J = level.jacobians(pts)
+    det = np.linalg.det(J)
+    return x, np.abs(det) * w[None, :]
+
+
+def assemble_rhs(level: LevelMesh, force_q: np.ndarray) -> np.ndarray:
+    """f_u = int force . phi_u over QGauss(3); force_q: (n_cells, n_q, dim).
+    Pressure block zero (incompressible). Condensed with the constraints."""
+    dim = level.dim
+    pts, w = fe.quadrature(dim, 3)
+    phi = fe.shape_values(dim, fe.Q2_NODES, pts)  # (nq, nv)
+    _, jxw = q_points_real(level)
+    nv = 3 ** dim
+    f = np.zeros(level.n_u + level.n_p)
+    loc = np.einsum("cqd,qn,cq->cdn", force_q, phi, jxw).reshape(level.n_cells, dim * nv)
+    np.add.at(f, level.cell_dofs_u.ravel(), loc.ravel())
+    fu = f[: level.n_u]
+    level.constraints_u.condense(fu)
+    f[: level.n_u] = fu
+    return f
+
+
+def pressure_scaling(level: LevelMesh, eta_mid: np.ndarray, length_scale: float) -> float:
+    """Geometric mean of the midpoint viscosity (volume weighted) / length scale."""
+    pts = np.full((1, level.dim), 0.5)
+    J = level.jacobians(pts)
+    vol = np.abs(np.linalg.det(J))[:, 0]
+    return float(np.exp(np.sum(np.log(eta_mid) * vol) / np.sum(vol)) / length_scale)
+
+
+def harmonic_average(eta_q: np.ndarray, jxw: np.ndarray) -> np.ndarray:
+    return np.sum(jxw, 1) / np.sum(jxw / eta_q, 1)
+
+
+def normalize_pressure_surface(level: LevelMesh, p: np.ndarray, top: float = 1.0) -> float:
+    """Shift p so that its mean over the top boundary (x_{dim-1} == top) is zero.
+    Returns the adjustment added. Exact for Q1 on straight faces."""
+    dim = level.dim
+    g = level.geometry.reshape(level.n_cells, -1)
+    num = den = 0.0
+    if level.geom_kind != 0:
+        raise NotImplementedError("surface normalisation implemented for box cells only")
+    on_top = np.abs(g[:, dim - 1] + g[:, 2 * dim - 1] - top) < 1e-12
+    # top face local pressure nodes: those with bit (dim-1) set
+    loc = [n for n in range(2 ** dim) if (n >> (dim - 1)) & 1]
+    for c in np.nonzero(on_top)[0]:
+        area = np.prod(g[c, dim:2 * dim - 1])
+        num += area * np.mean(p[level.cell_dofs_p[c, loc]])
+        den += area
+    adj = -num / den
+    p += adj
+    return adj
+
+
+def normalize_pressure_volume(level: LevelMesh, p: np.ndarray) -> float:
+    pts, w = fe.quadrature(level.dim, 3)
+    psi = fe.shape_values(level.dim, fe.Q1_NODES, pts)
+    _, jxw = q_points_real(level)
+    pq = np.einsum("qn,cn->cq", psi, p[level.cell_dofs_p])
+    adj = -np.sum(pq * jxw) / np.sum(jxw)
+    p += adj
+    return adj
+
+
+def evaluate_fields(level: LevelMesh, u: np.ndarray, p: np.ndarray, n1d: int):
+    """Velocity and pressure at QGauss(n1d) points: (n_cells, nq, dim), (n_cells, nq)."""
+    dim = level.dim
+    pts, w = fe.quadrature(dim, n1d)
+    phi = fe.shape_values(dim, fe.Q2_NODES, pts)
+    psi = fe.shape_values(dim, fe.Q1_NODES, pts)
+    nv = 3 ** dim
+    ul = u[level.cell_dofs_u].reshape(level.n_cells, dim, nv)
+    uq = np.einsum("qn,cdn->cqd", phi, ul)
+    pq = np.einsum("qn,cn->cq", psi, p[level.cell_dofs_p])
+    return uq, pq
+
+
+def error_norms(level: LevelMesh, u, p, exact_u_q, exact_p_q, n1d: int = 4):
+    """(u_L1, p_L1, u_L2, p_L2) against exact values at the QGauss(n1d) points.
+    The L1 norm of a vector field sums the absolute values of its components,
+    as VectorTools::integrate_difference does for L1_norm."""
+    uq, pq = evaluate_fields(level, u, p, n1d)
+    pts, w = fe.quadrature(level.dim, n1d)
+    J = level.jacobians(pts)
+    jxw = np.abs(np.linalg.det(J)) * w[None, :]
+    du = uq - exact_u_q
+    dp = pq - exact_p_q
+    u_l1 = np.sum(np.sum(np.abs(du), -1) * jxw)
+    p_l1 = np.sum(np.abs(dp) * jxw)
+    u_l2 = math.sqrt(np.sum(np.sum(du ** 2, -1) * jxw))
+    p_l2 = math.sqrt(np.sum(dp ** 2 * jxw))
+    return u_l1, p_l1, u_l2, p_l2
+
+
+# --------------------------------------------------------------------- problems
+def solcx(n_refinements: int, eta_B: float = 1e6, density_sign: float = -1.0,
+          name: str | None = None) -> StokesProblem:
+    """SolCx (benchmarks/solcx/solcx.h:2953-2975): eta = 1 for x < 1/2 and eta_B
+    otherwise, rho = density_sign * sin(pi y) cos(pi x), g = (0, -1), free slip on
+    all walls, harmonic averaging (constant per cell here). density_sign = -1 is
+    the reference benchmark; +1 is the variant of the 64x64 workload."""
+    n = 2 ** n_refinements
+    levels = box_hierarchy(2, n)
+    fine = levels[-1]
+    xq, jxw = q_points_real(fine)
+    eta_q = np.where(xq[..., 0] < 0.5, 1.0, eta_B)
+    eta = harmonic_average(eta_q, jxw)
+    rho = density_sign * np.sin(np.pi * xq[..., 1]) * np.cos(np.pi * xq[..., 0])
+    force = np.zeros(xq.shape)
+    force[..., 1] = -rho
+    rhs = assemble_rhs(fine, force)
+    mid = fine.map_points(np.full((1, 2), 0.5))[:, 0, :]
+    s = pressure_scaling(fine, np.where(mid[:, 0] < 0.5, 1.0, eta_B), 0.01 * 1.0)
+    return StokesProblem(name or f"solcx_{n}x{n}", levels, eta, 0, s, rhs, 1)
+
+
+def sinker_centres(seed: int, n: int = 8) -> np.ndarray:
+    rng = SplitMix64(seed)
+    return 0.2 + 0.6 * rng.uniform(3 * n).reshape(n, 3)
+
+
+def sinker_viscosity(x: np.ndarray, centres: np.ndarray, contrast_power: float = 2.0) -> np.ndarray:
+    """eta0 = 1e-3 + (1 - 1e-3) prod_i (1 - exp(-d_i^2 / (2 0.05^2))), then eta0**2
+    (a 1e6 contrast, range 1e-6 .. 1)."""
+    prod = np.ones(x.shape[:-1])
+    for c in centres:
+        d2 = np.sum((x - c) ** 2, -1)
+        prod *= 1.0 - np.exp(-d2 / (2 * 0.05 ** 2))
+    eta0 = 1e-3 + (1 - 1e-3) * prod
+    return eta0 ** contrast_power
+
+
+def sinker_density(x: np.ndarray, centres: np.ndarray, radius: float = 0.075) -> np.ndarray:
+    inside = np.zeros(x.shape[:-1], bool)
+    for c in centres:
+        inside |= np.sum((x - c) ** 2, -1) < radius ** 2
+    return inside.astype(float)
+
+
+def sinkers_3d(n: int = 32, seed: int = BASE_SEED + 2, projection: int = 1,
+               n_coarse: int = 1) -> StokesProblem:
+    """3D unit cube, n^3 Q2-Q1 cells, 8 smooth sinkers (centres seeded uniform in
+    [0.2, 0.8]^3), eta = eta0**2 (1e6 contrast), rho = 1 inside r = 0.075, g = -z,
+    free slip. ``projection`` = 1 uses ASPECT's default averaging for GMG
+    (project to Q1 only viscosity: per-quadrature-point viscosity); 0 uses the
+    harmonic cell average."""
+    levels = box_hierarchy(3, n, n_coarse=n_coarse)
+    fine = levels[-1]
+    centres = sinker_centres(seed)
+    xq, jxw = q_points_real(fine)
+    eta_q = sinker_viscosity(xq, centres)
+    eta = eta_q if projection == 1 else harmonic_average(eta_q, jxw)
+    rho = sinker_density(xq, centres)
+    force = np.zeros(xq.shape)
+    force[..., 2] = -rho
+    rhs = assemble_rhs(fine, force)
+    mid = fine.map_points(np.full((1, 3), 0.5))[:, 0, :]
+    s = pressure_scaling(fine, sinker_viscosity(mid, centres), 0.01)
+    return StokesProblem(f"sinkers_{n}^3", levels, eta, projection, s, rhs, 2,
+                         extra=dict(centres=centres, seed=seed))

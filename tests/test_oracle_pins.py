@@ -1,0 +1,105 @@
+"""The CPU oracle against the reference's own regression outputs and against
+brute-force assembled matrices. No GPU needed."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from aspect_gb300 import fe, mesh, problems
+from oracle import Oracle
+from tests import numpy_reference as nr
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.mark.parametrize("nref", [2, 4])
+def test_solcx_matches_reference_regression(nref):
+    """sol_cx_2_gmg / sol_cx_4_gmg: iteration count and the four error norms."""
+    golden = json.load(open(os.path.join(GOLDEN, "solcx_golden.json")))[str(2 ** nref)]
+    exact = np.load(os.path.join(GOLDEN, "solcx_exact.npz"))
+    P = problems.solcx(nref)
+    f = P.fine
+    assert (f.n_u, f.n_p) == (golden["n_u"], golden["n_p"])
+    o = Oracle(P.levels)
+    o.set_viscosity(P.eta, P.projection, P.pressure_scaling)
+    o.build_preconditioner(False)
+    x, info = o.solve(P.rhs, tol_rel=1e-7)
+    assert info["status"] == 0
+    assert info["cheap_iterations"] == golden["cheap_iterations"]
+    assert info["expensive_iterations"] == golden["expensive_iterations"]
+    u = x[: f.n_u].copy()
+    p = x[f.n_u:] * P.pressure_scaling
+    f.constraints_u.distribute(u)
+    problems.normalize_pressure_surface(f, p)
+    n = 2 ** nref
+    errs = problems.error_norms(f, u, p, exact[f"u_{n}"], exact[f"p_{n}"])
+    # the reference prints 7 significant digits
+    np.testing.assert_allclose(errs, golden["errors"], rtol=2e-6)
+
+
+def _small_problem(dim, n, per_q, seed=3):
+    levels = mesh.box_hierarchy(dim, n)
+    f = levels[-1]
+    rng = np.random.default_rng(seed)
+    nq = 3 ** dim
+    eta = np.exp(rng.normal(size=(f.n_cells, nq) if per_q else f.n_cells))
+    return levels, eta
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("per_q", [False, True])
+def test_oracle_operators_match_assembled(dim, per_q):
+    levels, eta = _small_problem(dim, 2, per_q)
+    f = levels[-1]
+    s = 3.7
+    o = Oracle(levels)
+    o.set_viscosity(eta, 0, s)
+    eq = eta if per_q else np.repeat(eta[:, None], 3 ** dim, 1)
+    A, BT, M = nr.stokes_blocks(f, eq, s)
+    Cu = nr.constraint_matrix(f.n_u, f.constraints_u)
+    mu = f.constraints_u.constrained_mask(f.n_u)
+    Ac = nr.constrained_operator(A, Cu, Cu, mu)
+    rng = np.random.default_rng(1)
+    x = rng.normal(size=f.n_u + f.n_p)
+    ya = o.vmult(1, len(levels) - 1, x[: f.n_u])
+    np.testing.assert_allclose(ya, Ac @ x[: f.n_u], rtol=1e-12, atol=1e-12 * np.abs(ya).max())
+    ym = o.vmult(3, len(levels) - 1, x[f.n_u:])
+    np.testing.assert_allclose(ym, M @ x[f.n_u:], rtol=1e-12, atol=1e-12 * np.abs(ym).max())
+    # full Stokes: [A BT; BT^T 0] with constrained velocity rows/cols
+    BTc = Cu.T @ BT
+    BTc[mu, :] = 0
+    K = np.block([[Ac, BTc], [BTc.T, np.zeros((f.n_p, f.n_p))]])
+    ys = o.vmult(0, len(levels) - 1, x)
+    np.testing.assert_allclose(ys, K @ x, rtol=1e-12, atol=1e-12 * np.abs(ys).max())
+    yb = o.vmult(2, len(levels) - 1, x[f.n_u:])
+    np.testing.assert_allclose(yb, BTc @ x[f.n_u:], rtol=1e-12, atol=1e-12 * np.abs(yb).max())
+    # diagonals
+    o.build_preconditioner(False)
+    dA = o.diagonal_inverse(len(levels) - 1, 0)
+    ref = 1.0 / np.where(mu, 1.0, np.diag(Ac))
+    np.testing.assert_allclose(dA, ref, rtol=1e-12)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_transfer_is_exact_embedding(dim):
+    """Prolongating a coarse FE function reproduces it at the fine DoF points."""
+    levels = mesh.box_hierarchy(dim, 4, free_slip=False)
+    o = Oracle(levels)
+    c, f = levels[-2], levels[-1]
+
+    def field(x, comp):
+        return 1 + x[:, 0] ** 2 - 0.5 * x[:, 1] * (comp + 1) + (x[:, -1] ** 2 if dim == 3 else 0)
+
+    uc = field(c.dof_points_u, c.dof_component_u)
+    uf = o.transfer(len(levels) - 1, 0, False, uc)
+    np.testing.assert_allclose(uf, field(f.dof_points_u, f.dof_component_u), rtol=1e-13, atol=1e-13)
+    pc = 1 + c.dof_points_p.sum(1)
+    pf = o.transfer(len(levels) - 1, 1, False, pc)
+    np.testing.assert_allclose(pf, 1 + f.dof_points_p.sum(1), rtol=1e-13)
+    # restriction is the transpose
+    rng = np.random.default_rng(0)
+    a, b = rng.normal(size=c.n_u), rng.normal(size=f.n_u)
+    lhs = b @ o.transfer(len(levels) - 1, 0, False, a)
+    rhs = a @ o.transfer(len(levels) - 1, 0, True, b)
+    assert abs(lhs - rhs) < 1e-12 * abs(lhs)
