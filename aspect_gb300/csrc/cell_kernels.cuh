@@ -1,0 +1,792 @@
+// Matrix-free cell kernels of the Q2-Q1 Stokes operators (sm_103a).
+//
+// Physics per quadrature point follows
+// source/simulator/solver/matrix_free_operators.cc:
+//   StokesOperator::local_apply   :376-547  (velocity test 2 eta eps(u) - s p I,
+//                                            pressure test -s div u)
+//   BTBlockOperator::local_apply  :668-701  (-s p I : eps(v))
+//   MassMatrixOperator            :787-845  (s^2 / eta p q)
+//   ABlockOperator                :974-1009 (2 eta eps(u), deviatoric if compressible)
+// Constrained rows are the identity and constrained columns are resolved
+// through the constraint lines, as MatrixFreeOperators::Base::vmult does.
+//
+// GB300 mapping (not the reference's SIMD-over-cells layout): one velocity
+// component per thread, `dim` threads per cell (10 cells per warp in 3D, 16 in
+// 2D). Each thread keeps the 3^dim nodal values of its component in registers,
+// interpolates them to the Gauss points (collocation), forms its row of the
+// velocity gradient, and exchanges the off-diagonal entries it needs for the
+// symmetric gradient with its sibling threads through warp shuffles. The cells
+// of one launch form one colour of a conflict-free colouring, so the scatter
+// is a plain read-modify-write and every result is bit-reproducible.
+#pragma once
+#include "common.cuh"
+#include "fe_tables.cuh"
+
+namespace gb {
+
+enum OpKind { OPK_STOKES = 0, OPK_A = 1, OPK_BT = 2, OPK_MASS = 3 };
+enum GeomKind { GEOM_CART = 0, GEOM_BOX = 1, GEOM_TABLE = 2 };
+
+// Device view of one level, passed by value to every kernel.
+template <typename T>
+struct LevelView {
+  int dim;
+  int n_cells, n_u, n_p;
+  int structured;
+  // structured box levels (internal lexicographic numbering, components blocked)
+  int nc[3];      // cells per direction
+  int Nn[3];      // Q2 nodes per direction
+  int Np[3];      // Q1 nodes per direction
+  int n_nodes;    // Q2 nodes
+  uint32_t zero_faces;  // bit (2*d+side)*3+comp: component comp is zero on that face
+  T inv_h[3];     // 1/h per direction
+  T det;          // cell volume
+  // general levels (cells sorted by colour)
+  const int* cdu;       // [n_cells][dim*3^dim]  >=0 dof, -1 zero, <=-2 line -(v+2)
+  const int* cdp;       // [n_cells][2^dim]
+  const int* lptr;      // velocity lines
+  const int* lcol;
+  const T* lw;
+  const int* plptr;     // pressure lines
+  const int* plcol;
+  const T* plw;
+  int geom;             // GeomKind
+  const T* gbox;        // [n_cells][dim+1]: 1/h_d, det
+  const T* gtab;        // [n_cells][nq][dim*dim+1]: invJ (dxi_d/dx_e at [d*dim+e]), JxW/w_q
+  const T* eta;         // [n_cells][eta_n]
+  int eta_n;
+  T s;                  // pressure scaling
+  int compressible;
+};
+
+template <int dim>
+struct Shape {
+  static constexpr int nv = fe::pow3(dim);
+  static constexpr int np = fe::pow2(dim);
+  static constexpr int nq = nv;
+  static constexpr int tpc = dim;                 // threads per cell
+  static constexpr int cpw = 32 / dim;            // cells per warp
+};
+
+// ---------------------------------------------------------------------------
+// 1D sweeps over registers (fully unrolled; matrices are compile-time).
+template <typename T, int dim, int dir, bool transpose>
+__device__ __forceinline__ void sweep_S(T* x) {
+  constexpr int st = fe::pow3(dir);
+#pragma unroll
+  for (int b = 0; b < fe::pow3(dim); ++b) {
+    if ((b / st) % 3 != 0) continue;
+    const T a0 = x[b], a1 = x[b + st], a2 = x[b + 2 * st];
+    if (!transpose) {
+      x[b] = T(fe::Sv(0, 0)) * a0 + T(fe::Sv(0, 1)) * a1 + T(fe::Sv(0, 2)) * a2;
+      x[b + st] = a1;
+      x[b + 2 * st] = T(fe::Sv(2, 0)) * a0 + T(fe::Sv(2, 1)) * a1 + T(fe::Sv(2, 2)) * a2;
+    } else {
+      x[b] = T(fe::Sv(0, 0)) * a0 + T(fe::Sv(2, 0)) * a2;
+      x[b + st] = T(fe::Sv(0, 1)) * a0 + a1 + T(fe::Sv(2, 1)) * a2;
+      x[b + 2 * st] = T(fe::Sv(0, 2)) * a0 + T(fe::Sv(2, 2)) * a2;
+    }
+  }
+}
+
+template <typename T, int dim, bool transpose>
+__device__ __forceinline__ void interpolate(T* x) {
+  sweep_S<T, dim, 0, transpose>(x);
+  sweep_S<T, dim, 1, transpose>(x);
+  if constexpr (dim == 3) sweep_S<T, dim, 2, transpose>(x);
+}
+
+// derivative along `dir` at Gauss point q of a collocated field
+template <typename T, int dim, int q, int dir>
+__device__ __forceinline__ T colloc_d(const T* x) {
+  constexpr int st = fe::pow3(dir);
+  constexpr int qd = (q / st) % 3;
+  constexpr int b = q - qd * st;
+  return T(fe::Dv(qd, 0)) * x[b] + T(fe::Dv(qd, 1)) * x[b + st] + T(fe::Dv(qd, 2)) * x[b + 2 * st];
+}
+template <typename T, int dim, int q, int dir>
+__device__ __forceinline__ void colloc_dT(T* x, T r) {
+  constexpr int st = fe::pow3(dir);
+  constexpr int qd = (q / st) % 3;
+  constexpr int b = q - qd * st;
+  x[b] += T(fe::Dv(qd, 0)) * r;
+  x[b + st] += T(fe::Dv(qd, 1)) * r;
+  x[b + 2 * st] += T(fe::Dv(qd, 2)) * r;
+}
+
+template <int dim, int q>
+__host__ __device__ constexpr double qweight() {
+  return dim == 2 ? fe::Wv(q % 3) * fe::Wv(q / 3) : fe::Wv(q % 3) * fe::Wv((q / 3) % 3) * fe::Wv(q / 9);
+}
+template <int dim, int q, int n>
+__host__ __device__ constexpr double psi_at() {
+  double v = fe::P1v(q % 3, n & 1) * fe::P1v((q / 3) % 3, (n >> 1) & 1);
+  if (dim == 3) v *= fe::P1v(q / 9, (n >> 2) & 1);
+  return v;
+}
+
+// select among values indexed relative to the thread's component
+template <typename T>
+__device__ __forceinline__ T sel3(T r0, T r1, T r2, int k) { return k == 0 ? r0 : (k == 1 ? r1 : r2); }
+
+// ---------------------------------------------------------------------------
+// DoF access
+template <typename T, int dim>
+struct StructuredCell {
+  int i, j, k;
+  int node0;  // Q2 node index of the cell's first node
+  int pnode0;
+};
+
+template <typename T, int dim>
+__device__ __forceinline__ void structured_cell(const LevelView<T>& L, int colour, int idx, int& cell,
+                                                StructuredCell<T, dim>& sc, bool& valid) {
+  const int ci = colour & 1, cj = (colour >> 1) & 1, ck = (colour >> 2) & 1;
+  const int mx = (L.nc[0] - ci + 1) >> 1, my = (L.nc[1] - cj + 1) >> 1;
+  const int mz = dim == 3 ? (L.nc[2] - ck + 1) >> 1 : 1;
+  valid = idx < mx * my * mz;
+  const int a = idx % mx, b = (idx / mx) % my, c = idx / (mx * my);
+  sc.i = 2 * a + ci;
+  sc.j = 2 * b + cj;
+  sc.k = dim == 3 ? 2 * c + ck : 0;
+  cell = (sc.k * L.nc[1] + sc.j) * L.nc[0] + sc.i;
+  sc.node0 = (2 * sc.k * L.Nn[1] + 2 * sc.j) * L.Nn[0] + 2 * sc.i;
+  sc.pnode0 = (sc.k * L.Np[1] + sc.j) * L.Np[0] + sc.i;
+}
+
+// Is velocity component `comp` of local node n of a structured cell constrained?
+template <typename T, int dim>
+__device__ __forceinline__ bool structured_zero(const LevelView<T>& L, const StructuredCell<T, dim>& sc,
+                                                int comp, int n) {
+  if (!L.zero_faces) return false;
+  const int gi[3] = {2 * sc.i + n % 3, 2 * sc.j + (n / 3) % 3, dim == 3 ? 2 * sc.k + n / 9 : 0};
+  bool z = false;
+#pragma unroll
+  for (int d = 0; d < dim; ++d) {
+    if (gi[d] == 0 && ((L.zero_faces >> ((2 * d) * 3 + comp)) & 1u)) z = true;
+    if (gi[d] == L.Nn[d] - 1 && ((L.zero_faces >> ((2 * d + 1) * 3 + comp)) & 1u)) z = true;
+  }
+  return z;
+}
+
+template <int dim>
+__device__ __forceinline__ int structured_node_offset(const int* Nn, int n) {
+  const int a = n % 3, b = (n / 3) % 3, c = dim == 3 ? n / 9 : 0;
+  return (c * Nn[1] + b) * Nn[0] + a;
+}
+template <int dim>
+__device__ __forceinline__ int structured_pnode_offset(const int* Np, int n) {
+  const int a = n & 1, b = (n >> 1) & 1, c = dim == 3 ? (n >> 2) & 1 : 0;
+  return (c * Np[1] + b) * Np[0] + a;
+}
+
+template <typename T>
+__device__ __forceinline__ T gather_general(const T* __restrict__ src, int e, const int* lptr, const int* lcol,
+                                            const T* lw) {
+  if (e >= 0) return src[e];
+  if (e == -1) return T(0);
+  const int l = -(e + 2);
+  T v = T(0);
+  for (int k = lptr[l]; k < lptr[l + 1]; ++k) v += lw[k] * src[lcol[k]];
+  return v;
+}
+template <typename T>
+__device__ __forceinline__ void scatter_general(T* __restrict__ dst, int e, T v, const int* lptr, const int* lcol,
+                                                const T* lw) {
+  if (e >= 0) { dst[e] += v; return; }
+  if (e == -1) return;
+  const int l = -(e + 2);
+  for (int k = lptr[l]; k < lptr[l + 1]; ++k) dst[lcol[k]] += lw[k] * v;
+}
+
+// ---------------------------------------------------------------------------
+// Geometry at one quadrature point: invJ[d][e] = dxi_d/dx_e and JxW.
+template <typename T, int dim>
+struct QGeom {
+  T iJ[dim][dim];
+  T jxw;
+};
+
+template <typename T, int dim, int q>
+__device__ __forceinline__ void qgeom(const LevelView<T>& L, int cell, const T* box, QGeom<T, dim>& g) {
+  if (L.geom == GEOM_TABLE) {
+    const T* t = L.gtab + ((size_t)cell * Shape<dim>::nq + q) * (dim * dim + 1);
+#pragma unroll
+    for (int d = 0; d < dim; ++d)
+#pragma unroll
+      for (int e = 0; e < dim; ++e) g.iJ[d][e] = t[d * dim + e];
+    g.jxw = t[dim * dim] * T(qweight<dim, q>());
+  } else {
+#pragma unroll
+    for (int d = 0; d < dim; ++d)
+#pragma unroll
+      for (int e = 0; e < dim; ++e) g.iJ[d][e] = d == e ? box[d] : T(0);
+    g.jxw = box[dim] * T(qweight<dim, q>());
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The velocity-test cell operator on registers.
+//   U: nodal values of this thread's velocity component (OPK_STOKES / OPK_A)
+//   P: nodal pressure values (OPK_STOKES / OPK_BT)
+// Output: V (nodal velocity-test contributions, this component),
+//         YP (partial pressure-test contributions of this component; STOKES)
+template <typename T, int dim, int op>
+__device__ __forceinline__ void velocity_cell_op(const LevelView<T>& L, int cell, int comp, unsigned lane_base,
+                                                 T* U, const T* P, T* V, T* YP, const T* box, T eta_cell,
+                                                 const T* __restrict__ eta_q) {
+  constexpr int nv = Shape<dim>::nv, np = Shape<dim>::np;
+  constexpr bool need_u = (op == OPK_STOKES || op == OPK_A);
+  constexpr bool need_p = (op == OPK_STOKES || op == OPK_BT);
+  const unsigned full = 0xffffffffu;
+  const int l1 = lane_base + (comp + 1) % dim;
+  const int l2 = lane_base + (comp + 2) % dim;
+  if (need_u) interpolate<T, dim, false>(U);
+#pragma unroll
+  for (int n = 0; n < nv; ++n) V[n] = T(0);
+  if (op == OPK_STOKES)
+#pragma unroll
+    for (int n = 0; n < np; ++n) YP[n] = T(0);
+  const T s = L.s;
+
+  static_for<nv>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    QGeom<T, dim> G;
+    if (L.geom == GEOM_CART) {
+#pragma unroll
+      for (int d = 0; d < dim; ++d)
+#pragma unroll
+        for (int e = 0; e < dim; ++e) G.iJ[d][e] = d == e ? L.inv_h[d] : T(0);
+      G.jxw = L.det * T(qweight<dim, q>());
+    } else {
+      qgeom<T, dim, q>(L, cell, box, G);
+    }
+    const T eta = eta_q ? eta_q[q] : eta_cell;
+    // real-space gradient row of this component: g[e] = d u_comp / d x_e
+    T g[3] = {T(0), T(0), T(0)};
+    if (need_u) {
+      T gr[3];
+      gr[0] = colloc_d<T, dim, q, 0>(U);
+      gr[1] = colloc_d<T, dim, q, 1>(U);
+      if constexpr (dim == 3) gr[2] = colloc_d<T, dim, q, 2>(U);
+      if (L.geom == GEOM_TABLE) {
+#pragma unroll
+        for (int e = 0; e < dim; ++e) {
+          T t = T(0);
+#pragma unroll
+          for (int d = 0; d < dim; ++d) t += gr[d] * G.iJ[d][e];
+          g[e] = t;
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < dim; ++e) g[e] = gr[e] * G.iJ[e][e];
+      }
+    }
+    T pq = T(0);
+    if constexpr (need_p) {
+      static_for<np>([&](auto nc) {
+        constexpr int n = decltype(nc)::value;
+        pq += T(psi_at<dim, q, n>()) * P[n];
+      });
+    }
+    // flux row F[comp][e] (absolute e)
+    T F[3] = {T(0), T(0), T(0)};
+    if (need_u) {
+      if constexpr (dim == 3) {
+        const int k1 = (comp + 1) % 3, k2 = (comp + 2) % 3;
+        // round 1: receive d_comp u_{comp+1}; round 2: receive d_comp u_{comp+2}
+        const T send1 = sel3(g[0], g[1], g[2], k2);
+        const T send2 = sel3(g[0], g[1], g[2], k1);
+        const T r1 = __shfl_sync(full, send1, l1);
+        const T r2 = __shfl_sync(full, send2, l2);
+        const T gcc = sel3(g[0], g[1], g[2], comp);
+        const T f0 = T(2) * eta * gcc;
+        const T f1 = eta * (sel3(g[0], g[1], g[2], k1) + r1);
+        const T f2 = eta * (sel3(g[0], g[1], g[2], k2) + r2);
+        T fdiag = f0;
+        if (L.compressible) {
+          // d_{c+1} u_{c+1} and d_{c+2} u_{c+2}
+          const T d1 = __shfl_sync(full, gcc, l1);
+          const T d2 = __shfl_sync(full, gcc, l2);
+          fdiag -= T(2) * eta / T(3) * (gcc + d1 + d2);
+        }
+        // absolute e: relative index (e - comp) mod 3
+        F[0] = sel3(fdiag, f1, f2, (3 - comp) % 3);
+        F[1] = sel3(fdiag, f1, f2, (4 - comp) % 3);
+        F[2] = sel3(fdiag, f1, f2, (5 - comp) % 3);
+      } else {
+        const int o = 1 - comp;
+        const T send = comp == 0 ? g[1] : g[0];
+        const T r = __shfl_sync(full, send, lane_base + o);
+        const T gcc = comp == 0 ? g[0] : g[1];
+        T fdiag = T(2) * eta * gcc;
+        if (L.compressible) {
+          const T d1 = __shfl_sync(full, gcc, lane_base + o);
+          fdiag -= T(2) * eta / T(3) * (gcc + d1);
+        }
+        const T foff = eta * ((comp == 0 ? g[1] : g[0]) + r);
+        F[0] = comp == 0 ? fdiag : foff;
+        F[1] = comp == 0 ? foff : fdiag;
+      }
+    }
+    if (need_p) {
+      // -s p on the diagonal entry of this row
+#pragma unroll
+      for (int e = 0; e < dim; ++e)
+        if (e == comp) F[e] -= s * pq;
+    }
+    // reference-direction flux R[d] = JxW sum_e F[e] invJ[d][e]
+    T R[3];
+    if (L.geom == GEOM_TABLE) {
+#pragma unroll
+      for (int d = 0; d < dim; ++d) {
+        T t = T(0);
+#pragma unroll
+        for (int e = 0; e < dim; ++e) t += F[e] * G.iJ[d][e];
+        R[d] = t * G.jxw;
+      }
+    } else {
+#pragma unroll
+      for (int d = 0; d < dim; ++d) R[d] = F[d] * G.iJ[d][d] * G.jxw;
+    }
+    colloc_dT<T, dim, q, 0>(V, R[0]);
+    colloc_dT<T, dim, q, 1>(V, R[1]);
+    if constexpr (dim == 3) colloc_dT<T, dim, q, 2>(V, R[2]);
+    if (op == OPK_STOKES) {
+      // partial divergence of this component: -s JxW d_comp u_comp
+      const T gcc = dim == 3 ? sel3(g[0], g[1], g[2], comp) : (comp == 0 ? g[0] : g[1]);
+      const T f = -s * G.jxw * gcc;
+#pragma unroll
+      static_for<np>([&](auto nc) {
+        constexpr int n = decltype(nc)::value;
+        YP[n] += T(psi_at<dim, q, n>()) * f;
+      });
+    }
+  });
+  interpolate<T, dim, true>(V);
+  (void)lane_base;
+}
+
+// ---------------------------------------------------------------------------
+// Operator application in two passes, both over the whole level:
+//   pass 1 (one thread group per cell, all cells in one launch): the cell's
+//          contributions to its own local DoFs, stored per cell (Eu, Ep);
+//   pass 2 (one thread per DoF): each DoF sums the contributions of its cells in a
+//          fixed order (lattice arithmetic, or a CSR list that also folds in the
+//          constraint lines) and applies a fused epilogue (plain store,
+//          Chebyshev update or residual).
+// No colouring, no atomics: one launch per pass keeps every SM busy and the sum
+// order is fixed, so results are bit-reproducible.
+
+template <typename T, int dim>
+__device__ __forceinline__ void structured_cell_lex(const LevelView<T>& L, int cell, StructuredCell<T, dim>& sc) {
+  sc.i = cell % L.nc[0];
+  sc.j = (cell / L.nc[0]) % L.nc[1];
+  sc.k = dim == 3 ? cell / (L.nc[0] * L.nc[1]) : 0;
+  sc.node0 = (2 * sc.k * L.Nn[1] + 2 * sc.j) * L.Nn[0] + 2 * sc.i;
+  sc.pnode0 = (sc.k * L.Np[1] + sc.j) * L.Np[0] + sc.i;
+}
+
+template <typename T, int dim, int op>
+__global__ void __launch_bounds__(128) velocity_cell_kernel(LevelView<T> L, const T* __restrict__ src_u,
+                                                             const T* __restrict__ src_p, T* __restrict__ Eu,
+                                                             T* __restrict__ Ep) {
+  constexpr int nv = Shape<dim>::nv, np = Shape<dim>::np, cpw = Shape<dim>::cpw;
+  constexpr bool need_u = (op == OPK_STOKES || op == OPK_A);
+  constexpr bool need_p = (op == OPK_STOKES || op == OPK_BT);
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int grp = lane / dim;
+  int comp = lane - grp * dim;
+  bool active = grp < cpw;
+  if (!active) { grp = cpw - 1; comp = 0; }
+  const unsigned lane_base = grp * dim;
+  const int idx = warp * cpw + grp;
+  active = active && idx < L.n_cells;
+  const int cell = active ? idx : 0;
+  StructuredCell<T, dim> sc{};
+  if (L.structured) structured_cell_lex<T, dim>(L, cell, sc);
+
+  T U[nv], V[nv], P[np], YP[np];
+  T box[4] = {T(0), T(0), T(0), T(0)};
+  if (L.geom == GEOM_BOX && active)
+#pragma unroll
+    for (int d = 0; d <= dim; ++d) box[d] = L.gbox[(size_t)cell * (dim + 1) + d];
+  if (need_u) {
+#pragma unroll
+    for (int n = 0; n < nv; ++n) {
+      T v = T(0);
+      if (active) {
+        if (L.structured) {
+          if (!structured_zero<T, dim>(L, sc, comp, n))
+            v = src_u[comp * L.n_nodes + sc.node0 + structured_node_offset<dim>(L.Nn, n)];
+        } else {
+          v = gather_general(src_u, L.cdu[(size_t)cell * dim * nv + comp * nv + n], L.lptr, L.lcol, L.lw);
+        }
+      }
+      U[n] = v;
+    }
+  }
+  if (need_p) {
+#pragma unroll
+    for (int n = 0; n < np; ++n) {
+      T v = T(0);
+      if (active) {
+        if (L.structured) v = src_p[sc.pnode0 + structured_pnode_offset<dim>(L.Np, n)];
+        else v = gather_general(src_p, L.cdp[(size_t)cell * np + n], L.plptr, L.plcol, L.plw);
+      }
+      P[n] = v;
+    }
+  }
+  T eta_cell = T(1);
+  const T* eta_q = nullptr;
+  if (op != OPK_BT && active) {
+    if (L.eta_n == 1) eta_cell = L.eta[cell];
+    else eta_q = L.eta + (size_t)cell * L.eta_n;
+  }
+  velocity_cell_op<T, dim, op>(L, cell, comp, lane_base, U, P, V, YP, box, eta_cell, eta_q);
+  if (active) {
+    T* e = Eu + ((size_t)cell * dim + comp) * nv;
+#pragma unroll
+    for (int n = 0; n < nv; ++n) e[n] = V[n];
+  }
+  if (op == OPK_STOKES) {
+    const unsigned full = 0xffffffffu;
+#pragma unroll
+    for (int n = 0; n < np; ++n) {
+      const T v = YP[n];
+      T t = v;
+#pragma unroll
+      for (int o = 1; o < dim; ++o) t += __shfl_sync(full, v, lane_base + (comp + o) % dim);
+      YP[n] = t;
+    }
+    if (active) {
+#pragma unroll
+      for (int n = 0; n < np; ++n)
+        if (n % dim == comp) Ep[(size_t)cell * np + n] = YP[n];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pressure mass operator: one thread per cell.
+template <typename T, int dim>
+__device__ __forceinline__ void mass_cell_op(const LevelView<T>& L, int cell, const T* P, T* YP, const T* box,
+                                             T eta_cell, const T* __restrict__ eta_q) {
+  constexpr int np = Shape<dim>::np, nq = Shape<dim>::nq;
+  const T s2 = L.s * L.s;
+#pragma unroll
+  for (int n = 0; n < np; ++n) YP[n] = T(0);
+  static_for<nq>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    T jxw;
+    if (L.geom == GEOM_CART) jxw = L.det * T(qweight<dim, q>());
+    else if (L.geom == GEOM_BOX) jxw = box[dim] * T(qweight<dim, q>());
+    else jxw = L.gtab[((size_t)cell * nq + q) * (dim * dim + 1) + dim * dim] * T(qweight<dim, q>());
+    const T eta = eta_q ? eta_q[q] : eta_cell;
+    T pq = T(0);
+    static_for<np>([&](auto nc) {
+      constexpr int n = decltype(nc)::value;
+      pq += T(psi_at<dim, q, n>()) * P[n];
+    });
+    const T f = s2 / eta * pq * jxw;
+    static_for<np>([&](auto nc) {
+      constexpr int n = decltype(nc)::value;
+      YP[n] += T(psi_at<dim, q, n>()) * f;
+    });
+  });
+}
+
+template <typename T, int dim>
+__global__ void __launch_bounds__(128) mass_cell_kernel(LevelView<T> L, const T* __restrict__ src_p,
+                                                         T* __restrict__ Ep) {
+  constexpr int np = Shape<dim>::np;
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= L.n_cells) return;
+  StructuredCell<T, dim> sc{};
+  if (L.structured) structured_cell_lex<T, dim>(L, cell, sc);
+  T P[np], YP[np];
+#pragma unroll
+  for (int n = 0; n < np; ++n)
+    P[n] = L.structured ? src_p[sc.pnode0 + structured_pnode_offset<dim>(L.Np, n)]
+                        : gather_general(src_p, L.cdp[(size_t)cell * np + n], L.plptr, L.plcol, L.plw);
+  T box[4] = {T(0), T(0), T(0), T(0)};
+  if (L.geom == GEOM_BOX)
+#pragma unroll
+    for (int d = 0; d <= dim; ++d) box[d] = L.gbox[(size_t)cell * (dim + 1) + d];
+  const T eta_cell = L.eta_n == 1 ? L.eta[cell] : T(1);
+  const T* eta_q = L.eta_n == 1 ? nullptr : L.eta + (size_t)cell * L.eta_n;
+  mass_cell_op<T, dim>(L, cell, P, YP, box, eta_cell, eta_q);
+#pragma unroll
+  for (int n = 0; n < np; ++n) Ep[(size_t)cell * np + n] = YP[n];
+}
+
+// ---------------------------------------------------------------------------
+// Pass 2: per-DoF gather with a fused epilogue.
+enum Epilogue {
+  EPI_STORE = 0,  // y = K x; constrained rows y = x
+  EPI_BT = 1,     // y = B^T p; constrained velocity rows y = 0
+  EPI_RESID = 2,  // y = b - K x; constrained rows y = b - x
+  EPI_CHEB = 3    // t = K x; d = f1 d + f2 dinv (b - t); x += d (x updated in place)
+};
+
+template <typename T>
+struct GatherArgs {
+  const T* E;      // per-cell contributions
+  T* x;            // operator input (identity rows; updated by EPI_CHEB)
+  T* y;            // output (EPI_STORE / EPI_BT / EPI_RESID)
+  const T* b;      // right-hand side (EPI_RESID / EPI_CHEB)
+  const T* dinv;   // inverse diagonal (EPI_CHEB)
+  T* d;            // Chebyshev update vector (EPI_CHEB)
+  T f1, f2;
+};
+
+// General levels: CSR of (cell-local slot, weight) per DoF, built at set-up
+// with the constraint lines folded in; cmask marks constrained DoFs.
+template <typename T>
+struct GatherCsr {
+  const int* ptr;
+  const int* slot;
+  const T* w;
+  const unsigned char* cmask;
+};
+
+template <typename T, int epi>
+__device__ __forceinline__ void gather_epilogue(const GatherArgs<T>& a, long g, T sum, bool constrained) {
+  if (epi == EPI_STORE) {
+    a.y[g] = constrained ? a.x[g] : sum;
+  } else if (epi == EPI_BT) {
+    a.y[g] = constrained ? T(0) : sum;
+  } else if (epi == EPI_RESID) {
+    a.y[g] = a.b[g] - (constrained ? a.x[g] : sum);
+  } else {
+    const T xg = a.x[g];
+    const T t = constrained ? xg : sum;
+    const T dn = a.f1 * a.d[g] + a.f2 * a.dinv[g] * (a.b[g] - t);
+    a.d[g] = dn;
+    a.x[g] = xg + dn;
+  }
+}
+
+// Velocity DoFs of a lattice level: a node's cells follow from its coordinates.
+template <typename T, int dim, int epi>
+__global__ void __launch_bounds__(256) velocity_gather_structured(LevelView<T> L, GatherArgs<T> a) {
+  constexpr int nv = Shape<dim>::nv;
+  const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (g >= L.n_u) return;
+  const int comp = (int)(g / L.n_nodes);
+  const int node = (int)(g - (long)comp * L.n_nodes);
+  const int gc[3] = {node % L.Nn[0], (node / L.Nn[0]) % L.Nn[1], dim == 3 ? node / (L.Nn[0] * L.Nn[1]) : 0};
+  int cidx[3][2], loc[3][2], cnt[3];
+  bool constrained = false;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    cnt[d] = 0;
+    if (d >= dim) { cnt[d] = 1; cidx[d][0] = 0; loc[d][0] = 0; continue; }
+    const int x = gc[d];
+    if (x & 1) {
+      cidx[d][0] = (x - 1) >> 1; loc[d][0] = 1; cnt[d] = 1;
+    } else {
+      if (x > 0) { cidx[d][cnt[d]] = (x >> 1) - 1; loc[d][cnt[d]] = 2; ++cnt[d]; }
+      if (x < L.Nn[d] - 1) { cidx[d][cnt[d]] = x >> 1; loc[d][cnt[d]] = 0; ++cnt[d]; }
+    }
+    if (x == 0 && ((L.zero_faces >> ((2 * d) * 3 + comp)) & 1u)) constrained = true;
+    if (x == L.Nn[d] - 1 && ((L.zero_faces >> ((2 * d + 1) * 3 + comp)) & 1u)) constrained = true;
+  }
+  T sum = T(0);
+  if (!constrained) {
+    for (int kz = 0; kz < cnt[2]; ++kz)
+      for (int ky = 0; ky < cnt[1]; ++ky)
+        for (int kx = 0; kx < cnt[0]; ++kx) {
+          const int cell = (cidx[2][kz] * L.nc[1] + cidx[1][ky]) * L.nc[0] + cidx[0][kx];
+          const int l = loc[0][kx] + 3 * loc[1][ky] + 9 * loc[2][kz];
+          sum += a.E[((size_t)cell * dim + comp) * nv + l];
+        }
+  }
+  gather_epilogue<T, epi>(a, g, sum, constrained);
+}
+
+// Pressure DoFs of a lattice level (never constrained there).
+template <typename T, int dim, int epi>
+__global__ void __launch_bounds__(256) pressure_gather_structured(LevelView<T> L, GatherArgs<T> a) {
+  constexpr int np = Shape<dim>::np;
+  const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (g >= L.n_p) return;
+  const int node = (int)g;
+  const int gc[3] = {node % L.Np[0], (node / L.Np[0]) % L.Np[1], dim == 3 ? node / (L.Np[0] * L.Np[1]) : 0};
+  int cidx[3][2], loc[3][2], cnt[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    cnt[d] = 0;
+    if (d >= dim) { cnt[d] = 1; cidx[d][0] = 0; loc[d][0] = 0; continue; }
+    const int x = gc[d];
+    if (x > 0) { cidx[d][cnt[d]] = x - 1; loc[d][cnt[d]] = 1; ++cnt[d]; }
+    if (x < L.Np[d] - 1) { cidx[d][cnt[d]] = x; loc[d][cnt[d]] = 0; ++cnt[d]; }
+  }
+  T sum = T(0);
+  for (int kz = 0; kz < cnt[2]; ++kz)
+    for (int ky = 0; ky < cnt[1]; ++ky)
+      for (int kx = 0; kx < cnt[0]; ++kx) {
+        const int cell = (cidx[2][kz] * L.nc[1] + cidx[1][ky]) * L.nc[0] + cidx[0][kx];
+        const int l = loc[0][kx] + 2 * loc[1][ky] + 4 * loc[2][kz];
+        sum += a.E[(size_t)cell * np + l];
+      }
+  gather_epilogue<T, epi>(a, g, sum, false);
+}
+
+template <typename T, int epi>
+__global__ void __launch_bounds__(256) gather_csr(long n, GatherCsr<T> G, GatherArgs<T> a) {
+  const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  const bool constrained = G.cmask[g] != 0;
+  T sum = T(0);
+  if (!constrained)
+    for (int k = G.ptr[g]; k < G.ptr[g + 1]; ++k) sum += G.w[k] * a.E[G.slot[k]];
+  gather_epilogue<T, epi>(a, g, sum, constrained);
+}
+
+// ---------------------------------------------------------------------------
+// Diagonals (MatrixFreeTools::compute_diagonal semantics): for every global DoF
+// g touched by a cell, v = local expansion of e_g, diag[g] += v . (K_cell v).
+// General levels use per-cell probe lists: probe k = (global dof, entries
+// (local index, weight)). Structured levels probe each unconstrained local DoF.
+template <typename T, int dim>
+__global__ void __launch_bounds__(128) velocity_diag_kernel(LevelView<T> L, int colour, int colour_begin,
+                                                             int colour_count, const int* __restrict__ probe_ptr,
+                                                             const int* __restrict__ probe_g,
+                                                             const int* __restrict__ probe_eptr,
+                                                             const int* __restrict__ probe_li,
+                                                             const T* __restrict__ probe_w, T* __restrict__ diag) {
+  constexpr int nv = Shape<dim>::nv, cpw = Shape<dim>::cpw;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int grp = lane / dim;
+  int comp = lane - grp * dim;
+  bool active = grp < cpw;
+  if (!active) { grp = cpw - 1; comp = 0; }
+  const unsigned lane_base = grp * dim;
+  const int idx = warp * cpw + grp;
+  active = active && idx < colour_count;
+  int cell = 0;
+  StructuredCell<T, dim> sc{};
+  if (L.structured) {
+    bool v;
+    structured_cell<T, dim>(L, colour, active ? idx : 0, cell, sc, v);
+    active = active && v;
+  } else {
+    cell = colour_begin + (active ? idx : 0);
+  }
+  T box[4] = {T(0), T(0), T(0), T(0)};
+  if (L.geom == GEOM_BOX && active)
+#pragma unroll
+    for (int d = 0; d <= dim; ++d) box[d] = L.gbox[(size_t)cell * (dim + 1) + d];
+  T eta_cell = T(1);
+  const T* eta_q = nullptr;
+  if (active) {
+    if (L.eta_n == 1) eta_cell = L.eta[cell];
+    else eta_q = L.eta + (size_t)cell * L.eta_n;
+  }
+  // number of probes is uniform within a warp only for structured levels; loop to
+  // the maximum over the warp so that every lane takes part in the shuffles
+  int my_probes = 0, p0 = 0;
+  if (L.structured) my_probes = dim * nv;
+  else if (active) { p0 = probe_ptr[cell]; my_probes = probe_ptr[cell + 1] - p0; }
+  int max_probes = my_probes;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) max_probes = max(max_probes, __shfl_xor_sync(0xffffffffu, max_probes, o));
+  for (int k = 0; k < max_probes; ++k) {
+    T U[nv], V[nv];
+    bool probe_ok = active && k < my_probes;
+    int target = -1;
+#pragma unroll
+    for (int n = 0; n < nv; ++n) U[n] = T(0);
+    if (probe_ok) {
+      if (L.structured) {
+        const int pc = k / nv, pn = k % nv;
+        if (structured_zero<T, dim>(L, sc, pc, pn)) probe_ok = false;
+        else {
+#pragma unroll
+          for (int n = 0; n < nv; ++n) U[n] = (pc == comp && pn == n) ? T(1) : T(0);
+          target = pc * L.n_nodes + sc.node0 + structured_node_offset<dim>(L.Nn, pn);
+        }
+      } else {
+        target = probe_g[p0 + k];
+        for (int e = probe_eptr[p0 + k]; e < probe_eptr[p0 + k + 1]; ++e) {
+          const int li = probe_li[e];
+          const T w = probe_w[e];
+#pragma unroll
+          for (int n = 0; n < nv; ++n)
+            if (li == comp * nv + n) U[n] += w;
+        }
+      }
+    }
+    T Uc[nv];
+#pragma unroll
+    for (int n = 0; n < nv; ++n) Uc[n] = U[n];
+    velocity_cell_op<T, dim, OPK_A>(L, cell, comp, lane_base, U, nullptr, V, nullptr, box, eta_cell, eta_q);
+    T part = T(0);
+#pragma unroll
+    for (int n = 0; n < nv; ++n) part += Uc[n] * V[n];
+    T tot = part;
+#pragma unroll
+    for (int o = 1; o < dim; ++o) tot += __shfl_sync(0xffffffffu, part, lane_base + (comp + o) % dim);
+    // all probes of structured levels have one owner thread (component pc)
+    const bool owner = L.structured ? (k / nv == comp) : (comp == 0);
+    if (probe_ok && owner && target >= 0) diag[target] += tot;
+  }
+}
+
+template <typename T, int dim>
+__global__ void __launch_bounds__(128) mass_diag_kernel(LevelView<T> L, int colour, int colour_begin,
+                                                         int colour_count, const int* __restrict__ probe_ptr,
+                                                         const int* __restrict__ probe_g,
+                                                         const int* __restrict__ probe_eptr,
+                                                         const int* __restrict__ probe_li,
+                                                         const T* __restrict__ probe_w, T* __restrict__ diag) {
+  constexpr int np = Shape<dim>::np;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= colour_count) return;
+  int cell;
+  StructuredCell<T, dim> sc{};
+  if (L.structured) {
+    bool v;
+    structured_cell<T, dim>(L, colour, idx, cell, sc, v);
+    if (!v) return;
+  } else {
+    cell = colour_begin + idx;
+  }
+  T box[4] = {T(0), T(0), T(0), T(0)};
+  if (L.geom == GEOM_BOX)
+#pragma unroll
+    for (int d = 0; d <= dim; ++d) box[d] = L.gbox[(size_t)cell * (dim + 1) + d];
+  const T eta_cell = L.eta_n == 1 ? L.eta[cell] : T(1);
+  const T* eta_q = L.eta_n == 1 ? nullptr : L.eta + (size_t)cell * L.eta_n;
+  int n_probes = L.structured ? np : probe_ptr[cell + 1] - probe_ptr[cell];
+  const int p0 = L.structured ? 0 : probe_ptr[cell];
+  for (int k = 0; k < n_probes; ++k) {
+    T P[np], YP[np];
+    int target;
+#pragma unroll
+    for (int n = 0; n < np; ++n) P[n] = T(0);
+    if (L.structured) {
+#pragma unroll
+      for (int n = 0; n < np; ++n) P[n] = n == k ? T(1) : T(0);
+      target = sc.pnode0 + structured_pnode_offset<dim>(L.Np, k);
+    } else {
+      target = probe_g[p0 + k];
+      for (int e = probe_eptr[p0 + k]; e < probe_eptr[p0 + k + 1]; ++e) {
+        const int li = probe_li[e];
+#pragma unroll
+        for (int n = 0; n < np; ++n)
+          if (li == n) P[n] += probe_w[e];
+      }
+    }
+    mass_cell_op<T, dim>(L, cell, P, YP, box, eta_cell, eta_q);
+    T tot = T(0);
+#pragma unroll
+    for (int n = 0; n < np; ++n) tot += P[n] * YP[n];
+    diag[target] += tot;
+  }
+}
+
+}  // namespace gb

@@ -1,0 +1,1326 @@
+// GB300 matrix-free GMG Stokes solver: operators, V-cycle, block
+// preconditioner, Krylov solvers and the C ABI of include/gb_gmg.h.
+//
+// Solver composition follows source/simulator/solver/stokes_matrix_free_local_smoothing.cc:
+//   smoothers / coarse solve     :774-861 (Chebyshev degree 4, range 15, 10
+//                                  eigenvalue-CG steps on levels > 0; degree 8,
+//                                  range 1e-3, 100 steps on level 0; 4 Schur
+//                                  smoothing steps; coarse = one smoother apply)
+//   V-cycle / PreconditionMG     :896-916 (deal.II Multigrid: pre-smoothing from
+//                                  zero, residual, restrict, recurse,
+//                                  prolongate, post-smoothing)
+//   initial residual, tolerance  :977-1041
+//   cheap GMRES, FGMRES fallback :1262-1397
+// and include/aspect/simulator/solver/block_stokes_preconditioner.h:101-352.
+// Everything runs on one GPU; the V-cycle runs in FP32 or FP64, the Krylov
+// solver, the Stokes residual and the Schur update in FP64.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/gb_gmg.h"
+#include "level.cuh"
+
+namespace gb {
+
+void launch_adjoint_gradient_impl(const LevelView<double>& L, int colour, int begin, int count, const double* u,
+                                  const double* lam, double* grad, cudaStream_t s);
+
+struct Handle {
+  gb_gmg_options opt{};
+  int dim = 3, n_levels = 0;
+  std::vector<Level> levels;
+  cudaStream_t st = nullptr;
+  std::string err;
+  double s = 1.0;
+  int compressible = 0, projection = 0;
+  double eta_min = 0, eta_max = 0;
+  bool setup_done = false, visc_done = false;
+  bool prec_done[2] = {false, false};  // per precision (0 fp64, 1 fp32)
+  long long cell_launches = 0;
+  // staging and FP64 active-level workspace
+  DevBuf<double> stage_a, stage_b, partial, dots_d;
+  double* dots_h = nullptr;
+  DevBuf<double> V, Z, wv, xv, rv, bv, tv, t2v, coef_d;
+  DevBuf<double> cg_r, cg_z, cg_p, cg_q, cg_x;
+  DevBuf<float> f32_a, f32_b;
+  int restart_alloc = -1;
+  int nA = 0, nS = 0, n_stokes64 = 0;
+  int* flag_d = nullptr;
+  // captured V-cycles [block][precision 0 fp64 / 1 fp32] and their staging vectors
+  cudaGraphExec_t vgraph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+  long long vgraph_kernels[2][2] = {{0, 0}, {0, 0}};
+  DevBuf<double> vin, vout;
+
+  Level& top() { return levels.back(); }
+  void reset_graphs() {
+    for (auto& r : vgraph)
+      for (auto& g : r)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+  }
+  long n_top() { return top().n_u + top().n_p; }
+};
+
+namespace {
+
+// ---------------------------------------------------------------- tridiagonal eigenvalues
+void tridiag_eigs(std::vector<double> d, std::vector<double> e, double& lmin, double& lmax) {
+  const int n = (int)d.size();
+  if (n == 0) { lmin = lmax = 0; return; }
+  e.resize(n, 0.0);
+  for (int l = 0; l < n; ++l) {
+    int iter = 0, m;
+    do {
+      for (m = l; m < n - 1; ++m) {
+        const double dd = std::fabs(d[m]) + std::fabs(d[m + 1]);
+        if (std::fabs(e[m]) <= 1e-15 * dd) break;
+      }
+      if (m != l) {
+        if (iter++ == 200) break;
+        double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+        double r = std::hypot(g, 1.0);
+        g = d[m] - d[l] + e[l] / (g + (g >= 0 ? std::fabs(r) : -std::fabs(r)));
+        double s_ = 1, c = 1, p = 0;
+        int i;
+        for (i = m - 1; i >= l; --i) {
+          const double f = s_ * e[i], b = c * e[i];
+          r = std::hypot(f, g);
+          e[i + 1] = r;
+          if (r == 0.0) { d[i + 1] -= p; e[m] = 0.0; break; }
+          s_ = f / r; c = g / r; g = d[i + 1] - p; r = (d[i] - g) * s_ + 2.0 * c * b;
+          p = s_ * r; d[i + 1] = g + p; g = c * r - b;
+        }
+        if (r == 0.0 && i >= l) continue;
+        d[l] -= p; e[l] = g; e[m] = 0.0;
+      }
+    } while (m != l);
+  }
+  lmin = *std::min_element(d.begin(), d.end());
+  lmax = *std::max_element(d.begin(), d.end());
+}
+
+double dot_host(Handle& H, long n, const double* a, const double* b) {
+  v_dot<double>(n, a, b, H.dots_d.p, H.partial.p, H.st);
+  GB_CUDA(cudaMemcpyAsync(H.dots_h, H.dots_d.p, sizeof(double), cudaMemcpyDeviceToHost, H.st));
+  GB_CUDA(cudaStreamSynchronize(H.st));
+  return H.dots_h[0];
+}
+template <typename T>
+double dot_host_T(Handle& H, long n, const T* a, const T* b) {
+  v_dot<T>(n, a, b, H.dots_d.p, H.partial.p, H.st);
+  GB_CUDA(cudaMemcpyAsync(H.dots_h, H.dots_d.p, sizeof(double), cudaMemcpyDeviceToHost, H.st));
+  GB_CUDA(cudaStreamSynchronize(H.st));
+  return H.dots_h[0];
+}
+
+// ---------------------------------------------------------------- operators
+template <typename T>
+void gather(Handle& H, Level& L, const LevelView<T>& v, int block, int epi, const GatherArgs<T>& a) {
+  GatherCsr<T> csr;
+  const GatherCsr<T>* pc = nullptr;
+  if (!L.structured) {
+    csr = L.csr<T>(block);
+    pc = &csr;
+  }
+  launch_gather<T>(v, block, epi, pc, a, H.st);
+  ++H.cell_launches;
+}
+
+// y = op(x) on a level; constrained rows act as the identity (zero for B^T)
+template <typename T>
+void apply_op(Handle& H, int lev, int op, const T* su, const T* sp, T* du, T* dp) {
+  Level& L = H.levels[lev];
+  LevelDev<T>& D = L.dev<T>();
+  const LevelView<T> v = L.view<T>(H.s, H.compressible);
+  launch_cell_pass<T>(v, op, su, sp, D.Eu.p, D.Ep.p, H.st);
+  ++H.cell_launches;
+  if (op == OPK_STOKES || op == OPK_A || op == OPK_BT) {
+    GatherArgs<T> a{};
+    a.E = D.Eu.p;
+    a.x = const_cast<T*>(su);
+    a.y = du;
+    gather<T>(H, L, v, 0, op == OPK_BT ? EPI_BT : EPI_STORE, a);
+  }
+  if (op == OPK_STOKES || op == OPK_MASS) {
+    GatherArgs<T> a{};
+    a.E = D.Ep.p;
+    a.x = const_cast<T*>(sp);
+    a.y = dp;
+    gather<T>(H, L, v, 1, EPI_STORE, a);
+  }
+}
+
+template <typename T>
+void level_op(Handle& H, int lev, int block, const T* x, T* y) {
+  if (block == 0) apply_op<T>(H, lev, OPK_A, x, nullptr, y, nullptr);
+  else apply_op<T>(H, lev, OPK_MASS, nullptr, x, nullptr, y);
+}
+
+// Chebyshev step fused into the gather: t = K x; d = f1 d + f2 D^-1 (b - t); x += d
+template <typename T>
+void level_op_cheb(Handle& H, int lev, int block, T* x, const T* b, const T* dinv, T* d, double f1, double f2) {
+  Level& L = H.levels[lev];
+  LevelDev<T>& D = L.dev<T>();
+  const LevelView<T> v = L.view<T>(H.s, H.compressible);
+  launch_cell_pass<T>(v, block == 0 ? OPK_A : OPK_MASS, x, x, D.Eu.p, D.Ep.p, H.st);
+  ++H.cell_launches;
+  GatherArgs<T> a{};
+  a.E = block == 0 ? D.Eu.p : D.Ep.p;
+  a.x = x;
+  a.b = b;
+  a.dinv = dinv;
+  a.d = d;
+  a.f1 = (T)f1;
+  a.f2 = (T)f2;
+  gather<T>(H, L, v, block, EPI_CHEB, a);
+}
+
+// residual fused into the gather: y = b - K x
+template <typename T>
+void level_op_resid(Handle& H, int lev, int block, const T* x, const T* b, T* y) {
+  Level& L = H.levels[lev];
+  LevelDev<T>& D = L.dev<T>();
+  const LevelView<T> v = L.view<T>(H.s, H.compressible);
+  launch_cell_pass<T>(v, block == 0 ? OPK_A : OPK_MASS, x, x, D.Eu.p, D.Ep.p, H.st);
+  ++H.cell_launches;
+  GatherArgs<T> a{};
+  a.E = block == 0 ? D.Eu.p : D.Ep.p;
+  a.x = const_cast<T*>(x);
+  a.y = y;
+  a.b = b;
+  gather<T>(H, L, v, block, EPI_RESID, a);
+}
+
+// ---------------------------------------------------------------- diagonals
+template <typename T>
+void compute_diagonals(Handle& H, int lev) {
+  Level& L = H.levels[lev];
+  LevelDev<T>& D = L.dev<T>();
+  const LevelView<T> v = L.view<T>(H.s, H.compressible);
+  D.dinvA.alloc(L.n_u);
+  D.dinvM.alloc(L.n_p);
+  D.dinvA.zero(H.st);
+  D.dinvM.zero(H.st);
+  ProbesView<T> pu{L.probe_ptr.p, L.probe_g.p, L.probe_eptr.p, L.probe_li.p, D.probe_w.p};
+  ProbesView<T> pp{L.pprobe_ptr.p, L.pprobe_g.p, L.pprobe_eptr.p, L.pprobe_li.p, D.pprobe_w.p};
+  for (int k = 0; k < L.n_colours; ++k) {
+    const int cnt = L.colour_count[k];
+    if (!cnt) continue;
+    const int begin = L.structured ? 0 : L.colour_begin[k];
+    launch_velocity_diag<T>(v, k, begin, cnt, pu, D.dinvA.p, H.st);
+    launch_mass_diag<T>(v, k, begin, cnt, pp, D.dinvM.p, H.st);
+    H.cell_launches += 2;
+  }
+  GB_CUDA(cudaStreamSynchronize(H.st));
+  for (int block = 0; block < 2; ++block) {
+    DevBuf<T>& buf = block == 0 ? D.dinvA : D.dinvM;
+    std::vector<T> d = buf.download();
+    const std::vector<int>& cons = block == 0 ? L.cons_u : L.cons_p;
+    for (int c : cons) d[c] = T(1);
+    for (size_t i = 0; i < d.size(); ++i) {
+      GB_CHECK(d[i] > T(0) && std::isfinite((double)d[i]), 6,
+               "No diagonal entry in a positive definite operator should be zero or negative.");
+      d[i] = T(1) / d[i];
+    }
+    buf.upload(d);
+  }
+}
+
+// ---------------------------------------------------------------- Chebyshev smoother
+struct ChebParams {
+  int degree, eig_its;
+  double range;
+};
+ChebParams cheb_params(const Handle& H, int lev) {
+  if (lev > 0) return {H.opt.smoother_degree, H.opt.eig_cg_iterations, H.opt.smoothing_range};
+  return {H.opt.coarse_degree, H.opt.coarse_eig_cg_iterations, H.opt.coarse_range};
+}
+
+template <typename T>
+void estimate_eigenvalues(Handle& H, int lev, int block) {
+  Level& L = H.levels[lev];
+  LevelDev<T>& D = L.dev<T>();
+  if (D.eig_given[block]) return;
+  const long n = block == 0 ? L.n_u : L.n_p;
+  const HostCons& C = block == 0 ? L.cu : L.cp;
+  const std::vector<int>& perm = block == 0 ? L.perm_u : L.perm_p;
+  const ChebParams cp = cheb_params(H, lev);
+  // PreconditionChebyshev's start vector: a period-11 mode (i mod 11, caller
+  // numbering) with its mean removed, over all entries. The pressure mass
+  // matrix has no null space and its largest eigenvector on small coarse levels
+  // is the constant mode, so for block 1 the mean is kept (else the Lanczos
+  // estimate misses that eigenvalue and the Chebyshev polynomial amplifies it).
+  std::vector<T> b(n, T(0));
+  double mean = 0;
+  if (block == 0) {
+    for (long i = 0; i < n; ++i) mean += (double)(i % 11);
+    mean /= std::max(n, 1L);
+  }
+  for (long i = 0; i < n; ++i) b[perm[i]] = (T)((double)(i % 11) - mean);
+  (void)C;
+  // use the level's work vectors: r = def, z = sol, p = d, Ap = t
+  T* r = block == 0 ? D.defA.p : D.defM.p;
+  T* z = block == 0 ? D.solA.p : D.solM.p;
+  T* p = block == 0 ? D.dA.p : D.dM.p;
+  T* Ap = block == 0 ? D.tA.p : D.tM.p;
+  const T* dinv = block == 0 ? D.dinvA.p : D.dinvM.p;
+  GB_CUDA(cudaMemcpyAsync(r, b.data(), n * sizeof(T), cudaMemcpyHostToDevice, H.st));
+  // z = D^-1 r ; p = z
+  v_cheb_first<T>(n, r, dinv, T(1), p, z, H.st);
+  double rz = dot_host_T<T>(H, n, r, z);
+  std::vector<double> alphas, betas;
+  for (int it = 0; it < cp.eig_its; ++it) {
+    level_op<T>(H, lev, block, p, Ap);
+    const double pAp = dot_host_T<T>(H, n, p, Ap);
+    if (!(pAp > 0)) break;
+    const double alpha = rz / pAp;
+    alphas.push_back(alpha);
+    v_axpby<T>(n, (T)(-alpha), Ap, T(1), r, H.st);  // r -= alpha Ap
+    // SolverControl(eig_cg_n_iterations, eig_cg_residual = 1e-2), absolute
+    if (std::sqrt(dot_host_T<T>(H, n, r, r)) < 1e-2) break;
+    v_cheb_first<T>(n, r, dinv, T(1), Ap, z, H.st);  // z = D^-1 r (Ap used as scratch)
+    const double rz_new = dot_host_T<T>(H, n, r, z);
+    const double beta = rz_new / rz;
+    betas.push_back(beta);
+    rz = rz_new;
+    v_axpby<T>(n, T(1), z, (T)beta, p, H.st);  // p = z + beta p
+  }
+  const int k = (int)alphas.size();
+  std::vector<double> dd(k), ee(k, 0.0);
+  for (int i = 0; i < k; ++i) {
+    dd[i] = 1.0 / alphas[i] + (i > 0 ? betas[i - 1] / alphas[i - 1] : 0.0);
+    if (i + 1 < k) ee[i] = std::sqrt(betas[i]) / alphas[i];
+  }
+  double* eig = block == 0 ? D.eigA : D.eigM;
+  tridiag_eigs(dd, ee, eig[0], eig[1]);
+  // leave the work vectors clean (the smoother relies on finite values)
+  GB_CUDA(cudaMemsetAsync(z, 0, n * sizeof(T), H.st));
+  GB_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), H.st));
+}
+
+template <typename T>
+void chebyshev_bounds(Handle& H, int lev, int block, double& theta, double& delta) {
+  LevelDev<T>& D = H.levels[lev].dev<T>();
+  const double* eig = block == 0 ? D.eigA : D.eigM;
+  const ChebParams cp = cheb_params(H, lev);
+  // a level without unconstrained DoFs has no spectrum; any positive bound is inert there
+  const double emax = eig[1] > 0 ? eig[1] : 1.0;
+  const double emin = eig[1] > 0 ? eig[0] : 1.0;
+  const double lmax = 1.2 * emax;
+  const double alpha = cp.range > 1.0 ? lmax / cp.range : std::min(0.9 * lmax, emin);
+  theta = 0.5 * (lmax + alpha);
+  delta = 0.5 * (lmax - alpha);
+}
+
+// x = Cheb(b) from zero (zero_start) or one step from x (PreconditionChebyshev vmult / step)
+template <typename T>
+void chebyshev(Handle& H, int lev, int block, T* x, const T* b, bool zero_start) {
+  Level& L = H.levels[lev];
+  LevelDev<T>& D = L.dev<T>();
+  const long n = block == 0 ? L.n_u : L.n_p;
+  const ChebParams cp = cheb_params(H, lev);
+  double theta, delta;
+  chebyshev_bounds<T>(H, lev, block, theta, delta);
+  const T* dinv = block == 0 ? D.dinvA.p : D.dinvM.p;
+  T* d = block == 0 ? D.dA.p : D.dM.p;
+  T* t = block == 0 ? D.tA.p : D.tM.p;
+  if (zero_start) {
+    v_cheb_first<T>(n, b, dinv, (T)(1.0 / theta), d, x, H.st);
+  } else {
+    level_op_cheb<T>(H, lev, block, x, b, dinv, d, 0.0, 1.0 / theta);
+  }
+  double rhok = delta / theta;
+  const double sigma = theta / delta;
+  for (int k = 1; k < cp.degree; ++k) {
+    const double rhokp = 1.0 / (2.0 * sigma - rhok);
+    const double f1 = rhokp * rhok, f2 = 2.0 * rhokp / delta;
+    rhok = rhokp;
+    level_op_cheb<T>(H, lev, block, x, b, dinv, d, f1, f2);
+  }
+  (void)t;
+}
+
+int smoothing_steps(const Handle& H, int block) { return block == 0 ? 1 : H.opt.schur_smoothing_steps; }
+
+template <typename T>
+void smoother_apply(Handle& H, int lev, int block, T* x, const T* b) {
+  chebyshev<T>(H, lev, block, x, b, true);
+  for (int k = 1; k < smoothing_steps(H, block); ++k) chebyshev<T>(H, lev, block, x, b, false);
+}
+template <typename T>
+void smoother_smooth(Handle& H, int lev, int block, T* x, const T* b) {
+  for (int k = 0; k < smoothing_steps(H, block); ++k) chebyshev<T>(H, lev, block, x, b, false);
+}
+
+template <typename T>
+void vcycle_level(Handle& H, int lev, int block) {
+  Level& L = H.levels[lev];
+  LevelDev<T>& D = L.dev<T>();
+  T* sol = block == 0 ? D.solA.p : D.solM.p;
+  T* def = block == 0 ? D.defA.p : D.defM.p;
+  T* t = block == 0 ? D.tA.p : D.tM.p;
+  const long n = block == 0 ? L.n_u : L.n_p;
+  if (lev == 0) {
+    smoother_apply<T>(H, 0, block, sol, def);
+    return;
+  }
+  Level& C = H.levels[lev - 1];
+  LevelDev<T>& DC = C.dev<T>();
+  T* csol = block == 0 ? DC.solA.p : DC.solM.p;
+  T* cdef = block == 0 ? DC.defA.p : DC.defM.p;
+  const long nc = block == 0 ? C.n_u : C.n_p;
+  smoother_apply<T>(H, lev, block, sol, def);
+  level_op_resid<T>(H, lev, block, sol, def, t);
+  GB_CUDA(cudaMemsetAsync(cdef, 0, nc * sizeof(T), H.st));
+  if (block == 0) v_spmv_add<T>(L.PuT_rows, L.PuT_ptr.p, L.PuT_col.p, D.PuT_val.p, t, cdef, H.st);
+  else v_spmv_add<T>(L.PpT_rows, L.PpT_ptr.p, L.PpT_col.p, D.PpT_val.p, t, cdef, H.st);
+  GB_CUDA(cudaMemsetAsync(csol, 0, nc * sizeof(T), H.st));
+  vcycle_level<T>(H, lev - 1, block);
+  if (block == 0) v_spmv_add<T>(L.Pu_rows, L.Pu_ptr.p, L.Pu_col.p, D.Pu_val.p, csol, sol, H.st);
+  else v_spmv_add<T>(L.Pp_rows, L.Pp_ptr.p, L.Pp_col.p, D.Pp_val.p, csol, sol, H.st);
+  smoother_smooth<T>(H, lev, block, sol, def);
+}
+
+// PreconditionMG::vmult: dst = V(src), FP64 internal vectors of the finest level
+template <typename T>
+void vcycle_T(Handle& H, int block, const double* src, double* dst) {
+  const int top = H.n_levels - 1;
+  Level& F = H.levels[top];
+  LevelDev<T>& D = F.dev<T>();
+  const long n = block == 0 ? F.n_u : F.n_p;
+  T* def = block == 0 ? D.defA.p : D.defM.p;
+  T* sol = block == 0 ? D.solA.p : D.solM.p;
+  if constexpr (std::is_same<T, double>::value) v_copy<double>(n, src, def, H.st);
+  else v_cast<double, float>(n, src, def, H.st);
+  vcycle_level<T>(H, top, block);
+  if constexpr (std::is_same<T, double>::value) v_copy<double>(n, sol, dst, H.st);
+  else v_cast<float, double>(n, sol, dst, H.st);
+}
+// The V-cycle of one block and precision is a fixed launch sequence (all
+// Chebyshev coefficients are known once the eigenvalues are), so it is captured
+// once into a CUDA graph and replayed; the FP64 input and output go through
+// staging vectors whose addresses are baked into the graph.
+void vcycle_exec(Handle& H, int block, int prec, const double* src, double* dst) {
+  const int pi = prec == GB_GMG_FP32 ? 1 : 0;
+  Level& F = H.top();
+  const long n = block == 0 ? F.n_u : F.n_p;
+  if (!H.vgraph[block][pi]) {
+    const long long c0 = H.cell_launches, v0 = VecCounter::launches();
+    cudaGraph_t graph = nullptr;
+    GB_CUDA(cudaStreamBeginCapture(H.st, cudaStreamCaptureModeThreadLocal));
+    try {
+      if (pi) vcycle_T<float>(H, block, H.vin.p, H.vout.p);
+      else vcycle_T<double>(H, block, H.vin.p, H.vout.p);
+    } catch (...) {
+      cudaStreamEndCapture(H.st, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    GB_CUDA(cudaStreamEndCapture(H.st, &graph));
+    GB_CUDA(cudaGraphInstantiate(&H.vgraph[block][pi], graph, 0));
+    size_t nn = 0;
+    GB_CUDA(cudaGraphGetNodes(graph, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    GB_CUDA(cudaGraphGetNodes(graph, nodes.data(), &nn));
+    long long nk = 0;
+    for (auto nd : nodes) {
+      cudaGraphNodeType t;
+      GB_CUDA(cudaGraphNodeGetType(nd, &t));
+      if (t == cudaGraphNodeTypeKernel) ++nk;
+    }
+    H.vgraph_kernels[block][pi] = nk;
+    cudaGraphDestroy(graph);
+    H.cell_launches = c0;  // capture issued nothing; replays are counted below
+    VecCounter::launches() = v0;
+  }
+  v_copy<double>(n, src, H.vin.p, H.st);
+  GB_CUDA(cudaGraphLaunch(H.vgraph[block][pi], H.st));
+  H.cell_launches += H.vgraph_kernels[block][pi];
+  v_copy<double>(n, H.vout.p, dst, H.st);
+}
+
+void vcycle(Handle& H, int block, int prec, const double* src, double* dst) {
+  if (block == 0) ++H.nA; else ++H.nS;
+  vcycle_exec(H, block, prec, src, dst);
+}
+
+// ---------------------------------------------------------------- FP64 active-level operators
+void stokes64(Handle& H, const double* x, double* y) {
+  Level& F = H.top();
+  apply_op<double>(H, H.n_levels - 1, OPK_STOKES, x, x + F.n_u, y, y + F.n_u);
+  ++H.n_stokes64;
+}
+// Stokes operator with FP32 arithmetic on FP64 vectors (inner solves of GMRES_IR)
+void stokes32(Handle& H, const double* x, double* y) {
+  Level& F = H.top();
+  const long n = F.n_u + F.n_p;
+  v_cast<double, float>(n, x, H.f32_a.p, H.st);
+  apply_op<float>(H, H.n_levels - 1, OPK_STOKES, H.f32_a.p, H.f32_a.p + F.n_u, H.f32_b.p, H.f32_b.p + F.n_u);
+  v_cast<float, double>(n, H.f32_b.p, y, H.st);
+}
+
+// ---------------------------------------------------------------- block preconditioner
+int cg_solve(Handle& H, int block, int prec, long n, double* x, const double* b, double tol, int maxit);
+
+void block_preconditioner(Handle& H, int prec, bool expensive, const gb_gmg_solve_params* P, const double* src,
+                          double* dst) {
+  Level& F = H.top();
+  const long nu = F.n_u, np = F.n_p;
+  if (!expensive) {
+    vcycle(H, 1, prec, src + nu, dst + nu);
+  } else {
+    const double sn = std::sqrt(dot_host(H, np, src + nu, src + nu));
+    GB_CUDA(cudaMemsetAsync(dst + nu, 0, np * sizeof(double), H.st));
+    if (sn > 1e-50) H.nS += cg_solve(H, 1, prec, np, dst + nu, src + nu, sn * P->tol_S, 100) - 0;
+  }
+  v_scale<double>(np, -1.0, dst + nu, H.st);
+  apply_op<double>(H, H.n_levels - 1, OPK_BT, nullptr, dst + nu, H.t2v.p, nullptr);
+  v_axpby<double>(nu, 1.0, src, -1.0, H.t2v.p, H.st);  // t = src_u - B^T p
+  if (!expensive) {
+    vcycle(H, 0, prec, H.t2v.p, dst);
+  } else {
+    const double tn = std::sqrt(dot_host(H, nu, H.t2v.p, H.t2v.p));
+    H.nA += cg_solve(H, 0, prec, nu, dst, H.t2v.p, tn * P->tol_A, 10000);
+  }
+}
+
+// preconditioned CG of the expensive inner solves (FP64 operator, V-cycle preconditioner)
+int cg_solve(Handle& H, int block, int prec, long n, double* x, const double* b, double tol, int maxit) {
+  const int top = H.n_levels - 1;
+  double* r = H.cg_r.p;
+  double* z = H.cg_z.p;
+  double* p = H.cg_p.p;
+  double* q = H.cg_q.p;
+  auto op = [&](const double* a, double* y) {
+    if (block == 0) apply_op<double>(H, top, OPK_A, a, nullptr, y, nullptr);
+    else apply_op<double>(H, top, OPK_MASS, nullptr, a, nullptr, y);
+  };
+  auto pre = [&](const double* a, double* y) { vcycle_exec(H, block, prec, a, y); };
+  GB_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), H.st));
+  v_copy<double>(n, b, r, H.st);
+  double rn = std::sqrt(dot_host(H, n, r, r));
+  if (rn <= tol) return 0;
+  pre(r, z);
+  v_copy<double>(n, z, p, H.st);
+  double rz = dot_host(H, n, r, z);
+  for (int it = 1; it <= maxit; ++it) {
+    op(p, q);
+    const double alpha = rz / dot_host(H, n, p, q);
+    v_axpby<double>(n, alpha, p, 1.0, x, H.st);
+    v_axpby<double>(n, -alpha, q, 1.0, r, H.st);
+    rn = std::sqrt(dot_host(H, n, r, r));
+    if (rn <= tol) return it;
+    pre(r, z);
+    const double rz2 = dot_host(H, n, r, z);
+    const double beta = rz2 / rz;
+    rz = rz2;
+    v_axpby<double>(n, 1.0, z, beta, p, H.st);
+  }
+  throw Error(GB_GMG_NO_CONVERGENCE, "iterative inner CG solver did not converge");
+}
+
+// ---------------------------------------------------------------- GMRES / FGMRES
+void ensure_krylov(Handle& H, int restart) {
+  const long n = H.n_top();
+  if (H.restart_alloc >= restart) return;
+  H.V.alloc((size_t)(restart + 1) * n);
+  H.Z.alloc((size_t)restart * n);
+  H.coef_d.alloc(restart + 2);
+  if (H.dots_d.n < (size_t)restart + 2) {
+    H.dots_d.alloc(restart + 2);
+    if (H.dots_h) cudaFreeHost(H.dots_h);
+    H.dots_h = nullptr;
+    GB_CUDA(cudaMallocHost(&H.dots_h, (restart + 2) * sizeof(double)));
+  }
+  H.restart_alloc = restart;
+}
+
+// Solves K x = b (right preconditioning). Returns iterations.
+int gmres(Handle& H, double* x, const double* b, double tol, int maxit, int restart, bool flexible,
+          bool expensive, int prec, bool fp32_operator, const gb_gmg_solve_params* P, bool& converged,
+          double& final_res) {
+  const long n = H.n_top();
+  ensure_krylov(H, restart);
+  double* V = H.V.p;
+  double* Z = H.Z.p;
+  double* w = H.wv.p;
+  double* r = H.rv.p;
+  double* tmp = H.tv.p;
+  auto K = [&](const double* a, double* y) {
+    if (fp32_operator) stokes32(H, a, y);
+    else stokes64(H, a, y);
+  };
+  int it = 0;
+  converged = false;
+  std::vector<double> hbuf(restart + 2);
+  while (true) {
+    K(x, tmp);
+    v_copy<double>(n, b, r, H.st);
+    v_axpby<double>(n, -1.0, tmp, 1.0, r, H.st);
+    const double beta = std::sqrt(dot_host(H, n, r, r));
+    final_res = beta;
+    GB_CHECK(std::isfinite(beta), GB_GMG_NAN_DETECTED, "NaN or Inf in the Stokes residual");
+    if (beta <= tol) { converged = true; return it; }
+    if (it >= maxit) return it;
+    v_copy<double>(n, r, V, H.st);
+    v_scale<double>(n, 1.0 / beta, V, H.st);
+    std::vector<std::vector<double>> Hc;
+    std::vector<double> cs, sn, g(1, beta);
+    int j = 0;
+    for (; j < restart && it < maxit; ++j) {
+      double* vj = V + (size_t)j * n;
+      double* zj = flexible ? Z + (size_t)j * n : H.xv.p;
+      block_preconditioner(H, prec, expensive, P, vj, zj);
+      K(zj, w);
+      ++it;
+      std::vector<double> h(j + 2, 0.0);
+      // classical Gram-Schmidt with one conditional re-orthogonalisation
+      v_multidot(n, w, V, n, j + 1, true, H.dots_d.p, H.partial.p, H.st);
+      GB_CUDA(cudaMemcpyAsync(H.dots_h, H.dots_d.p, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, H.st));
+      GB_CUDA(cudaStreamSynchronize(H.st));
+      const double norm_before = std::sqrt(H.dots_h[j + 1]);
+      for (int pass = 0; pass < 2; ++pass) {
+        if (pass == 1) {
+          v_multidot(n, w, V, n, j + 1, false, H.dots_d.p, H.partial.p, H.st);
+          GB_CUDA(cudaMemcpyAsync(H.dots_h, H.dots_d.p, (j + 1) * sizeof(double), cudaMemcpyDeviceToHost, H.st));
+          GB_CUDA(cudaStreamSynchronize(H.st));
+        }
+        for (int i = 0; i <= j; ++i) {
+          hbuf[i] = -H.dots_h[i];
+          h[i] += H.dots_h[i];
+        }
+        GB_CUDA(cudaMemcpyAsync(H.coef_d.p, hbuf.data(), (j + 1) * sizeof(double), cudaMemcpyHostToDevice, H.st));
+        v_multiaxpy(n, j + 1, H.coef_d.p, V, n, w, H.st);
+        const double nw = std::sqrt(dot_host(H, n, w, w));
+        h[j + 1] = nw;
+        if (pass == 0 && nw > 0.7 * norm_before) break;
+      }
+      const double hn = h[j + 1];
+      for (int i = 0; i < j; ++i) {
+        const double t = cs[i] * h[i] + sn[i] * h[i + 1];
+        h[i + 1] = -sn[i] * h[i] + cs[i] * h[i + 1];
+        h[i] = t;
+      }
+      const double den = std::hypot(h[j], h[j + 1]);
+      GB_CHECK(den > 0 && std::isfinite(den), GB_GMG_BREAKDOWN, "GMRES breakdown");
+      const double c_ = h[j] / den, s_ = h[j + 1] / den;
+      cs.push_back(c_);
+      sn.push_back(s_);
+      h[j] = den;
+      h[j + 1] = 0;
+      g.push_back(-s_ * g[j]);
+      g[j] = c_ * g[j];
+      Hc.push_back(h);
+      v_copy<double>(n, w, V + (size_t)(j + 1) * n, H.st);
+      v_scale<double>(n, 1.0 / (hn > 0 ? hn : 1.0), V + (size_t)(j + 1) * n, H.st);
+      final_res = std::fabs(g[j + 1]);
+      if (final_res <= tol) { ++j; break; }
+    }
+    const int m = j;
+    std::vector<double> y(m);
+    for (int i = m - 1; i >= 0; --i) {
+      double t = g[i];
+      for (int k = i + 1; k < m; ++k) t -= Hc[k][i] * y[k];
+      y[i] = t / Hc[i][i];
+    }
+    GB_CUDA(cudaMemcpyAsync(H.coef_d.p, y.data(), m * sizeof(double), cudaMemcpyHostToDevice, H.st));
+    if (flexible) {
+      v_multiaxpy(n, m, H.coef_d.p, Z, n, x, H.st);
+    } else {
+      GB_CUDA(cudaMemsetAsync(tmp, 0, n * sizeof(double), H.st));
+      v_multiaxpy(n, m, H.coef_d.p, V, n, tmp, H.st);
+      block_preconditioner(H, prec, expensive, P, tmp, H.xv.p);
+      v_axpby<double>(n, 1.0, H.xv.p, 1.0, x, H.st);
+    }
+    // the next pass starts from the true FP64 residual of the updated iterate:
+    // convergence is only reported on that residual
+  }
+}
+
+// ---------------------------------------------------------------- the solve
+void ensure_workspace(Handle& H) {
+  const long n = H.n_top();
+  long nmax = 0;
+  for (auto& L : H.levels) nmax = std::max(nmax, L.n_u + L.n_p);
+  H.stage_a.alloc(nmax);
+  H.stage_b.alloc(nmax);
+  for (DevBuf<double>* b : {&H.wv, &H.xv, &H.rv, &H.bv, &H.tv, &H.t2v, &H.cg_r, &H.cg_z, &H.cg_p, &H.cg_q, &H.cg_x})
+    if (b->n != (size_t)n) { b->alloc(n); b->zero(H.st); }
+  H.f32_a.alloc(n);
+  H.f32_b.alloc(n);
+  H.vin.alloc(n);
+  H.vout.alloc(n);
+  H.partial.alloc((kDotChunk + 1) * kDotBlocks);
+  H.dots_d.alloc(256);
+  if (!H.dots_h) GB_CUDA(cudaMallocHost(&H.dots_h, 256 * sizeof(double)));
+  if (!H.flag_d) GB_CUDA(cudaMalloc(&H.flag_d, sizeof(int)));
+}
+
+template <typename T>
+void alloc_level_work(Level& L, cudaStream_t st) {
+  LevelDev<T>& D = L.dev<T>();
+  for (DevBuf<T>* b : {&D.solA, &D.defA, &D.tA, &D.dA}) { b->alloc(L.n_u); b->zero(st); }
+  for (DevBuf<T>* b : {&D.solM, &D.defM, &D.tM, &D.dM}) { b->alloc(L.n_p); b->zero(st); }
+}
+
+template <typename T>
+void build_preconditioner_T(Handle& H) {
+  for (int l = 0; l < H.n_levels; ++l) {
+    alloc_level_work<T>(H.levels[l], H.st);
+    compute_diagonals<T>(H, l);
+  }
+  for (int l = 0; l < H.n_levels; ++l) {
+    estimate_eigenvalues<T>(H, l, 0);
+    estimate_eigenvalues<T>(H, l, 1);
+  }
+  GB_CUDA(cudaStreamSynchronize(H.st));
+}
+
+void to_internal(Handle& H, int lev, const double* d_caller, double* d_internal, bool with_u, bool with_p) {
+  Level& L = H.levels[lev];
+  if (with_u) v_permute_scatter<double, double>(L.n_u, L.perm_u_d.p, d_caller, d_internal, H.st);
+  if (with_p)
+    v_permute_scatter<double, double>(L.n_p, L.perm_p_d.p, d_caller + (with_u ? L.n_u : 0),
+                                      d_internal + (with_u ? L.n_u : 0), H.st);
+}
+void to_caller(Handle& H, int lev, const double* d_internal, double* d_caller, bool with_u, bool with_p) {
+  Level& L = H.levels[lev];
+  if (with_u) v_permute_gather<double, double>(L.n_u, L.perm_u_d.p, d_internal, d_caller, H.st);
+  if (with_p)
+    v_permute_gather<double, double>(L.n_p, L.perm_p_d.p, d_internal + (with_u ? L.n_u : 0),
+                                     d_caller + (with_u ? L.n_u : 0), H.st);
+}
+
+void solve_internal(Handle& H, const gb_gmg_solve_params* P, gb_gmg_outputs* out) {
+  Level& F = H.top();
+  const long nu = F.n_u, n = H.n_top();
+  double* x = H.cg_x.p;   // solution (internal)
+  double* b = H.bv.p;     // rhs (internal)
+  const int prec = P->mg_precision;
+  GB_CHECK(H.prec_done[prec == GB_GMG_FP32 ? 1 : 0], GB_GMG_NOT_READY, "build_preconditioner has not been called");
+  // constrained entries of the initial guess are zero during the solve
+  v_zero_indexed<double>((long)F.cons_u.size(), F.cons_u_d.p, x, H.st);
+  v_zero_indexed<double>((long)F.cons_p.size(), F.cons_p_d.p, x + nu, H.st);
+  H.nA = H.nS = H.n_stokes64 = 0;
+  cudaEvent_t e0, e1;
+  GB_CUDA(cudaEventCreate(&e0));
+  GB_CUDA(cudaEventCreate(&e1));
+  GB_CUDA(cudaEventRecord(e0, H.st));
+  // initial residual and tolerance (:977-1041)
+  double* t = H.tv.p;
+  stokes64(H, x, t);
+  v_copy<double>(n, b, H.rv.p, H.st);
+  v_axpby<double>(n, -1.0, t, 1.0, H.rv.p, H.st);
+  out->initial_nonlinear_residual = std::sqrt(dot_host(H, n, H.rv.p, H.rv.p));
+  v_copy<double>(n, x, H.wv.p, H.st);
+  GB_CUDA(cudaMemsetAsync(H.wv.p, 0, nu * sizeof(double), H.st));
+  stokes64(H, H.wv.p, t);
+  v_copy<double>(nu, b, H.rv.p, H.st);
+  v_axpby<double>(nu, -1.0, t, 1.0, H.rv.p, H.st);
+  const double ru = std::sqrt(dot_host(H, nu, H.rv.p, H.rv.p));
+  const double rp = std::sqrt(dot_host(H, n - nu, b + nu, b + nu));
+  const double tol = P->absolute_tolerance > 0 ? P->absolute_tolerance
+                                               : P->linear_solver_tolerance * std::sqrt(ru * ru + rp * rp);
+  out->solver_tolerance = tol;
+  bool conv = false;
+  double fr = 0;
+  out->cheap_iterations = out->expensive_iterations = 0;
+  if (P->krylov == GB_GMG_GMRES_IR) {
+    // FP64 iterative refinement: r = b - K x in FP64, inner FGMRES with the FP32
+    // operator and FP32 V-cycles on K d = r, x += d.
+    double* d = H.xv.p;
+    double* rr = H.rv.p;
+    int outer = 0;
+    while (true) {
+      stokes64(H, x, t);
+      v_copy<double>(n, b, rr, H.st);
+      v_axpby<double>(n, -1.0, t, 1.0, rr, H.st);
+      fr = std::sqrt(dot_host(H, n, rr, rr));
+      GB_CHECK(std::isfinite(fr), GB_GMG_NAN_DETECTED, "NaN or Inf in the Stokes residual");
+      if (fr <= tol) { conv = true; break; }
+      if (outer >= 50 || out->cheap_iterations >= P->n_cheap_steps) break;
+      ++outer;
+      GB_CUDA(cudaMemsetAsync(d, 0, n * sizeof(double), H.st));
+      bool c2;
+      double f2;
+      const double inner_tol = std::max(tol, P->ir_inner_tolerance * fr) * 0.5;
+      // the inner solve keeps its own copies of b (rr) in bv-sized storage
+      v_copy<double>(n, rr, H.cg_r.p, H.st);
+      out->cheap_iterations += gmres(H, d, H.cg_r.p, inner_tol, P->n_cheap_steps, P->restart, true, false, prec,
+                                     true, P, c2, f2);
+      v_axpby<double>(n, 1.0, d, 1.0, x, H.st);
+    }
+  } else {
+    // The cheap phase of the reference is plain GMRES because its preconditioner
+    // is a fixed linear operator. A V-cycle in FP32 is not exactly linear any
+    // more, so with FP32 levels the cheap phase is flexible GMRES (FGMRES).
+    const bool flexible_cheap = prec == GB_GMG_FP32;
+    if (P->n_cheap_steps > 0)
+      out->cheap_iterations =
+          gmres(H, x, b, tol, P->n_cheap_steps, P->restart, flexible_cheap, false, prec, false, P, conv, fr);
+    if (!conv && P->n_expensive_steps > 0)
+      out->expensive_iterations =
+          gmres(H, x, b, tol, P->n_expensive_steps, P->restart, true, true, prec, false, P, conv, fr);
+  }
+  GB_CUDA(cudaEventRecord(e1, H.st));
+  GB_CUDA(cudaEventSynchronize(e1));
+  float ms = 0;
+  GB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  out->solve_seconds = ms * 1e-3;
+  out->final_linear_residual = fr;
+  out->A_preconditioner_applications = H.nA;
+  out->S_preconditioner_applications = H.nS;
+  out->fp64_stokes_applications = H.n_stokes64;
+  out->status = conv ? GB_GMG_OK : GB_GMG_NO_CONVERGENCE;
+}
+
+}  // namespace
+}  // namespace gb
+
+// =====================================================================================
+// C ABI
+// =====================================================================================
+using gb::Handle;
+
+struct gb_gmg {
+  Handle h;
+};
+
+#define ABI_TRY(H, ...)                                        \
+  try {                                                        \
+    __VA_ARGS__;                                               \
+    return GB_GMG_OK;                                          \
+  } catch (const gb::Error& e) {                               \
+    (H)->h.err = e.what();                                     \
+    return e.code;                                             \
+  } catch (const std::bad_alloc& e) {                          \
+    (H)->h.err = "out of host memory";                         \
+    return GB_GMG_OUT_OF_MEMORY;                               \
+  } catch (const std::exception& e) {                          \
+    (H)->h.err = e.what();                                     \
+    return GB_GMG_INVALID_ARGUMENT;                            \
+  }
+
+extern "C" {
+
+void gb_gmg_default_options(gb_gmg_options* o) {
+  o->verbose = 0;
+  o->smoother_degree = 4;
+  o->smoothing_range = 15.0;
+  o->eig_cg_iterations = 10;
+  o->coarse_degree = 8;
+  o->coarse_range = 1e-3;
+  o->coarse_eig_cg_iterations = 100;
+  o->schur_smoothing_steps = 4;
+  o->force_indexed_layout = 0;
+}
+
+void gb_gmg_default_solve_params(gb_gmg_solve_params* p) {
+  p->linear_solver_tolerance = 1e-7;
+  p->absolute_tolerance = 0.0;
+  p->n_cheap_steps = 1000;
+  p->n_expensive_steps = 1000;
+  p->restart = 100;
+  p->tol_A = 1e-2;
+  p->tol_S = 1e-6;
+  p->mg_precision = GB_GMG_FP64;
+  p->krylov = GB_GMG_GMRES;
+  p->ir_inner_tolerance = 1e-3;
+}
+
+int gb_gmg_create(const gb_gmg_options* opt, int dim, int degree_v, int n_levels, gb_gmg** out) {
+  if (!out) return GB_GMG_INVALID_ARGUMENT;
+  *out = nullptr;
+  if ((dim != 2 && dim != 3) || degree_v != 2 || n_levels < 1) return GB_GMG_INVALID_ARGUMENT;
+  gb_gmg* g = new gb_gmg();
+  if (opt) g->h.opt = *opt;
+  else gb_gmg_default_options(&g->h.opt);
+  g->h.dim = dim;
+  g->h.n_levels = n_levels;
+  g->h.levels.resize(n_levels);
+  for (auto& L : g->h.levels) L.dim = dim;
+  if (cudaStreamCreateWithFlags(&g->h.st, cudaStreamNonBlocking) != cudaSuccess) {
+    delete g;
+    return GB_GMG_CUDA_ERROR;
+  }
+  *out = g;
+  return GB_GMG_OK;
+}
+
+void gb_gmg_destroy(gb_gmg* g) {
+  if (!g) return;
+  cudaStreamSynchronize(g->h.st);
+  g->h.reset_graphs();
+  if (g->h.dots_h) cudaFreeHost(g->h.dots_h);
+  if (g->h.flag_d) cudaFree(g->h.flag_d);
+  cudaStreamDestroy(g->h.st);
+  delete g;
+}
+
+const char* gb_gmg_last_error(const gb_gmg* g) { return g ? g->h.err.c_str() : "null handle"; }
+
+int gb_gmg_set_level_mesh(gb_gmg* g, int level, int64_t n_cells, const int32_t* cdu, const int32_t* cdp,
+                          int geometry_kind, const double* geom, int64_t n_u, int64_t n_p) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(level >= 0 && level < H.n_levels, 1, "level out of range");
+    GB_CHECK(n_cells > 0 && n_u > 0 && n_p > 0 && cdu && cdp && geom, 1, "empty mesh or null array");
+    GB_CHECK(n_u < (1LL << 31) && n_p < (1LL << 31), 1, "more than 2^31 DoFs per block");
+    GB_CHECK(geometry_kind == 0 || geometry_kind == 1, 1, "unknown geometry kind");
+    gb::Level& L = H.levels[level];
+    const int nv = H.dim == 3 ? 27 : 9, np = H.dim == 3 ? 8 : 4;
+    L.n_cells = n_cells;
+    L.n_u = n_u;
+    L.n_p = n_p;
+    L.cdu.assign(cdu, cdu + n_cells * H.dim * nv);
+    L.cdp.assign(cdp, cdp + n_cells * np);
+    for (int v : L.cdu) GB_CHECK(v >= 0 && v < n_u, 1, "velocity DoF index out of range");
+    for (int v : L.cdp) GB_CHECK(v >= 0 && v < n_p, 1, "pressure DoF index out of range");
+    L.geom_kind = geometry_kind;
+    const size_t ng = geometry_kind == 0 ? (size_t)n_cells * 2 * H.dim : (size_t)n_cells * nv * H.dim;
+    L.geom.assign(geom, geom + ng);
+    L.cu.init(n_u);
+    L.cp.init(n_p);
+    H.setup_done = false;
+  })
+}
+
+int gb_gmg_set_level_constraints(gb_gmg* g, int level, int block, int64_t n_lines, const int32_t* rows,
+                                 const int32_t* ptr, const int32_t* cols, const double* w, const double* inhom) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(level >= 0 && level < H.n_levels && (block == 0 || block == 1), 1, "level/block out of range");
+    gb::Level& L = H.levels[level];
+    GB_CHECK(L.n_cells > 0, 2, "set the level mesh before its constraints");
+    gb::HostCons& C = block == 0 ? L.cu : L.cp;
+    const long n = block == 0 ? L.n_u : L.n_p;
+    C.init(n);
+    for (int64_t i = 0; i < n_lines; ++i) {
+      GB_CHECK(rows[i] >= 0 && rows[i] < n, 1, "constraint row out of range");
+      GB_CHECK(C.line_of[rows[i]] < 0, 1, "duplicate constraint line");
+      C.line_of[rows[i]] = (int)i;
+      for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+        GB_CHECK(cols[k] >= 0 && cols[k] < n, 1, "constraint entry out of range");
+        C.cols.push_back(cols[k]);
+        C.w.push_back(w[k]);
+      }
+      C.ptr.push_back((int)C.cols.size());
+      C.inhom.push_back(inhom ? inhom[i] : 0.0);
+    }
+    H.setup_done = false;
+  })
+}
+
+int gb_gmg_set_transfer(gb_gmg* g, int level, const int32_t* parent, const uint8_t* child) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(level >= 1 && level < H.n_levels, 1, "transfer level out of range");
+    gb::Level& L = H.levels[level];
+    GB_CHECK(L.n_cells > 0, 2, "set the level mesh before its transfer");
+    L.parent.assign(parent, parent + L.n_cells);
+    L.child.assign(child, child + L.n_cells);
+    for (unsigned char c : L.child) GB_CHECK(c < (1u << H.dim), 1, "child index out of range");
+    L.has_transfer = true;
+    H.setup_done = false;
+  })
+}
+
+int gb_gmg_finalize_setup(gb_gmg* g) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    for (auto& L : H.levels) GB_CHECK(L.n_cells > 0, 2, "a level has no mesh");
+    for (auto& L : H.levels) gb::setup_level(L, H.opt.force_indexed_layout != 0);
+    for (int l = 1; l < H.n_levels; ++l) gb::setup_transfer(H.levels[l], H.levels[l - 1]);
+    gb::ensure_workspace(H);
+    GB_CUDA(cudaStreamSynchronize(H.st));
+    H.reset_graphs();
+    H.setup_done = true;
+    H.visc_done = false;
+    H.prec_done[0] = H.prec_done[1] = false;
+  })
+}
+
+int gb_gmg_set_viscosity(gb_gmg* g, const double* eta, int n_per_cell, int projection, double s, int compressible) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(H.setup_done, GB_GMG_NOT_READY, "finalize_setup has not been called");
+    const int nq = H.dim == 3 ? 27 : 9;
+    GB_CHECK(n_per_cell == 1 || n_per_cell == nq, 1, "n_per_cell must be 1 or 3^dim");
+    GB_CHECK(s > 0 && std::isfinite(s), 1, "pressure scaling must be positive");
+    H.s = s;
+    H.compressible = compressible;
+    H.projection = projection;
+    gb::compute_level_viscosity(H.levels, eta, n_per_cell, projection, H.eta_min, H.eta_max);
+    for (auto& L : H.levels) gb::upload_viscosity(L);
+    H.reset_graphs();
+    H.visc_done = true;
+    H.prec_done[0] = H.prec_done[1] = false;
+  })
+}
+
+int gb_gmg_build_preconditioner(gb_gmg* g) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
+    H.reset_graphs();
+    gb::build_preconditioner_T<double>(H);
+    H.prec_done[0] = true;
+    gb::build_preconditioner_T<float>(H);
+    H.prec_done[1] = true;
+  })
+}
+
+int gb_gmg_vmult(gb_gmg* g, int op, int level, int precision, const double* src, double* dst) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
+    GB_CHECK(level >= 0 && level < H.n_levels && op >= 0 && op <= 3, 1, "level/op out of range");
+    gb::Level& L = H.levels[level];
+    const long nin = op == 0 ? L.n_u + L.n_p : (op == 1 ? L.n_u : L.n_p);
+    const long nout = op == 0 ? L.n_u + L.n_p : (op == 3 ? L.n_p : L.n_u);
+    GB_CUDA(cudaMemcpyAsync(H.stage_a.p, src, nin * sizeof(double), cudaMemcpyHostToDevice, H.st));
+    double* a = H.stage_a.p;
+    double* b = H.stage_b.p;
+    // caller -> internal into b, apply into a, internal -> caller into b
+    const bool in_u = op <= 1, in_p = op == 0 || op >= 2;
+    const bool out_u = op <= 2, out_p = op == 0 || op == 3;
+    if (in_u && in_p) gb::to_internal(H, level, a, b, true, true);
+    else if (in_u) gb::to_internal(H, level, a, b, true, false);
+    else gb::v_permute_scatter<double, double>(L.n_p, L.perm_p_d.p, a, b, H.st);
+    const double* su = in_u ? b : nullptr;
+    const double* sp = in_p ? (in_u ? b + L.n_u : b) : nullptr;
+    if (precision == GB_GMG_FP64) {
+      double* du = out_u ? a : nullptr;
+      double* dp = out_p ? (out_u ? a + L.n_u : a) : nullptr;
+      gb::apply_op<double>(H, level, op, su, sp, du, dp);
+    } else {
+      gb::v_cast<double, float>(nin, b, H.f32_a.p, H.st);
+      const float* fu = in_u ? H.f32_a.p : nullptr;
+      const float* fp = in_p ? (in_u ? H.f32_a.p + L.n_u : H.f32_a.p) : nullptr;
+      float* du = out_u ? H.f32_b.p : nullptr;
+      float* dp = out_p ? (out_u ? H.f32_b.p + L.n_u : H.f32_b.p) : nullptr;
+      gb::apply_op<float>(H, level, op, fu, fp, du, dp);
+      gb::v_cast<float, double>(nout, H.f32_b.p, a, H.st);
+    }
+    if (out_u && out_p) gb::to_caller(H, level, a, b, true, true);
+    else if (out_u) gb::to_caller(H, level, a, b, true, false);
+    else gb::v_permute_gather<double, double>(L.n_p, L.perm_p_d.p, a, b, H.st);
+    GB_CUDA(cudaMemcpyAsync(dst, b, nout * sizeof(double), cudaMemcpyDeviceToHost, H.st));
+    GB_CUDA(cudaStreamSynchronize(H.st));
+  })
+}
+
+int gb_gmg_vmult_device(gb_gmg* g, int op, int precision, const double* d_src, double* d_dst) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
+    GB_CHECK(op == 0, 1, "vmult_device supports the Stokes operator");
+    const int top = H.n_levels - 1;
+    gb::Level& L = H.levels[top];
+    gb::to_internal(H, top, d_src, H.stage_a.p, true, true);
+    if (precision == GB_GMG_FP64) {
+      gb::apply_op<double>(H, top, 0, H.stage_a.p, H.stage_a.p + L.n_u, H.stage_b.p, H.stage_b.p + L.n_u);
+    } else {
+      gb::stokes32(H, H.stage_a.p, H.stage_b.p);
+    }
+    gb::to_caller(H, top, H.stage_b.p, d_dst, true, true);
+    GB_CUDA(cudaStreamSynchronize(H.st));
+  })
+}
+
+int gb_gmg_get_diagonal_inverse(gb_gmg* g, int level, int block, int precision, double* out) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    const int pi = precision == GB_GMG_FP32 ? 1 : 0;
+    GB_CHECK(H.prec_done[pi], GB_GMG_NOT_READY, "build_preconditioner has not been called");
+    gb::Level& L = H.levels.at(level);
+    const std::vector<int>& perm = block == 0 ? L.perm_u : L.perm_p;
+    std::vector<double> v;
+    if (pi) {
+      auto d = (block == 0 ? L.f32.dinvA : L.f32.dinvM).download();
+      v.assign(d.begin(), d.end());
+    } else {
+      v = (block == 0 ? L.f64.dinvA : L.f64.dinvM).download();
+    }
+    for (size_t i = 0; i < perm.size(); ++i) out[i] = v[perm[i]];
+  })
+}
+
+int gb_gmg_get_eigenvalues(gb_gmg* g, int level, int block, int precision, double* mm) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    gb::Level& L = g->h.levels.at(level);
+    const double* e = precision == GB_GMG_FP32 ? (block == 0 ? L.f32.eigA : L.f32.eigM)
+                                               : (block == 0 ? L.f64.eigA : L.f64.eigM);
+    mm[0] = e[0];
+    mm[1] = e[1];
+  })
+}
+
+int gb_gmg_set_eigenvalues(gb_gmg* g, int level, int block, int precision, const double* mm) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    gb::Level& L = g->h.levels.at(level);
+    double* e;
+    bool* given;
+    if (precision == GB_GMG_FP32) {
+      e = block == 0 ? L.f32.eigA : L.f32.eigM;
+      given = &L.f32.eig_given[block];
+    } else {
+      e = block == 0 ? L.f64.eigA : L.f64.eigM;
+      given = &L.f64.eig_given[block];
+    }
+    e[0] = mm[0];
+    e[1] = mm[1];
+    *given = true;
+    g->h.reset_graphs();
+  })
+}
+
+int gb_gmg_transfer(gb_gmg* g, int fine_level, int block, int precision, int restrict_, const double* src,
+                    double* dst) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(H.setup_done && fine_level >= 1 && fine_level < H.n_levels, 1, "bad transfer level");
+    gb::Level& F = H.levels[fine_level];
+    gb::Level& C = H.levels[fine_level - 1];
+    const long nf = block == 0 ? F.n_u : F.n_p, nc = block == 0 ? C.n_u : C.n_p;
+    const long nin = restrict_ ? nf : nc, nout = restrict_ ? nc : nf;
+    const gb::Level& Lin = restrict_ ? F : C;
+    const gb::Level& Lout = restrict_ ? C : F;
+    const int* pin = block == 0 ? Lin.perm_u_d.p : Lin.perm_p_d.p;
+    const int* pout = block == 0 ? Lout.perm_u_d.p : Lout.perm_p_d.p;
+    GB_CUDA(cudaMemcpyAsync(H.stage_a.p, src, nin * sizeof(double), cudaMemcpyHostToDevice, H.st));
+    gb::v_permute_scatter<double, double>(nin, pin, H.stage_a.p, H.stage_b.p, H.st);
+    GB_CUDA(cudaMemsetAsync(H.stage_a.p, 0, nout * sizeof(double), H.st));
+    auto run = [&](auto tag) {
+      using T = decltype(tag);
+      gb::LevelDev<T>& D = F.dev<T>();
+      const T* x;
+      T* y;
+      if constexpr (std::is_same<T, double>::value) {
+        x = H.stage_b.p;
+        y = H.stage_a.p;
+      } else {
+        gb::v_cast<double, float>(nin, H.stage_b.p, H.f32_a.p, H.st);
+        GB_CUDA(cudaMemsetAsync(H.f32_b.p, 0, nout * sizeof(float), H.st));
+        x = H.f32_a.p;
+        y = H.f32_b.p;
+      }
+      if (restrict_) {
+        if (block == 0) gb::v_spmv_add<T>(F.PuT_rows, F.PuT_ptr.p, F.PuT_col.p, D.PuT_val.p, x, y, H.st);
+        else gb::v_spmv_add<T>(F.PpT_rows, F.PpT_ptr.p, F.PpT_col.p, D.PpT_val.p, x, y, H.st);
+      } else {
+        if (block == 0) gb::v_spmv_add<T>(F.Pu_rows, F.Pu_ptr.p, F.Pu_col.p, D.Pu_val.p, x, y, H.st);
+        else gb::v_spmv_add<T>(F.Pp_rows, F.Pp_ptr.p, F.Pp_col.p, D.Pp_val.p, x, y, H.st);
+      }
+      if constexpr (!std::is_same<T, double>::value) gb::v_cast<float, double>(nout, H.f32_b.p, H.stage_a.p, H.st);
+    };
+    if (precision == GB_GMG_FP32) run(float()); else run(double());
+    gb::v_permute_gather<double, double>(nout, pout, H.stage_a.p, H.stage_b.p, H.st);
+    GB_CUDA(cudaMemcpyAsync(dst, H.stage_b.p, nout * sizeof(double), cudaMemcpyDeviceToHost, H.st));
+    GB_CUDA(cudaStreamSynchronize(H.st));
+  })
+}
+
+int gb_gmg_vcycle(gb_gmg* g, int block, int precision, const double* src, double* dst) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(H.prec_done[precision == GB_GMG_FP32 ? 1 : 0], GB_GMG_NOT_READY, "build_preconditioner missing");
+    const int top = H.n_levels - 1;
+    gb::Level& F = H.levels[top];
+    const long n = block == 0 ? F.n_u : F.n_p;
+    const int* perm = block == 0 ? F.perm_u_d.p : F.perm_p_d.p;
+    GB_CUDA(cudaMemcpyAsync(H.stage_a.p, src, n * sizeof(double), cudaMemcpyHostToDevice, H.st));
+    gb::v_permute_scatter<double, double>(n, perm, H.stage_a.p, H.stage_b.p, H.st);
+    gb::vcycle(H, block, precision, H.stage_b.p, H.stage_a.p);
+    gb::v_permute_gather<double, double>(n, perm, H.stage_a.p, H.stage_b.p, H.st);
+    GB_CUDA(cudaMemcpyAsync(dst, H.stage_b.p, n * sizeof(double), cudaMemcpyDeviceToHost, H.st));
+    GB_CUDA(cudaStreamSynchronize(H.st));
+  })
+}
+
+int gb_gmg_block_preconditioner(gb_gmg* g, int precision, const double* src, double* dst) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(H.prec_done[precision == GB_GMG_FP32 ? 1 : 0], GB_GMG_NOT_READY, "build_preconditioner missing");
+    const int top = H.n_levels - 1;
+    const long n = H.n_top();
+    GB_CUDA(cudaMemcpyAsync(H.stage_a.p, src, n * sizeof(double), cudaMemcpyHostToDevice, H.st));
+    gb::to_internal(H, top, H.stage_a.p, H.stage_b.p, true, true);
+    gb_gmg_solve_params P;
+    gb_gmg_default_solve_params(&P);
+    gb::block_preconditioner(H, precision, false, &P, H.stage_b.p, H.stage_a.p);
+    gb::to_caller(H, top, H.stage_a.p, H.stage_b.p, true, true);
+    GB_CUDA(cudaMemcpyAsync(dst, H.stage_b.p, n * sizeof(double), cudaMemcpyDeviceToHost, H.st));
+    GB_CUDA(cudaStreamSynchronize(H.st));
+  })
+}
+
+int gb_gmg_solve_device(gb_gmg* g, const double* d_rhs, double* d_sol, const gb_gmg_solve_params* prm,
+                        gb_gmg_outputs* out) {
+  if (!g || !out) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    gb_gmg_solve_params P;
+    if (prm) P = *prm; else gb_gmg_default_solve_params(&P);
+    GB_CHECK(P.restart >= 1, 1, "restart must be >= 1");
+    const int top = H.n_levels - 1;
+    gb::to_internal(H, top, d_rhs, H.bv.p, true, true);
+    gb::to_internal(H, top, d_sol, H.cg_x.p, true, true);
+    *out = gb_gmg_outputs{};
+    gb::solve_internal(H, &P, out);
+    gb::to_caller(H, top, H.cg_x.p, d_sol, true, true);
+    GB_CUDA(cudaStreamSynchronize(H.st));
+    if (out->status != GB_GMG_OK) {
+      H.err = "the iterative Stokes solver did not converge";
+      return out->status;
+    }
+  })
+}
+
+int gb_gmg_solve(gb_gmg* g, const double* rhs, double* sol, const gb_gmg_solve_params* prm, gb_gmg_outputs* out) {
+  if (!g || !out) return GB_GMG_INVALID_ARGUMENT;
+  Handle& H = g->h;
+  const long n = H.setup_done ? H.n_top() : 0;
+  if (!n) { H.err = "finalize_setup has not been called"; return GB_GMG_NOT_READY; }
+  int rc;
+  try {
+    GB_CUDA(cudaMemcpyAsync(H.stage_a.p, rhs, n * sizeof(double), cudaMemcpyHostToDevice, H.st));
+    GB_CUDA(cudaMemcpyAsync(H.stage_b.p, sol, n * sizeof(double), cudaMemcpyHostToDevice, H.st));
+  } catch (const gb::Error& e) { H.err = e.what(); return e.code; }
+  rc = gb_gmg_solve_device(g, H.stage_a.p, H.stage_b.p, prm, out);
+  if (rc == GB_GMG_OK || rc == GB_GMG_NO_CONVERGENCE) {
+    if (cudaMemcpyAsync(sol, H.stage_b.p, n * sizeof(double), cudaMemcpyDeviceToHost, H.st) != cudaSuccess ||
+        cudaStreamSynchronize(H.st) != cudaSuccess) {
+      H.err = "CUDA error copying the solution";
+      return GB_GMG_CUDA_ERROR;
+    }
+  }
+  return rc;
+}
+
+int gb_gmg_adjoint_gradient(gb_gmg* g, const double* u, const double* lambda, double* grad) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
+    const int top = H.n_levels - 1;
+    gb::Level& F = H.levels[top];
+    GB_CUDA(cudaMemcpyAsync(H.stage_a.p, u, F.n_u * sizeof(double), cudaMemcpyHostToDevice, H.st));
+    gb::to_internal(H, top, H.stage_a.p, H.stage_b.p, true, false);
+    GB_CUDA(cudaMemcpyAsync(H.stage_a.p, lambda, F.n_u * sizeof(double), cudaMemcpyHostToDevice, H.st));
+    gb::to_internal(H, top, H.stage_a.p, H.wv.p, true, false);
+    double* gcell = H.tv.p;  // n_cells <= n_u
+    GB_CUDA(cudaMemsetAsync(gcell, 0, F.n_cells * sizeof(double), H.st));
+    const gb::LevelView<double> v = F.view<double>(H.s, H.compressible);
+    for (int k = 0; k < F.n_colours; ++k) {
+      const int cnt = F.colour_count[k];
+      if (!cnt) continue;
+      gb::launch_adjoint_gradient_impl(v, k, F.structured ? 0 : F.colour_begin[k], cnt, H.stage_b.p, H.wv.p, gcell,
+                                       H.st);
+      ++H.cell_launches;
+    }
+    std::vector<double> gi(F.n_cells);
+    GB_CUDA(cudaMemcpyAsync(gi.data(), gcell, F.n_cells * sizeof(double), cudaMemcpyDeviceToHost, H.st));
+    GB_CUDA(cudaStreamSynchronize(H.st));
+    for (long c = 0; c < F.n_cells; ++c) grad[c] = gi[F.internal_of_cell[c]];
+  })
+}
+
+int gb_gmg_time_operation(gb_gmg* g, int what, int precision, int repeats, double* seconds) {
+  if (!g || !seconds || repeats < 1) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    const int pi = precision == GB_GMG_FP32 ? 1 : 0;
+    GB_CHECK(what >= 0 && what <= 5, 1, "unknown operation");
+    if (what >= 3) GB_CHECK(H.prec_done[pi], GB_GMG_NOT_READY, "build_preconditioner has not been called");
+    else GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
+    const int top = H.n_levels - 1;
+    gb::Level& F = H.levels[top];
+    const long n = H.n_top(), nu = F.n_u;
+    // deterministic source data
+    std::vector<double> src(n);
+    for (long i = 0; i < n; ++i) src[i] = (double)(i % 11) - 5.0;
+    GB_CUDA(cudaMemcpyAsync(H.stage_a.p, src.data(), n * sizeof(double), cudaMemcpyHostToDevice, H.st));
+    gb::v_cast<double, float>(n, H.stage_a.p, H.f32_a.p, H.st);
+    auto call = [&]() {
+      double* a = H.stage_a.p;
+      double* b = H.stage_b.p;
+      switch (what) {
+        case 0:
+          if (pi) gb::apply_op<float>(H, top, 0, H.f32_a.p, H.f32_a.p + nu, H.f32_b.p, H.f32_b.p + nu);
+          else gb::apply_op<double>(H, top, 0, a, a + nu, b, b + nu);
+          break;
+        case 1:
+          if (pi) gb::apply_op<float>(H, top, 1, H.f32_a.p, nullptr, H.f32_b.p, nullptr);
+          else gb::apply_op<double>(H, top, 1, a, nullptr, b, nullptr);
+          break;
+        case 2:
+          if (pi) gb::apply_op<float>(H, top, 3, nullptr, H.f32_a.p, nullptr, H.f32_b.p);
+          else gb::apply_op<double>(H, top, 3, nullptr, a, nullptr, b);
+          break;
+        case 3: {
+          gb_gmg_solve_params P;
+          gb_gmg_default_solve_params(&P);
+          gb::block_preconditioner(H, precision, false, &P, a, b);
+          break;
+        }
+        case 4: gb::vcycle(H, 0, precision, a, b); break;
+        case 5: gb::vcycle(H, 1, precision, a + nu, b + nu); break;
+      }
+    };
+    call();
+    cudaEvent_t e0, e1;
+    GB_CUDA(cudaEventCreate(&e0));
+    GB_CUDA(cudaEventCreate(&e1));
+    GB_CUDA(cudaEventRecord(e0, H.st));
+    for (int r = 0; r < repeats; ++r) call();
+    GB_CUDA(cudaEventRecord(e1, H.st));
+    GB_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    GB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *seconds = ms * 1e-3 / repeats;
+  })
+}
+
+int gb_gmg_memory_consumption(const gb_gmg* g, size_t* bytes) {
+  if (!g || !bytes) return GB_GMG_INVALID_ARGUMENT;
+  const Handle& H = g->h;
+  size_t b = 0;
+  for (const auto& L : H.levels) b += L.device_bytes();
+  for (const gb::DevBuf<double>* x : {&H.stage_a, &H.stage_b, &H.partial, &H.dots_d, &H.V, &H.Z, &H.wv, &H.xv,
+                                      &H.rv, &H.bv, &H.tv, &H.t2v, &H.coef_d, &H.cg_r, &H.cg_z, &H.cg_p, &H.cg_q,
+                                      &H.cg_x})
+    b += x->bytes();
+  b += H.f32_a.bytes() + H.f32_b.bytes();
+  *bytes = b;
+  return GB_GMG_OK;
+}
+
+int64_t gb_gmg_kernel_launches(const gb_gmg* g) {
+  if (!g) return 0;
+  return g->h.cell_launches + gb::VecCounter::launches();
+}
+
+}  // extern "C"

@@ -1,0 +1,85 @@
+// Instantiates the launchers for one scalar type GB_T (included by
+// kernels_f32.cu / kernels_f64.cu so that the two precisions compile in parallel).
+#include "ops.cuh"
+
+namespace gb {
+
+namespace {
+constexpr int kCellThreads = 128;
+constexpr int kGatherThreads = 256;
+template <int dim>
+int cell_grid(int count) {
+  const int cells_per_block = (kCellThreads / 32) * Shape<dim>::cpw;
+  return ceil_div(count, cells_per_block);
+}
+
+template <int dim>
+void cell_pass_dim(const LevelView<GB_T>& L, int op, const GB_T* su, const GB_T* sp, GB_T* Eu, GB_T* Ep,
+                   cudaStream_t s) {
+  if (op == OPK_MASS) {
+    mass_cell_kernel<GB_T, dim><<<ceil_div(L.n_cells, kCellThreads), kCellThreads, 0, s>>>(L, sp, Ep);
+    return;
+  }
+  const int g = cell_grid<dim>(L.n_cells);
+  if (op == OPK_STOKES) velocity_cell_kernel<GB_T, dim, OPK_STOKES><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
+  else if (op == OPK_A) velocity_cell_kernel<GB_T, dim, OPK_A><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
+  else velocity_cell_kernel<GB_T, dim, OPK_BT><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
+}
+
+template <int dim, int epi>
+void gather_dim_epi(const LevelView<GB_T>& L, int block, const GatherCsr<GB_T>* csr, const GatherArgs<GB_T>& a,
+                    cudaStream_t s) {
+  const long n = block == 0 ? L.n_u : L.n_p;
+  const int g = ceil_div(n, kGatherThreads);
+  if (csr) gather_csr<GB_T, epi><<<g, kGatherThreads, 0, s>>>(n, *csr, a);
+  else if (block == 0) velocity_gather_structured<GB_T, dim, epi><<<g, kGatherThreads, 0, s>>>(L, a);
+  else pressure_gather_structured<GB_T, dim, epi><<<g, kGatherThreads, 0, s>>>(L, a);
+}
+
+template <int dim>
+void gather_dim(const LevelView<GB_T>& L, int block, int epi, const GatherCsr<GB_T>* csr,
+                const GatherArgs<GB_T>& a, cudaStream_t s) {
+  switch (epi) {
+    case EPI_STORE: gather_dim_epi<dim, EPI_STORE>(L, block, csr, a, s); break;
+    case EPI_BT: gather_dim_epi<dim, EPI_BT>(L, block, csr, a, s); break;
+    case EPI_RESID: gather_dim_epi<dim, EPI_RESID>(L, block, csr, a, s); break;
+    default: gather_dim_epi<dim, EPI_CHEB>(L, block, csr, a, s); break;
+  }
+}
+}  // namespace
+
+template <>
+void launch_cell_pass<GB_T>(const LevelView<GB_T>& L, int op, const GB_T* su, const GB_T* sp, GB_T* Eu, GB_T* Ep,
+                            cudaStream_t s) {
+  if (L.n_cells <= 0) return;
+  if (L.dim == 3) cell_pass_dim<3>(L, op, su, sp, Eu, Ep, s);
+  else cell_pass_dim<2>(L, op, su, sp, Eu, Ep, s);
+}
+
+template <>
+void launch_gather<GB_T>(const LevelView<GB_T>& L, int block, int epi, const GatherCsr<GB_T>* csr,
+                         const GatherArgs<GB_T>& a, cudaStream_t s) {
+  if (L.dim == 3) gather_dim<3>(L, block, epi, csr, a, s);
+  else gather_dim<2>(L, block, epi, csr, a, s);
+}
+
+template <>
+void launch_velocity_diag<GB_T>(const LevelView<GB_T>& L, int colour, int begin, int count,
+                                const ProbesView<GB_T>& pr, GB_T* diag, cudaStream_t s) {
+  if (count <= 0) return;
+  if (L.dim == 3)
+    velocity_diag_kernel<GB_T, 3><<<cell_grid<3>(count), kCellThreads, 0, s>>>(L, colour, begin, count, pr.ptr, pr.g, pr.eptr, pr.li, pr.w, diag);
+  else
+    velocity_diag_kernel<GB_T, 2><<<cell_grid<2>(count), kCellThreads, 0, s>>>(L, colour, begin, count, pr.ptr, pr.g, pr.eptr, pr.li, pr.w, diag);
+}
+
+template <>
+void launch_mass_diag<GB_T>(const LevelView<GB_T>& L, int colour, int begin, int count, const ProbesView<GB_T>& pr,
+                            GB_T* diag, cudaStream_t s) {
+  if (count <= 0) return;
+  const int g = ceil_div(count, kCellThreads);
+  if (L.dim == 3) mass_diag_kernel<GB_T, 3><<<g, kCellThreads, 0, s>>>(L, colour, begin, count, pr.ptr, pr.g, pr.eptr, pr.li, pr.w, diag);
+  else mass_diag_kernel<GB_T, 2><<<g, kCellThreads, 0, s>>>(L, colour, begin, count, pr.ptr, pr.g, pr.eptr, pr.li, pr.w, diag);
+}
+
+}  // namespace gb

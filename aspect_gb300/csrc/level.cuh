@@ -1,0 +1,124 @@
+// Host-side level data of the GB300 GMG Stokes library.
+#pragma once
+#include <array>
+#include <map>
+#include <set>
+#include <vector>
+
+#include "ops.cuh"
+#include "vec.cuh"
+
+namespace gb {
+
+// Closed constraints of one block, caller numbering.
+struct HostCons {
+  std::vector<int> line_of;  // per DoF: -1 or line index
+  std::vector<int> ptr{0}, cols;
+  std::vector<double> w, inhom;
+  void init(long n) {
+    line_of.assign(n, -1);
+    ptr.assign(1, 0);
+    cols.clear();
+    w.clear();
+    inhom.clear();
+  }
+  bool constrained(int g) const { return line_of[g] >= 0; }
+  int n_entries(int g) const {
+    const int l = line_of[g];
+    return l < 0 ? -1 : ptr[l + 1] - ptr[l];
+  }
+};
+
+// A (DoF, weight) expansion of a cell-local DoF in unconstrained DoFs.
+struct Expansion {
+  int n = 0;
+  int g[16];
+  double w[16];
+};
+Expansion expand(const HostCons& c, int g);
+
+struct Csr {
+  std::vector<int> ptr{0}, col;
+  std::vector<double> val;
+  long rows() const { return (long)ptr.size() - 1; }
+  Csr transpose(long n_cols) const;
+};
+
+template <typename T>
+struct LevelDev {
+  DevBuf<T> lw, plw, gbox, gtab, eta;
+  DevBuf<T> probe_w, pprobe_w;
+  DevBuf<T> Pu_val, PuT_val, Pp_val, PpT_val;  // transfer from the next coarser level
+  DevBuf<T> dinvA, dinvM;
+  DevBuf<T> gu_w, gp_w;  // gather weights (general levels)
+  DevBuf<T> Eu, Ep;      // per-cell contributions of pass 1
+  // V-cycle work vectors (A block: n_u, Schur block: n_p)
+  DevBuf<T> solA, defA, tA, dA, solM, defM, tM, dM;
+  double eigA[2] = {0, 0}, eigM[2] = {0, 0};
+  bool eig_given[2] = {false, false};
+};
+
+struct Level {
+  int dim = 3;
+  long n_cells = 0, n_u = 0, n_p = 0;
+  // caller data
+  std::vector<int> cdu, cdp;
+  int geom_kind = 0;
+  std::vector<double> geom;
+  HostCons cu, cp;
+  std::vector<int> parent;
+  std::vector<unsigned char> child;
+  bool has_transfer = false;
+  // internal layout
+  bool structured = false;
+  int nc[3] = {1, 1, 1};
+  double h[3] = {1, 1, 1};
+  uint32_t zero_faces = 0;
+  std::vector<int> perm_u, perm_p;        // caller DoF -> internal DoF
+  std::vector<int> internal_of_cell;      // caller cell -> internal cell
+  std::vector<int> cell_of_internal;      // internal cell -> caller cell
+  int n_colours = 0;
+  std::vector<int> colour_begin, colour_count;
+  std::vector<int> cons_u, cons_p;        // internal constrained DoFs
+  // device data
+  DevBuf<int> cdu_d, cdp_d, lptr_d, lcol_d, plptr_d, plcol_d;
+  DevBuf<int> perm_u_d, perm_p_d, cons_u_d, cons_p_d;
+  DevBuf<int> probe_ptr, probe_g, probe_eptr, probe_li;
+  DevBuf<int> pprobe_ptr, pprobe_g, pprobe_eptr, pprobe_li;
+  DevBuf<int> Pu_ptr, Pu_col, PuT_ptr, PuT_col, Pp_ptr, Pp_col, PpT_ptr, PpT_col;
+  long Pu_rows = 0, PuT_rows = 0, Pp_rows = 0, PpT_rows = 0;
+  // pass-2 gather lists of general levels (caller numbering = internal numbering)
+  DevBuf<int> gu_ptr, gu_slot, gp_ptr, gp_slot;
+  DevBuf<unsigned char> cmask_u, cmask_p;
+  LevelDev<float> f32;
+  LevelDev<double> f64;
+  // viscosity table, internal cell order
+  std::vector<double> eta;
+  int eta_n = 1;
+
+  template <typename T>
+  LevelDev<T>& dev();
+  template <typename T>
+  LevelView<T> view(double s, int compressible);
+  template <typename T>
+  GatherCsr<T> csr(int block) {
+    LevelDev<T>& D = dev<T>();
+    if (block == 0) return GatherCsr<T>{gu_ptr.p, gu_slot.p, D.gu_w.p, cmask_u.p};
+    return GatherCsr<T>{gp_ptr.p, gp_slot.p, D.gp_w.p, cmask_p.p};
+  }
+  size_t device_bytes() const;
+};
+
+template <>
+inline LevelDev<float>& Level::dev<float>() { return f32; }
+template <>
+inline LevelDev<double>& Level::dev<double>() { return f64; }
+
+// set-up steps (level_setup.cu)
+void setup_level(Level& L, bool force_indexed);
+void setup_transfer(Level& fine, const Level& coarse);
+void compute_level_viscosity(std::vector<Level>& levels, const double* eta_in, int n_per_cell, int projection,
+                             double& eta_min, double& eta_max);
+void upload_viscosity(Level& L);
+
+}  // namespace gb

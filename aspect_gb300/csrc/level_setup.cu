@@ -1,0 +1,755 @@
+// Level set-up on the host: internal layout, colouring, constraint encoding,
+// geometry tables, diagonal probes, transfer operators and viscosity tables.
+//
+// A level whose cells are equal axis-aligned boxes filling a lattice, with
+// velocity constraints that are whole (face, component) Dirichlet sets, is
+// renumbered lexicographically with the velocity components blocked; its cell
+// kernels then compute every index and constraint from the cell's lattice
+// position and read no index arrays at all. Every other level keeps the
+// caller's numbering and uses index arrays with encoded constraint lines.
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <set>
+
+#include "level.cuh"
+
+namespace gb {
+
+Expansion expand(const HostCons& c, int g) {
+  Expansion e;
+  const int l = c.line_of[g];
+  if (l < 0) {
+    e.n = 1;
+    e.g[0] = g;
+    e.w[0] = 1.0;
+    return e;
+  }
+  e.n = c.ptr[l + 1] - c.ptr[l];
+  GB_CHECK(e.n <= 16, 1, "constraint line with more than 16 entries");
+  for (int k = 0; k < e.n; ++k) {
+    e.g[k] = c.cols[c.ptr[l] + k];
+    e.w[k] = c.w[c.ptr[l] + k];
+  }
+  return e;
+}
+
+Csr Csr::transpose(long n_cols) const {
+  Csr t;
+  t.ptr.assign(n_cols + 1, 0);
+  for (int c : col) t.ptr[c + 1]++;
+  for (long i = 0; i < n_cols; ++i) t.ptr[i + 1] += t.ptr[i];
+  t.col.resize(col.size());
+  t.val.resize(val.size());
+  std::vector<int> fill(t.ptr.begin(), t.ptr.end() - 1);
+  for (long r = 0; r < rows(); ++r)
+    for (int k = ptr[r]; k < ptr[r + 1]; ++k) {
+      const int c = col[k];
+      t.col[fill[c]] = (int)r;
+      t.val[fill[c]] = val[k];
+      ++fill[c];
+    }
+  return t;
+}
+
+namespace {
+
+int nv_of(int dim) { return dim == 3 ? 27 : 9; }
+int np_of(int dim) { return dim == 3 ? 8 : 4; }
+
+// ---------------------------------------------------------------- 1D basis (host)
+void lagrange(const double* nodes, int n, double x, double* val, double* der) {
+  for (int i = 0; i < n; ++i) {
+    double v = 1, d = 0, den = 1;
+    for (int m = 0; m < n; ++m)
+      if (m != i) den *= nodes[i] - nodes[m];
+    for (int m = 0; m < n; ++m) {
+      if (m == i) continue;
+      double t = 1;
+      for (int k = 0; k < n; ++k)
+        if (k != i && k != m) t *= x - nodes[k];
+      d += t;
+      v *= x - nodes[m];
+    }
+    val[i] = v / den;
+    der[i] = d / den;
+  }
+}
+
+// ---------------------------------------------------------------- structure detection
+bool detect_structured(Level& L) {
+  const int d = L.dim, nv = nv_of(d), np = np_of(d), nu = d * nv;
+  if (L.geom_kind != 0 || L.n_cells == 0) return false;
+  // pressure constraints are not part of the lattice fast path
+  for (long g = 0; g < L.n_p; ++g)
+    if (L.cp.constrained((int)g)) return false;
+  double h[3], lo[3], hi[3];
+  for (int e = 0; e < d; ++e) {
+    h[e] = L.geom[d + e];
+    lo[e] = 1e300;
+    hi[e] = -1e300;
+  }
+  for (long c = 0; c < L.n_cells; ++c)
+    for (int e = 0; e < d; ++e) {
+      const double he = L.geom[c * 2 * d + d + e];
+      if (std::fabs(he - h[e]) > 1e-12 * std::fabs(h[e])) return false;
+      lo[e] = std::min(lo[e], L.geom[c * 2 * d + e]);
+      hi[e] = std::max(hi[e], L.geom[c * 2 * d + e]);
+    }
+  long total = 1;
+  int nc[3] = {1, 1, 1};
+  for (int e = 0; e < d; ++e) {
+    const double r = (hi[e] - lo[e]) / h[e];
+    nc[e] = (int)std::lround(r) + 1;
+    if (std::fabs(r - (nc[e] - 1)) > 1e-6) return false;
+    total *= nc[e];
+  }
+  if (total != L.n_cells) return false;
+  const int Nn[3] = {2 * nc[0] + 1, 2 * nc[1] + 1, d == 3 ? 2 * nc[2] + 1 : 1};
+  const int Np[3] = {nc[0] + 1, nc[1] + 1, d == 3 ? nc[2] + 1 : 1};
+  const long n_nodes = (long)Nn[0] * Nn[1] * Nn[2];
+  const long n_pnodes = (long)Np[0] * Np[1] * Np[2];
+  if (d * n_nodes != L.n_u || n_pnodes != L.n_p) return false;
+  std::vector<int> perm_u(L.n_u, -1), perm_p(L.n_p, -1), used_u(L.n_u, 0), used_p(L.n_p, 0);
+  std::vector<int> ioc(L.n_cells, -1);
+  std::vector<char> cell_seen(L.n_cells, 0);
+  for (long c = 0; c < L.n_cells; ++c) {
+    int ijk[3] = {0, 0, 0};
+    for (int e = 0; e < d; ++e) {
+      const double r = (L.geom[c * 2 * d + e] - lo[e]) / h[e];
+      ijk[e] = (int)std::lround(r);
+      if (std::fabs(r - ijk[e]) > 1e-6) return false;
+    }
+    const long ic = ((long)ijk[2] * nc[1] + ijk[1]) * nc[0] + ijk[0];
+    if (cell_seen[ic]) return false;
+    cell_seen[ic] = 1;
+    ioc[c] = (int)ic;
+    for (int comp = 0; comp < d; ++comp)
+      for (int n = 0; n < nv; ++n) {
+        const int a = n % 3, b = (n / 3) % 3, cc = n / 9;
+        const long node = ((long)(2 * ijk[2] + cc) * Nn[1] + (2 * ijk[1] + b)) * Nn[0] + 2 * ijk[0] + a;
+        const long internal = comp * n_nodes + node;
+        const int g = L.cdu[c * nu + comp * nv + n];
+        if (g < 0 || g >= L.n_u) return false;
+        if (perm_u[g] == -1) {
+          if (used_u[internal]) return false;
+          perm_u[g] = (int)internal;
+          used_u[internal] = 1;
+        } else if (perm_u[g] != internal) {
+          return false;
+        }
+      }
+    for (int n = 0; n < np; ++n) {
+      const int a = n & 1, b = (n >> 1) & 1, cc = (n >> 2) & 1;
+      const long node = ((long)(ijk[2] + cc) * Np[1] + (ijk[1] + b)) * Np[0] + ijk[0] + a;
+      const int g = L.cdp[c * np + n];
+      if (g < 0 || g >= L.n_p) return false;
+      if (perm_p[g] == -1) {
+        if (used_p[node]) return false;
+        perm_p[g] = (int)node;
+        used_p[node] = 1;
+      } else if (perm_p[g] != node) {
+        return false;
+      }
+    }
+  }
+  // velocity constraints: Dirichlet lines forming whole (face, component) sets
+  std::vector<char> cons_internal(L.n_u, 0);
+  for (long g = 0; g < L.n_u; ++g) {
+    if (!L.cu.constrained((int)g)) continue;
+    if (L.cu.n_entries((int)g) != 0) return false;
+    cons_internal[perm_u[g]] = 1;
+  }
+  uint32_t zf = 0;
+  for (int e = 0; e < d; ++e)
+    for (int side = 0; side < 2; ++side)
+      for (int comp = 0; comp < d; ++comp) {
+        bool all = true;
+        const int fixed = side ? Nn[e] - 1 : 0;
+        for (long node = 0; node < n_nodes && all; ++node) {
+          const int gi[3] = {(int)(node % Nn[0]), (int)((node / Nn[0]) % Nn[1]), (int)(node / ((long)Nn[0] * Nn[1]))};
+          if (gi[e] != fixed) continue;
+          if (!cons_internal[comp * n_nodes + node]) all = false;
+        }
+        if (all) zf |= 1u << ((2 * e + side) * 3 + comp);
+      }
+  // every constrained DoF must be covered by the face sets and vice versa
+  std::vector<int> cons_list;
+  for (long node = 0; node < n_nodes; ++node) {
+    const int gi[3] = {(int)(node % Nn[0]), (int)((node / Nn[0]) % Nn[1]), (int)(node / ((long)Nn[0] * Nn[1]))};
+    for (int comp = 0; comp < d; ++comp) {
+      bool z = false;
+      for (int e = 0; e < d; ++e) {
+        if (gi[e] == 0 && ((zf >> ((2 * e) * 3 + comp)) & 1u)) z = true;
+        if (gi[e] == Nn[e] - 1 && ((zf >> ((2 * e + 1) * 3 + comp)) & 1u)) z = true;
+      }
+      if (z != (bool)cons_internal[comp * n_nodes + node]) return false;
+      if (z) cons_list.push_back((int)(comp * n_nodes + node));
+    }
+  }
+  std::sort(cons_list.begin(), cons_list.end());
+  // accepted
+  L.structured = true;
+  for (int e = 0; e < 3; ++e) {
+    L.nc[e] = e < d ? nc[e] : 1;
+    L.h[e] = e < d ? h[e] : 1.0;
+  }
+  L.zero_faces = zf;
+  L.perm_u = std::move(perm_u);
+  L.perm_p = std::move(perm_p);
+  L.internal_of_cell = ioc;
+  L.cell_of_internal.assign(L.n_cells, 0);
+  for (long c = 0; c < L.n_cells; ++c) L.cell_of_internal[ioc[c]] = (int)c;
+  L.cons_u = cons_list;
+  L.cons_p.clear();
+  const int ncol = d == 3 ? 8 : 4;
+  L.n_colours = ncol;
+  L.colour_begin.assign(ncol, 0);
+  L.colour_count.assign(ncol, 0);
+  for (int k = 0; k < ncol; ++k) {
+    long cnt = 1;
+    for (int e = 0; e < d; ++e) cnt *= (nc[e] - ((k >> e) & 1) + 1) / 2;
+    L.colour_count[k] = (int)cnt;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------- general levels
+void setup_general(Level& L) {
+  const int d = L.dim, nv = nv_of(d), np = np_of(d), nu = d * nv, nq = nv;
+  L.structured = false;
+  L.perm_u.resize(L.n_u);
+  L.perm_p.resize(L.n_p);
+  for (long i = 0; i < L.n_u; ++i) L.perm_u[i] = (int)i;
+  for (long i = 0; i < L.n_p; ++i) L.perm_p[i] = (int)i;
+  // greedy colouring on the DoFs each cell writes (after constraint expansion)
+  std::vector<std::vector<int>> writes(L.n_cells);
+  for (long c = 0; c < L.n_cells; ++c) {
+    std::set<int> s;
+    for (int i = 0; i < nu; ++i) {
+      Expansion e = expand(L.cu, L.cdu[c * nu + i]);
+      for (int k = 0; k < e.n; ++k) s.insert(e.g[k]);
+    }
+    for (int i = 0; i < np; ++i) {
+      Expansion e = expand(L.cp, L.cdp[c * np + i]);
+      for (int k = 0; k < e.n; ++k) s.insert((int)(L.n_u + e.g[k]));
+    }
+    writes[c].assign(s.begin(), s.end());
+  }
+  std::vector<std::vector<int>> cells_of(L.n_u + L.n_p);
+  for (long c = 0; c < L.n_cells; ++c)
+    for (int g : writes[c]) cells_of[g].push_back((int)c);
+  std::vector<int> col(L.n_cells, -1);
+  int ncol = 0;
+  for (long c = 0; c < L.n_cells; ++c) {
+    std::vector<char> used(ncol + 1, 0);
+    for (int g : writes[c])
+      for (int o : cells_of[g])
+        if (col[o] >= 0) used[col[o]] = 1;
+    int k = 0;
+    while (used[k]) ++k;
+    col[c] = k;
+    ncol = std::max(ncol, k + 1);
+  }
+  L.n_colours = ncol;
+  L.colour_count.assign(ncol, 0);
+  for (long c = 0; c < L.n_cells; ++c) L.colour_count[col[c]]++;
+  L.colour_begin.assign(ncol, 0);
+  for (int k = 1; k < ncol; ++k) L.colour_begin[k] = L.colour_begin[k - 1] + L.colour_count[k - 1];
+  std::vector<int> fill(L.colour_begin);
+  L.internal_of_cell.assign(L.n_cells, 0);
+  L.cell_of_internal.assign(L.n_cells, 0);
+  for (long c = 0; c < L.n_cells; ++c) {
+    const int ic = fill[col[c]]++;
+    L.internal_of_cell[c] = ic;
+    L.cell_of_internal[ic] = (int)c;
+  }
+  // constraint lines with entries get compact ids; Dirichlet lines become -1
+  auto encode_lines = [&](const HostCons& C, long n, std::vector<int>& line_id, std::vector<int>& lptr,
+                          std::vector<int>& lcol, std::vector<double>& lw, std::vector<int>& cons) {
+    line_id.assign(n, -1);
+    lptr.assign(1, 0);
+    lcol.clear();
+    lw.clear();
+    cons.clear();
+    for (long g = 0; g < n; ++g) {
+      if (!C.constrained((int)g)) continue;
+      cons.push_back((int)g);
+      const int ne = C.n_entries((int)g);
+      if (ne == 0) continue;
+      line_id[g] = (int)lptr.size() - 1;
+      const int l = C.line_of[g];
+      for (int k = C.ptr[l]; k < C.ptr[l + 1]; ++k) {
+        GB_CHECK(!C.constrained(C.cols[k]), 1, "constraints are not closed (a master is constrained)");
+        lcol.push_back(C.cols[k]);
+        lw.push_back(C.w[k]);
+      }
+      lptr.push_back((int)lcol.size());
+    }
+  };
+  std::vector<int> lid_u, lptr_u, lcol_u, lid_p, lptr_p, lcol_p;
+  std::vector<double> lw_u, lw_p;
+  encode_lines(L.cu, L.n_u, lid_u, lptr_u, lcol_u, lw_u, L.cons_u);
+  encode_lines(L.cp, L.n_p, lid_p, lptr_p, lcol_p, lw_p, L.cons_p);
+  auto code = [](const HostCons& C, const std::vector<int>& lid, int g) -> int {
+    if (!C.constrained(g)) return g;
+    return lid[g] < 0 ? -1 : -(lid[g] + 2);
+  };
+  std::vector<int> cdu(L.n_cells * nu), cdp(L.n_cells * np);
+  for (long c = 0; c < L.n_cells; ++c) {
+    const long ic = L.internal_of_cell[c];
+    for (int i = 0; i < nu; ++i) cdu[ic * nu + i] = code(L.cu, lid_u, L.cdu[c * nu + i]);
+    for (int i = 0; i < np; ++i) cdp[ic * np + i] = code(L.cp, lid_p, L.cdp[c * np + i]);
+  }
+  L.cdu_d.upload(cdu);
+  L.cdp_d.upload(cdp);
+  L.lptr_d.upload(lptr_u);
+  L.lcol_d.upload(lcol_u);
+  L.plptr_d.upload(lptr_p);
+  L.plcol_d.upload(lcol_p);
+  L.f64.lw.upload(lw_u);
+  L.f64.plw.upload(lw_p);
+  L.f32.lw.upload(std::vector<float>(lw_u.begin(), lw_u.end()));
+  L.f32.plw.upload(std::vector<float>(lw_p.begin(), lw_p.end()));
+  // geometry
+  if (L.geom_kind == 0) {
+    std::vector<double> gb((size_t)L.n_cells * (d + 1));
+    for (long c = 0; c < L.n_cells; ++c) {
+      const long ic = L.internal_of_cell[c];
+      double det = 1;
+      for (int e = 0; e < d; ++e) {
+        const double he = L.geom[c * 2 * d + d + e];
+        gb[ic * (d + 1) + e] = 1.0 / he;
+        det *= he;
+      }
+      gb[ic * (d + 1) + d] = det;
+    }
+    L.f64.gbox.upload(gb);
+    L.f32.gbox.upload(std::vector<float>(gb.begin(), gb.end()));
+  } else {
+    const double g3[3] = {0.5 - std::sqrt(15.0) / 10, 0.5, 0.5 + std::sqrt(15.0) / 10};
+    const double q2n[3] = {0.0, 0.5, 1.0};
+    double v1[3][3], d1[3][3];
+    for (int q = 0; q < 3; ++q) lagrange(q2n, 3, g3[q], v1[q], d1[q]);
+    const int stride = d * d + 1;
+    std::vector<double> gt((size_t)L.n_cells * nq * stride);
+    for (long c = 0; c < L.n_cells; ++c) {
+      const long ic = L.internal_of_cell[c];
+      const double* X = &L.geom[(size_t)c * nv * d];
+      for (int q = 0; q < nq; ++q) {
+        const int qi[3] = {q % 3, (q / 3) % 3, q / 9};
+        double J[3][3] = {{0}};
+        for (int n = 0; n < nv; ++n) {
+          const int ni[3] = {n % 3, (n / 3) % 3, n / 9};
+          for (int b = 0; b < d; ++b) {
+            double t = 1;
+            for (int e = 0; e < d; ++e) t *= (e == b ? d1[qi[e]][ni[e]] : v1[qi[e]][ni[e]]);
+            for (int a = 0; a < d; ++a) J[a][b] += X[n * d + a] * t;
+          }
+        }
+        double det, inv[3][3];
+        if (d == 2) {
+          det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+          inv[0][0] = J[1][1] / det;
+          inv[0][1] = -J[0][1] / det;
+          inv[1][0] = -J[1][0] / det;
+          inv[1][1] = J[0][0] / det;
+        } else {
+          det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+          inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+          inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+          inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+          inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+          inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+          inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+          inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+          inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+          inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+        }
+        GB_CHECK(det != 0, 1, "degenerate cell geometry");
+        double* o = &gt[((size_t)ic * nq + q) * stride];
+        for (int a = 0; a < d; ++a)
+          for (int b = 0; b < d; ++b) o[a * d + b] = inv[a][b];
+        o[d * d] = std::fabs(det);
+      }
+    }
+    L.f64.gtab.upload(gt);
+    L.f32.gtab.upload(std::vector<float>(gt.begin(), gt.end()));
+  }
+  // pass-2 gather lists: for every DoF, the (cell, local slot, weight) entries
+  // that contribute to it, constraint lines folded in; sorted by slot
+  auto build_gather = [&](const std::vector<int>& cd, const HostCons& C, int nl, long n, DevBuf<int>& gptr,
+                          DevBuf<int>& gslot, DevBuf<double>& gw64, DevBuf<float>& gw32, DevBuf<unsigned char>& cm) {
+    std::vector<std::vector<std::pair<long, double>>> ent(n);
+    for (long ic = 0; ic < L.n_cells; ++ic) {
+      const long c = L.cell_of_internal[ic];
+      for (int i = 0; i < nl; ++i) {
+        Expansion e = expand(C, cd[c * nl + i]);
+        for (int k = 0; k < e.n; ++k) ent[e.g[k]].push_back({ic * nl + i, e.w[k]});
+      }
+    }
+    std::vector<int> ptr(1, 0), slot;
+    std::vector<double> w;
+    std::vector<unsigned char> mask(n, 0);
+    for (long g = 0; g < n; ++g) {
+      mask[g] = C.constrained((int)g) ? 1 : 0;
+      for (auto& pr : ent[g]) {
+        GB_CHECK(pr.first < (1L << 31), 1, "level too large for 32-bit gather slots");
+        slot.push_back((int)pr.first);
+        w.push_back(pr.second);
+      }
+      ptr.push_back((int)slot.size());
+    }
+    gptr.upload(ptr);
+    gslot.upload(slot);
+    gw64.upload(w);
+    gw32.upload(std::vector<float>(w.begin(), w.end()));
+    cm.upload(mask);
+  };
+  build_gather(L.cdu, L.cu, nu, L.n_u, L.gu_ptr, L.gu_slot, L.f64.gu_w, L.f32.gu_w, L.cmask_u);
+  build_gather(L.cdp, L.cp, np, L.n_p, L.gp_ptr, L.gp_slot, L.f64.gp_w, L.f32.gp_w, L.cmask_p);
+  // diagonal probes: per internal cell, the unconstrained DoFs it touches
+  auto build_probes = [&](const std::vector<int>& cd, const HostCons& C, int nl, DevBuf<int>& pptr, DevBuf<int>& pg,
+                          DevBuf<int>& peptr, DevBuf<int>& pli, DevBuf<double>& pw64, DevBuf<float>& pw32) {
+    std::vector<int> ptr(1, 0), g, eptr(1, 0), li;
+    std::vector<double> w;
+    for (long ic = 0; ic < L.n_cells; ++ic) {
+      const long c = L.cell_of_internal[ic];
+      std::map<int, std::vector<std::pair<int, double>>> m;
+      for (int i = 0; i < nl; ++i) {
+        Expansion e = expand(C, cd[c * nl + i]);
+        for (int k = 0; k < e.n; ++k) m[e.g[k]].push_back({i, e.w[k]});
+      }
+      for (auto& kv : m) {
+        g.push_back(kv.first);
+        for (auto& p : kv.second) {
+          li.push_back(p.first);
+          w.push_back(p.second);
+        }
+        eptr.push_back((int)li.size());
+      }
+      ptr.push_back((int)g.size());
+    }
+    pptr.upload(ptr);
+    pg.upload(g);
+    peptr.upload(eptr);
+    pli.upload(li);
+    pw64.upload(w);
+    pw32.upload(std::vector<float>(w.begin(), w.end()));
+  };
+  build_probes(L.cdu, L.cu, nu, L.probe_ptr, L.probe_g, L.probe_eptr, L.probe_li, L.f64.probe_w, L.f32.probe_w);
+  build_probes(L.cdp, L.cp, np, L.pprobe_ptr, L.pprobe_g, L.pprobe_eptr, L.pprobe_li, L.f64.pprobe_w,
+               L.f32.pprobe_w);
+}
+
+}  // namespace
+
+void setup_level(Level& L, bool force_indexed) {
+  if (force_indexed || !detect_structured(L)) setup_general(L);
+  const int nu = L.dim * nv_of(L.dim), np = np_of(L.dim);
+  L.f64.Eu.alloc((size_t)L.n_cells * nu);
+  L.f64.Ep.alloc((size_t)L.n_cells * np);
+  L.f32.Eu.alloc((size_t)L.n_cells * nu);
+  L.f32.Ep.alloc((size_t)L.n_cells * np);
+  L.perm_u_d.upload(L.perm_u);
+  L.perm_p_d.upload(L.perm_p);
+  L.cons_u_d.upload(L.cons_u);
+  L.cons_p_d.upload(L.cons_p);
+}
+
+// Prolongation from `coarse` to `fine` (rows: fine internal unconstrained DoFs,
+// columns: coarse internal DoFs): the coarse FE function, with its constraints
+// resolved, evaluated at the fine support points (reference coordinates of the
+// child inside its parent). Restriction is the transpose.
+void setup_transfer(Level& F, const Level& C) {
+  const int d = F.dim, nv = nv_of(d), np = np_of(d), nu = d * nv;
+  GB_CHECK(F.has_transfer, 2, "missing child/parent data for a level");
+  const double q2n[3] = {0.0, 0.5, 1.0}, q1n[2] = {0.0, 1.0};
+  for (int block = 0; block < 2; ++block) {
+    const int nl = block == 0 ? nv : np;
+    const int ncomp = block == 0 ? d : 1;
+    const long nf = block == 0 ? F.n_u : F.n_p;
+    const HostCons& FC = block == 0 ? F.cu : F.cp;
+    const HostCons& CC = block == 0 ? C.cu : C.cp;
+    const std::vector<int>& fperm = block == 0 ? F.perm_u : F.perm_p;
+    const std::vector<int>& cperm = block == 0 ? C.perm_u : C.perm_p;
+    std::vector<std::map<int, double>> rows(nf);
+    std::vector<char> done(nf, 0);
+    for (long fc = 0; fc < F.n_cells; ++fc) {
+      const int pc = F.parent[fc], ch = F.child[fc];
+      GB_CHECK(pc >= 0 && pc < C.n_cells, 1, "parent index out of range");
+      for (int n = 0; n < nl; ++n) {
+        double xi[3];
+        for (int e = 0; e < d; ++e) {
+          const int idx = block == 0 ? (e == 0 ? n % 3 : e == 1 ? (n / 3) % 3 : n / 9)
+                                     : (e == 0 ? n % 2 : e == 1 ? (n / 2) % 2 : n / 4);
+          const double loc = block == 0 ? 0.5 * idx : (double)idx;
+          xi[e] = 0.5 * (((ch >> e) & 1) + loc);
+        }
+        double phi[27];
+        double vv[3][3], dd[3][3];
+        for (int e = 0; e < d; ++e) lagrange(block == 0 ? q2n : q1n, block == 0 ? 3 : 2, xi[e], vv[e], dd[e]);
+        for (int m = 0; m < nl; ++m) {
+          double t = 1;
+          for (int e = 0; e < d; ++e) {
+            const int mi = block == 0 ? (e == 0 ? m % 3 : e == 1 ? (m / 3) % 3 : m / 9)
+                                      : (e == 0 ? m % 2 : e == 1 ? (m / 2) % 2 : m / 4);
+            t *= vv[e][mi];
+          }
+          phi[m] = t;
+        }
+        for (int comp = 0; comp < ncomp; ++comp) {
+          const int gf = block == 0 ? F.cdu[fc * nu + comp * nl + n] : F.cdp[fc * np + n];
+          if (FC.constrained(gf) || done[gf]) continue;
+          done[gf] = 1;
+          for (int m = 0; m < nl; ++m) {
+            if (std::fabs(phi[m]) < 1e-14) continue;
+            const int gc = block == 0 ? C.cdu[(long)pc * nu + comp * nl + m] : C.cdp[(long)pc * np + m];
+            Expansion e = expand(CC, gc);
+            for (int k = 0; k < e.n; ++k) rows[gf][e.g[k]] += phi[m] * e.w[k];
+          }
+        }
+      }
+    }
+    // internal numbering
+    std::vector<std::map<int, double>> irows(nf);
+    for (long g = 0; g < nf; ++g)
+      for (auto& kv : rows[g]) irows[fperm[g]][cperm[kv.first]] += kv.second;
+    Csr P;
+    for (long r = 0; r < nf; ++r) {
+      for (auto& kv : irows[r])
+        if (std::fabs(kv.second) > 1e-14) {
+          P.col.push_back(kv.first);
+          P.val.push_back(kv.second);
+        }
+      P.ptr.push_back((int)P.col.size());
+    }
+    Csr PT = P.transpose(block == 0 ? C.n_u : C.n_p);
+    if (block == 0) {
+      F.Pu_ptr.upload(P.ptr); F.Pu_col.upload(P.col); F.Pu_rows = P.rows();
+      F.PuT_ptr.upload(PT.ptr); F.PuT_col.upload(PT.col); F.PuT_rows = PT.rows();
+      F.f64.Pu_val.upload(P.val); F.f64.PuT_val.upload(PT.val);
+      F.f32.Pu_val.upload(std::vector<float>(P.val.begin(), P.val.end()));
+      F.f32.PuT_val.upload(std::vector<float>(PT.val.begin(), PT.val.end()));
+    } else {
+      F.Pp_ptr.upload(P.ptr); F.Pp_col.upload(P.col); F.Pp_rows = P.rows();
+      F.PpT_ptr.upload(PT.ptr); F.PpT_col.upload(PT.col); F.PpT_rows = PT.rows();
+      F.f64.Pp_val.upload(P.val); F.f64.PpT_val.upload(PT.val);
+      F.f32.Pp_val.upload(std::vector<float>(P.val.begin(), P.val.end()));
+      F.f32.PpT_val.upload(std::vector<float>(PT.val.begin(), PT.val.end()));
+    }
+  }
+}
+
+// Level viscosity tables (stokes_matrix_free_local_smoothing.cc:174-294), in
+// caller cell order into Level::eta (then permuted by upload_viscosity).
+void compute_level_viscosity(std::vector<Level>& levels, const double* eta_in, int n_per_cell, int projection,
+                             double& eta_min, double& eta_max) {
+  const int nlev = (int)levels.size();
+  Level& Fl = levels.back();
+  const int d = Fl.dim, nq = nv_of(d), ncv = np_of(d);
+  eta_min = 1e300;
+  eta_max = -1e300;
+  for (long i = 0; i < Fl.n_cells * n_per_cell; ++i) {
+    GB_CHECK(eta_in[i] > 0 && std::isfinite(eta_in[i]), 6, "viscosity must be positive and finite");
+    eta_min = std::min(eta_min, eta_in[i]);
+    eta_max = std::max(eta_max, eta_in[i]);
+  }
+  // JxW of the finest level per quadrature point (for the DGQ0 projection)
+  const double g3[3] = {0.5 - std::sqrt(15.0) / 10, 0.5, 0.5 + std::sqrt(15.0) / 10};
+  const double w3[3] = {5.0 / 18, 8.0 / 18, 5.0 / 18};
+  double psi[27][8];
+  for (int q = 0; q < nq; ++q) {
+    const int qi[3] = {q % 3, (q / 3) % 3, q / 9};
+    for (int n = 0; n < ncv; ++n) {
+      double t = 1;
+      for (int e = 0; e < d; ++e) t *= ((n >> e) & 1) ? g3[qi[e]] : 1 - g3[qi[e]];
+      psi[q][n] = t;
+    }
+  }
+  auto jxw_of = [&](long c, int q) {
+    // volume weight; cells of one level have their own Jacobians
+    const int qi[3] = {q % 3, (q / 3) % 3, q / 9};
+    double w = 1;
+    for (int e = 0; e < d; ++e) w *= w3[qi[e]];
+    if (Fl.geom_kind == 0) {
+      double det = 1;
+      for (int e = 0; e < d; ++e) det *= Fl.geom[c * 2 * d + d + e];
+      return w * det;
+    }
+    // Q2 geometry: recompute |det J| at the point
+    const double q2n[3] = {0.0, 0.5, 1.0};
+    double v1[3][3], d1[3][3];
+    for (int e = 0; e < d; ++e) lagrange(q2n, 3, g3[qi[e]], v1[e], d1[e]);
+    double J[3][3] = {{0}};
+    const double* X = &Fl.geom[(size_t)c * nq * d];
+    for (int n = 0; n < nq; ++n) {
+      const int ni[3] = {n % 3, (n / 3) % 3, n / 9};
+      for (int b = 0; b < d; ++b) {
+        double t = 1;
+        for (int e = 0; e < d; ++e) t *= (e == b ? d1[e][ni[e]] : v1[e][ni[e]]);
+        for (int a = 0; a < d; ++a) J[a][b] += X[n * d + a] * t;
+      }
+    }
+    double det = d == 2 ? J[0][0] * J[1][1] - J[0][1] * J[1][0]
+                        : J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                              J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                              J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    return w * std::fabs(det);
+  };
+  std::vector<std::vector<double>> dg(nlev);
+  if (projection == 0) {
+    dg[nlev - 1].assign(Fl.n_cells, 0.0);
+    for (long c = 0; c < Fl.n_cells; ++c) {
+      if (n_per_cell == 1) {
+        dg[nlev - 1][c] = eta_in[c];
+      } else {
+        double a = 0, v = 0;
+        for (int q = 0; q < nq; ++q) {
+          const double jw = jxw_of(c, q);
+          a += jw * eta_in[c * nq + q];
+          v += jw;
+        }
+        dg[nlev - 1][c] = a / v;
+      }
+    }
+    for (int l = nlev - 1; l > 0; --l) {
+      Level& F = levels[l];
+      std::vector<double> sum(levels[l - 1].n_cells, 0.0), cnt(levels[l - 1].n_cells, 0.0);
+      for (long c = 0; c < F.n_cells; ++c) {
+        sum[F.parent[c]] += dg[l][c];
+        cnt[F.parent[c]] += 1;
+      }
+      dg[l - 1].resize(levels[l - 1].n_cells);
+      for (size_t c = 0; c < sum.size(); ++c) dg[l - 1][c] = sum[c] / cnt[c];
+    }
+    for (int l = 0; l < nlev; ++l) {
+      Level& L = levels[l];
+      const bool per_q = (l == nlev - 1 && n_per_cell == nq);
+      L.eta_n = per_q ? nq : 1;
+      L.eta.assign((size_t)L.n_cells * L.eta_n, 0);
+      for (long c = 0; c < L.n_cells; ++c) {
+        if (per_q)
+          for (int q = 0; q < nq; ++q) L.eta[c * nq + q] = eta_in[c * nq + q];
+        else
+          L.eta[c] = dg[l][c];
+      }
+    }
+  } else {
+    GB_CHECK(n_per_cell == nq, 1, "projection to Q1 needs one value per quadrature point");
+    dg[nlev - 1].assign((size_t)Fl.n_cells * ncv, 0.0);
+    for (long c = 0; c < Fl.n_cells; ++c) {
+      double M[8][8] = {{0}}, b[8] = {0}, x[8];
+      for (int q = 0; q < nq; ++q) {
+        const double jw = jxw_of(c, q);
+        for (int i = 0; i < ncv; ++i) {
+          b[i] += jw * psi[q][i] * eta_in[c * nq + q];
+          for (int j = 0; j < ncv; ++j) M[i][j] += jw * psi[q][i] * psi[q][j];
+        }
+      }
+      for (int i = 0; i < ncv; ++i)
+        for (int r = i + 1; r < ncv; ++r) {
+          const double f = M[r][i] / M[i][i];
+          for (int k = i; k < ncv; ++k) M[r][k] -= f * M[i][k];
+          b[r] -= f * b[i];
+        }
+      for (int i = ncv - 1; i >= 0; --i) {
+        double t = b[i];
+        for (int k = i + 1; k < ncv; ++k) t -= M[i][k] * x[k];
+        x[i] = t / M[i][i];
+      }
+      for (int i = 0; i < ncv; ++i) dg[nlev - 1][c * ncv + i] = x[i];
+    }
+    for (int l = nlev - 1; l > 0; --l) {
+      Level& F = levels[l];
+      dg[l - 1].assign((size_t)levels[l - 1].n_cells * ncv, 0.0);
+      for (long c = 0; c < F.n_cells; ++c) {
+        const int ch = F.child[c], p = F.parent[c];
+        dg[l - 1][(size_t)p * ncv + ch] = dg[l][c * ncv + ch];
+      }
+    }
+    for (int l = 0; l < nlev; ++l) {
+      Level& L = levels[l];
+      L.eta_n = nq;
+      L.eta.assign((size_t)L.n_cells * nq, 0);
+      for (long c = 0; c < L.n_cells; ++c)
+        for (int q = 0; q < nq; ++q) {
+          double v = 0;
+          for (int i = 0; i < ncv; ++i) v += psi[q][i] * dg[l][c * ncv + i];
+          L.eta[c * nq + q] = std::min(std::max(v, eta_min), eta_max);
+        }
+    }
+  }
+}
+
+void upload_viscosity(Level& L) {
+  std::vector<double> e((size_t)L.n_cells * L.eta_n);
+  for (long c = 0; c < L.n_cells; ++c) {
+    const long ic = L.internal_of_cell[c];
+    for (int k = 0; k < L.eta_n; ++k) e[ic * L.eta_n + k] = L.eta[c * L.eta_n + k];
+  }
+  L.f64.eta.upload(e);
+  L.f32.eta.upload(std::vector<float>(e.begin(), e.end()));
+}
+
+template <typename T>
+LevelView<T> Level::view(double s, int compressible) {
+  LevelView<T> v{};
+  LevelDev<T>& D = dev<T>();
+  v.dim = dim;
+  v.n_cells = (int)n_cells;
+  v.n_u = (int)n_u;
+  v.n_p = (int)n_p;
+  v.structured = structured ? 1 : 0;
+  for (int e = 0; e < 3; ++e) {
+    v.nc[e] = nc[e];
+    v.Nn[e] = e < dim ? 2 * nc[e] + 1 : 1;
+    v.Np[e] = e < dim ? nc[e] + 1 : 1;
+    v.inv_h[e] = (T)(1.0 / h[e]);
+  }
+  double det = 1;
+  for (int e = 0; e < dim; ++e) det *= h[e];
+  v.det = (T)det;
+  v.n_nodes = v.Nn[0] * v.Nn[1] * v.Nn[2];
+  v.zero_faces = zero_faces;
+  v.cdu = cdu_d.p;
+  v.cdp = cdp_d.p;
+  v.lptr = lptr_d.p;
+  v.lcol = lcol_d.p;
+  v.lw = D.lw.p;
+  v.plptr = plptr_d.p;
+  v.plcol = plcol_d.p;
+  v.plw = D.plw.p;
+  v.geom = structured ? GEOM_CART : (geom_kind == 0 ? GEOM_BOX : GEOM_TABLE);
+  v.gbox = D.gbox.p;
+  v.gtab = D.gtab.p;
+  v.eta = D.eta.p;
+  v.eta_n = eta_n;
+  v.s = (T)s;
+  v.compressible = compressible;
+  return v;
+}
+template LevelView<float> Level::view<float>(double, int);
+template LevelView<double> Level::view<double>(double, int);
+
+size_t Level::device_bytes() const {
+  size_t b = cdu_d.bytes() + cdp_d.bytes() + lptr_d.bytes() + lcol_d.bytes() + plptr_d.bytes() + plcol_d.bytes() +
+             perm_u_d.bytes() + perm_p_d.bytes() + cons_u_d.bytes() + cons_p_d.bytes() + probe_ptr.bytes() +
+             probe_g.bytes() + probe_eptr.bytes() + probe_li.bytes() + pprobe_ptr.bytes() + pprobe_g.bytes() +
+             pprobe_eptr.bytes() + pprobe_li.bytes() + Pu_ptr.bytes() + Pu_col.bytes() + PuT_ptr.bytes() +
+             PuT_col.bytes() + Pp_ptr.bytes() + Pp_col.bytes() + PpT_ptr.bytes() + PpT_col.bytes() + gu_ptr.bytes() +
+             gu_slot.bytes() + gp_ptr.bytes() + gp_slot.bytes() + cmask_u.bytes() + cmask_p.bytes();
+  auto add = [&](const auto& D) {
+    b += D.lw.bytes() + D.plw.bytes() + D.gbox.bytes() + D.gtab.bytes() + D.eta.bytes() + D.probe_w.bytes() +
+         D.pprobe_w.bytes() + D.Pu_val.bytes() + D.PuT_val.bytes() + D.Pp_val.bytes() + D.PpT_val.bytes() +
+         D.dinvA.bytes() + D.dinvM.bytes() + D.solA.bytes() + D.defA.bytes() + D.tA.bytes() + D.dA.bytes() +
+         D.solM.bytes() + D.defM.bytes() + D.tM.bytes() + D.dM.bytes() + D.gu_w.bytes() + D.gp_w.bytes() +
+         D.Eu.bytes() + D.Ep.bytes();
+  };
+  add(f32);
+  add(f64);
+  return b;
+}
+
+}  // namespace gb

@@ -1,0 +1,32 @@
+// Host-side launchers of the cell kernels.
+#pragma once
+#include "cell_kernels.cuh"
+
+namespace gb {
+
+// Per-cell diagonal probes of a general level (device pointers).
+template <typename T>
+struct ProbesView {
+  const int* ptr = nullptr;   // [n_cells+1]
+  const int* g = nullptr;     // [n_probes] target DoF
+  const int* eptr = nullptr;  // [n_probes+1]
+  const int* li = nullptr;    // [n_entries] cell-local index
+  const T* w = nullptr;       // [n_entries]
+};
+
+// pass 1 of an operator (op: OPK_*), all cells of the level
+template <typename T>
+void launch_cell_pass(const LevelView<T>& L, int op, const T* src_u, const T* src_p, T* Eu, T* Ep, cudaStream_t s);
+// pass 2 for block 0 (velocity DoFs) or 1 (pressure DoFs); csr == nullptr on lattice levels
+template <typename T>
+void launch_gather(const LevelView<T>& L, int block, int epi, const GatherCsr<T>* csr, const GatherArgs<T>& a,
+                   cudaStream_t s);
+// diagonals, colour by colour (set-up only)
+template <typename T>
+void launch_velocity_diag(const LevelView<T>& L, int colour, int begin, int count, const ProbesView<T>& pr,
+                          T* diag, cudaStream_t s);
+template <typename T>
+void launch_mass_diag(const LevelView<T>& L, int colour, int begin, int count, const ProbesView<T>& pr, T* diag,
+                      cudaStream_t s);
+
+}  // namespace gb

@@ -1,0 +1,62 @@
+// Vector kernels (HBM-bound) of the GMG V-cycle and the FP64 Krylov solver.
+#pragma once
+#include "common.cuh"
+
+namespace gb {
+
+// Fixed reduction grid: partial sums are formed per block in a fixed order and
+// summed in a fixed order, so every dot product is bit-reproducible.
+constexpr int kDotBlocks = 304;  // 2 x 152 SMs
+constexpr int kDotThreads = 256;
+constexpr int kDotChunk = 8;     // vectors per multi-dot launch
+
+struct VecCounter {
+  static long long& launches() {
+    static long long n = 0;
+    return n;
+  }
+};
+
+template <typename T>
+void v_axpby(long n, T a, const T* x, T b, T* y, cudaStream_t s);  // y = a x + b y
+template <typename T>
+void v_copy(long n, const T* x, T* y, cudaStream_t s);
+template <typename T>
+void v_scale(long n, T a, T* y, cudaStream_t s);
+template <typename Ts, typename Td>
+void v_cast(long n, const Ts* x, Td* y, cudaStream_t s);
+// Chebyshev: zero start  d = f2 * dinv * b, x = d
+template <typename T>
+void v_cheb_first(long n, const T* b, const T* dinv, T f2, T* d, T* x, cudaStream_t s);
+// Chebyshev step: d = f1 d + f2 dinv (b - t), x += d
+template <typename T>
+void v_cheb_step(long n, const T* b, const T* t, const T* dinv, T f1, T f2, T* d, T* x, cudaStream_t s);
+// out = a - b
+template <typename T>
+void v_sub(long n, const T* a, const T* b, T* out, cudaStream_t s);
+// dst[idx[k]] = src[idx[k]]
+template <typename T>
+void v_copy_indexed(long m, const int* idx, const T* src, T* dst, cudaStream_t s);
+template <typename T>
+void v_zero_indexed(long m, const int* idx, T* dst, cudaStream_t s);
+// out[perm[i]] = in[i] (scatter) or out[i] = in[perm[i]] (gather); Ts -> Td
+template <typename Ts, typename Td>
+void v_permute_scatter(long n, const int* perm, const Ts* in, Td* out, cudaStream_t s);
+template <typename Ts, typename Td>
+void v_permute_gather(long n, const int* perm, const Ts* in, Td* out, cudaStream_t s);
+// y += A x (CSR)
+template <typename T>
+void v_spmv_add(long rows, const int* ptr, const int* col, const T* val, const T* x, T* y, cudaStream_t s);
+// out[j] = <w, V_j> for j < k (V rows of stride ld), plus out[k] = <w, w> if with_norm
+// partial: workspace of (kDotChunk+1) * kDotBlocks doubles
+void v_multidot(long n, const double* w, const double* V, long ld, int k, bool with_norm, double* out_dev,
+                double* partial, cudaStream_t s);
+template <typename T>
+void v_dot(long n, const T* a, const T* b, double* out_dev, double* partial, cudaStream_t s);
+// w += sum_j coef[j] V_j  (coef on the device)
+void v_multiaxpy(long n, int k, const double* coef_dev, const double* V, long ld, double* w, cudaStream_t s);
+// NaN / Inf check: flag[0] |= 1 if any non-finite entry
+template <typename T>
+void v_check_finite(long n, const T* x, int* flag, cudaStream_t s);
+
+}  // namespace gb

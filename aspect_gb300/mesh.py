@@ -259,3 +259,25 @@ def permute_dofs(level: LevelMesh, seed: int) -> tuple[LevelMesh, np.ndarray, np
         dof_component_u=level.dof_component_u[inv_u] if level.dof_component_u is not None else None,
         dof_points_p=level.dof_points_p[inv_p] if level.dof_points_p is not None else None)
     return out, pu, pp
+
+
+def to_q2_geometry(level: LevelMesh, distortion=None) -> LevelMesh:
+    """Same level with GEOM_Q2 cell geometry (3^dim support points per cell),
+    optionally moved by ``distortion(x) -> dx`` (applied pointwise, so shared
+    points stay shared)."""
+    X = level.q2_support_points().copy()
+    if distortion is not None:
+        flat = X.reshape(-1, level.dim)
+        X = (flat + distortion(flat)).reshape(X.shape)
+    return dataclasses.replace(level, geom_kind=GEOM_Q2, geometry=X.reshape(level.n_cells, -1))
+
+
+def smooth_distortion(amplitude: float = 0.03):
+    """A displacement that vanishes on the boundary of the unit box."""
+    def f(x):
+        b = np.prod(np.sin(np.pi * x), axis=1)
+        d = np.zeros_like(x)
+        for k in range(x.shape[1]):
+            d[:, k] = amplitude * b * np.cos(np.pi * (k + 1) * x[:, (k + 1) % x.shape[1]])
+        return d
+    return f

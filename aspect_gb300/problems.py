@@ -195,15 +195,15 @@ def sinker_centres(seed: int, n: int = 8) -> np.ndarray:
     return 0.2 + 0.6 * rng.uniform(3 * n).reshape(n, 3)
 
 
-def sinker_viscosity(x: np.ndarray, centres: np.ndarray, contrast_power: float = 2.0) -> np.ndarray:
-    """eta0 = 1e-3 + (1 - 1e-3) prod_i (1 - exp(-d_i^2 / (2 0.05^2))), then eta0**2
-    (a 1e6 contrast, range 1e-6 .. 1)."""
+def sinker_viscosity(x: np.ndarray, centres: np.ndarray, eta_min: float = 1e-6) -> np.ndarray:
+    """eta = eta_min + (1 - eta_min) prod_i (1 - exp(-d_i^2 / (2 0.05^2))): the
+    smooth-sinker formula with its contrast parameter set to 1e6 (eta_min = 1e-6,
+    range 1e-6 .. 1)."""
     prod = np.ones(x.shape[:-1])
     for c in centres:
         d2 = np.sum((x - c) ** 2, -1)
         prod *= 1.0 - np.exp(-d2 / (2 * 0.05 ** 2))
-    eta0 = 1e-3 + (1 - 1e-3) * prod
-    return eta0 ** contrast_power
+    return eta_min + (1 - eta_min) * prod
 
 
 def sinker_density(x: np.ndarray, centres: np.ndarray, radius: float = 0.075) -> np.ndarray:
@@ -216,7 +216,8 @@ def sinker_density(x: np.ndarray, centres: np.ndarray, radius: float = 0.075) ->
 def sinkers_3d(n: int = 32, seed: int = BASE_SEED + 2, projection: int = 1,
                n_coarse: int = 1) -> StokesProblem:
     """3D unit cube, n^3 Q2-Q1 cells, 8 smooth sinkers (centres seeded uniform in
-    [0.2, 0.8]^3), eta = eta0**2 (1e6 contrast), rho = 1 inside r = 0.075, g = -z,
+    [0.2, 0.8]^3), eta = 1e-6 + (1-1e-6) prod_i(...) (1e6 contrast), rho = 1
+    inside r = 0.075, g = -z,
     free slip. ``projection`` = 1 uses ASPECT's default averaging for GMG
     (project to Q1 only viscosity: per-quadrature-point viscosity); 0 uses the
     harmonic cell average."""

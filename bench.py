@@ -1,0 +1,387 @@
+"""Benchmark: matrix-free GMG Stokes solve, FP32-MG vs FP64-MG at a 1e-8 FP64 residual.
+
+Workload (one step = one Stokes solve from a zero initial guess): 3D unit cube,
+32^3 Q2-Q1 cells (823,875 velocity + 35,937 pressure DoFs, 6 levels), 8 smooth
+sinkers (centres seeded SplitMix64 20261206), viscosity
+1e-6 + (1-1e-6) prod_i(1 - exp(-d_i^2/(2 0.05^2))) (1e6 contrast), per-quadrature-point viscosity with the Q1 projection (ASPECT's default
+averaging for GMG), free slip, FGMRES (restart 100) with the block-Schur
+preconditioner and an FP32 V-cycle, FP64 outer residual, relative tolerance 1e-8.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+`value` is DoFs solved per second with inputs resident in HBM (device-timed);
+`e2e` is the same through the host-array C ABI (gb_gmg_solve) with the host<->device
+copies inside the timed region. `--impl reference` times the CPU oracle (the
+FP64-MG restatement of the reference algorithm) on the host cores.
+N > 1 runs independent replicas (the solve does not shard; one GPU each).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Stokes solve time & operator GDoF/s: FP32-MG vs FP64-MG at 1e-8 FP64 residual"
+WORKLOAD = "sinkers_32^3_Q2Q1_eta1e6_q1proj_fgmres_fp32mg_tol1e-8"
+TOL = 1e-8
+N_CELLS_1D = 32
+CPU_SAMPLE_ITERATIONS = 12
+
+
+def log(*a):
+    print(f"[bench {time.strftime('%H:%M:%S')}]", *a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if "Active" in s[3 + i]
+                          and "Not" not in s[3 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def build_problem():
+    from aspect_gb300 import problems
+    return problems.sinkers_3d(N_CELLS_1D)
+
+
+def algorithmic_bytes(P, op: str, word: int) -> int:
+    """Compulsory bytes of one operator application (src + dst vectors + viscosity
+    table); DoF indices and constraints are not counted."""
+    f = P.fine
+    eta_words = f.n_cells * (27 if P.projection == 1 else 1)
+    if op == "stokes":
+        n = f.n_u + f.n_p
+    elif op == "A":
+        n = f.n_u
+    else:
+        n = f.n_p
+    return 2 * n * word + eta_words * word
+
+
+def cpu_baseline(P, n_threads: int, iterations_to_converge: int):
+    """FP64-MG oracle on the host cores: CPU_SAMPLE_ITERATIONS GMRES iterations of
+    the same solve, scaled to the converged iteration count."""
+    from oracle import Oracle
+    o = Oracle(P.levels, n_threads=n_threads)
+    o.set_viscosity(P.eta, P.projection, P.pressure_scaling)
+    o.build_preconditioner(False)
+    o.estimate_eigenvalues()
+    t = time.perf_counter()
+    _, info = o.solve(P.rhs, tol_rel=TOL, n_cheap=CPU_SAMPLE_ITERATIONS, n_expensive=0)
+    dt = time.perf_counter() - t
+    its = max(info["cheap_iterations"], 1)
+    est = dt / its * iterations_to_converge
+    return {"seconds_sample": dt, "iterations_sample": its, "seconds_per_solve_est": est,
+            "dofs_per_s": P.n_dofs / est}
+
+
+def run_reference(args):
+    world, rank, _ = dist_init()
+    if world > 1 and rank != 0:
+        return
+    P = build_problem()
+    threads = os.cpu_count() or 1
+    # the FP64-MG reference needs this many iterations on the workload (same
+    # algorithm as the GPU FP64-MG path; measured there and in the oracle)
+    its_full = int(os.environ.get("GB_FP64_ITERATIONS", "0")) or None
+    vals, times = [], []
+    from oracle import Oracle
+    o = Oracle(P.levels, n_threads=threads)
+    o.set_viscosity(P.eta, P.projection, P.pressure_scaling)
+    o.build_preconditioner(False)
+    o.estimate_eigenvalues()
+    for step in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        _, info = o.solve(P.rhs, tol_rel=TOL, n_cheap=CPU_SAMPLE_ITERATIONS, n_expensive=0)
+        dt = time.perf_counter() - t
+        if step >= args.warmup:
+            per_it = dt / max(info["cheap_iterations"], 1)
+            times.append(per_it)
+    per_it = statistics.median(times)
+    its = its_full or REFERENCE_FP64_ITERATIONS
+    sec = per_it * its
+    value = P.n_dofs / sec / 1e6
+    line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "MDoF/s", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD.replace("fp32mg", "fp64mg"), "n_dofs": P.n_dofs},
+            "cpu_baseline": {"value": value, "unit": "MDoF/s", "cores": threads, "kind": "port",
+                             "sample": f"{CPU_SAMPLE_ITERATIONS} GMRES iterations per step of the same 32^3 "
+                                       f"FP64-MG solve (CPU oracle, OpenMP over colour-ordered cells), "
+                                       f"seconds per iteration x {its} iterations to 1e-8"},
+            "e2e": {"value": value, "unit": "MDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# iterations of the FP64-MG solve of this workload to 1e-8 (measured on the GPU
+# path, which runs the same algorithm as the oracle; used to scale CPU samples)
+REFERENCE_FP64_ITERATIONS = 400
+
+
+def run_gpu(args):
+    import torch
+    from aspect_gb300 import gmg
+
+    world, rank, local = dist_init()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    P = build_problem()
+    f = P.fine
+    n = P.n_dofs
+    log("problem built", n)
+    t0 = time.perf_counter()
+    g = gmg.from_problem(P)
+    setup_s = time.perf_counter() - t0
+    log("setup done", setup_s)
+
+    rhs_d = torch.from_numpy(P.rhs).to(dev)
+    sol_d = torch.zeros(n, dtype=torch.float64, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > 129 MB L2
+    params = dict(linear_solver_tolerance=TOL, mg_precision=gmg.FP32, krylov=gmg.GMRES)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        sol_d.zero_()
+        o = g.solve_device(rhs_d.data_ptr(), sol_d.data_ptr(), **params)
+        log("warmup solve", o)
+    barrier()
+    launches0 = g.kernel_launches()
+    step_s, outs = [], []
+    torch.cuda.profiler.start()  # ncu --profile-from-start off captures the timed solves only
+    with ClockSampler(local) as clk:
+        barrier()
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            sol_d.zero_()
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            out = g.solve_device(rhs_d.data_ptr(), sol_d.data_ptr(), **params)
+            e1.record()
+            torch.cuda.synchronize()
+            step_s.append(e0.elapsed_time(e1) * 1e-3)
+            outs.append(out)
+        barrier()
+        wall = time.perf_counter() - wall0
+    torch.cuda.profiler.stop()
+    launches = g.kernel_launches() - launches0
+    t_sum = sum(step_s)
+    log("timed solves", step_s)
+    if world > 1:
+        tt = torch.tensor([t_sum], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_sum = float(tt.item())
+    value = world * args.steps * n / t_sum / 1e6
+    mixed = outs[-1]
+
+    # --- end to end through the host-array ABI (pinned host buffers)
+    rhs_h = torch.from_numpy(P.rhs.copy()).pin_memory()
+    sol_h = torch.zeros(n, dtype=torch.float64).pin_memory()
+    import ctypes
+    e2e_s = []
+    for _ in range(max(1, min(args.steps, 3))):
+        sol_h.zero_()
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        prm = gmg.default_solve_params(**params)
+        o = gmg.Outputs()
+        g._chk(g.L.gb_gmg_solve(g.h, ctypes.c_void_p(rhs_h.data_ptr()), ctypes.c_void_p(sol_h.data_ptr()),
+                                ctypes.byref(prm), ctypes.byref(o)))
+        torch.cuda.synchronize()
+        e2e_s.append(time.perf_counter() - t)
+    e2e_value = world * n / statistics.median(e2e_s) / 1e6
+
+    # --- FP64-MG comparison and the iterative-refinement variant (one timed solve each)
+    def timed_solve(**kw):
+        sol_d.zero_()
+        g.solve_device(rhs_d.data_ptr(), sol_d.data_ptr(), **kw)  # warm
+        sol_d.zero_()
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        o = g.solve_device(rhs_d.data_ptr(), sol_d.data_ptr(), **kw)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) * 1e-3, o, sol_d.clone()
+
+    t64, o64, x64 = timed_solve(linear_solver_tolerance=TOL, mg_precision=gmg.FP64)
+    log("fp64-mg solve", t64, o64)
+    tir, oir, xir = timed_solve(linear_solver_tolerance=TOL, mg_precision=gmg.FP32, krylov=gmg.GMRES_IR)
+    log("gmres-ir solve", tir, oir)
+    _, _, x32 = timed_solve(**params)
+    rel = lambda a, b: float(torch.linalg.norm(a[: f.n_u] - b[: f.n_u]) / torch.linalg.norm(b[: f.n_u]))
+
+    # --- operator timings (stokes_vmult etc.) and the roofline of the dominant kernel
+    ops = {}
+    for name, what, prec in [("stokes_vmult_fp64", gmg.TIME_STOKES_VMULT, gmg.FP64),
+                             ("stokes_vmult_fp32", gmg.TIME_STOKES_VMULT, gmg.FP32),
+                             ("A_vmult_fp32", gmg.TIME_A_VMULT, gmg.FP32),
+                             ("A_vmult_fp64", gmg.TIME_A_VMULT, gmg.FP64),
+                             ("mass_vmult_fp32", gmg.TIME_MASS_VMULT, gmg.FP32),
+                             ("stokes_preconditioner_fp32", gmg.TIME_STOKES_PRECONDITIONER, gmg.FP32),
+                             ("stokes_preconditioner_fp64", gmg.TIME_STOKES_PRECONDITIONER, gmg.FP64),
+                             ("A_preconditioner_fp32", gmg.TIME_A_PRECONDITIONER, gmg.FP32),
+                             ("S_preconditioner_fp32", gmg.TIME_S_PRECONDITIONER, gmg.FP32)]:
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        ops[name] = g.time_operation(what, prec, 20)
+    gdofs = {"stokes_vmult_fp64": n / ops["stokes_vmult_fp64"] / 1e9,
+             "stokes_vmult_fp32": n / ops["stokes_vmult_fp32"] / 1e9,
+             "A_vmult_fp32": f.n_u / ops["A_vmult_fp32"] / 1e9,
+             "A_vmult_fp64": f.n_u / ops["A_vmult_fp64"] / 1e9}
+    # share of the mixed solve: FP64 Stokes applications vs finest-level FP32 A-block
+    # applications (8 per A V-cycle on the finest level: 3 + 4 smoothing, 1 residual)
+    t_stokes64 = mixed["fp64_stokes_applications"] * ops["stokes_vmult_fp64"]
+    t_a32 = 8 * mixed["A_preconditioner_applications"] * ops["A_vmult_fp32"]
+    if t_stokes64 >= t_a32:
+        dom, t_dom, b_dom = "velocity_apply_kernel<double,3,STOKES>", ops["stokes_vmult_fp64"], \
+            algorithmic_bytes(P, "stokes", 8)
+    else:
+        dom, t_dom, b_dom = "velocity_apply_kernel<float,3,A>", ops["A_vmult_fp32"], algorithmic_bytes(P, "A", 4)
+    peak, peak_kind = peaks()
+    achieved = b_dom / t_dom / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as fh:
+            tr = json.load(fh).get(dom)
+            traffic = tr["bytes_per_application"] if tr else None
+    except Exception:
+        pass
+    clocks = clk.summary()
+
+    if rank != 0:
+        return
+    its_mixed = mixed["cheap_iterations"] + mixed["expensive_iterations"]
+    its64 = o64["cheap_iterations"] + o64["expensive_iterations"]
+    log("operators", ops)
+    cpu = cpu_baseline(P, os.cpu_count() or 1, its64)
+    log("cpu baseline", cpu)
+    line = {
+        "metric": METRIC, "value": value, "unit": "MDoF/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_sum / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (V-cycle) / f64 (Krylov, Stokes residual)",
+        "data": f"synthetic: 8 sinkers seeded SplitMix64({P.extra['seed']})",
+        "config": {"workload": WORKLOAD, "cells": f.n_cells, "n_u": f.n_u, "n_p": f.n_p, "levels": len(P.levels),
+                   "tolerance": TOL, "krylov": "FGMRES(100), FP64", "mg": "FP32 V-cycle, Chebyshev(4)",
+                   "l2": "flushed between timed solves (256 MiB write)", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "MDoF/s", "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": n * 8},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_application": b_dom, "seconds_per_application": t_dom},
+        "cpu_baseline": {"value": cpu["dofs_per_s"] / 1e6, "unit": "MDoF/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"{cpu['iterations_sample']} GMRES iterations of the same 32^3 solve, FP64-MG "
+                                   f"CPU oracle ({cpu['seconds_sample']:.1f} s), scaled to {its64} iterations"},
+        "clocks": clocks,
+        "detail": {
+            "setup_seconds": setup_s, "wall_seconds_timed": wall,
+            "mixed": {"solve_s": t_sum / args.steps, "iterations": its_mixed,
+                      "fp64_stokes_applications": mixed["fp64_stokes_applications"],
+                      "final_residual": mixed["final_linear_residual"], "tolerance": mixed["solver_tolerance"]},
+            "fp64_mg": {"solve_s": t64, "iterations": its64, "final_residual": o64["final_linear_residual"]},
+            "speedup_mixed_vs_fp64_mg": t64 / (t_sum / args.steps),
+            "gmres_ir": {"solve_s": tir, "iterations": oir["cheap_iterations"],
+                         "fp64_stokes_applications": oir["fp64_stokes_applications"],
+                         "speedup_vs_fp64_mg": t64 / tir},
+            "velocity_rel_l2_vs_fp64_mg": {"mixed": rel(x32, x64), "gmres_ir": rel(xir, x64)},
+            "operator_seconds": ops, "operator_gdofs": gdofs,
+            "solve_share_seconds": {"stokes_vmult_fp64": t_stokes64, "A_vmult_fp32_finest": t_a32},
+        },
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,227 @@
+/*
+ * gb_gmg.h -- C ABI of the GB300 matrix-free geometric-multigrid Stokes solver
+ * (Q2-Q1 Taylor-Hood, global-coarsening level hierarchy).
+ *
+ * This is the boundary an ASPECT-side StokesMatrixFreeHandler implementation
+ * binds to. It replaces, call for call, the work done behind
+ *   include/aspect/simulator/solver/stokes_matrix_free.h:47-98
+ *     (StokesMatrixFreeHandler: setup_dofs / assemble / build_preconditioner)
+ *   include/aspect/simulator/solver/interface.h:36-58,90-94
+ *     (StokesSolver::SolverOutputs, StokesSolver::Interface::solve)
+ * as implemented in source/simulator/solver/stokes_matrix_free_local_smoothing.cc
+ * and source/simulator/solver/stokes_matrix_free_global_coarsening.cc.
+ *
+ * Conventions
+ *  - Every function returns GB_GMG_OK (0) or an error code; nothing throws
+ *    across the ABI. gb_gmg_last_error() gives the message of the last error.
+ *  - The caller owns every host array; the library copies what it needs into
+ *    GB300 device memory (HBM). The handle owns all device memory. Set-up calls
+ *    allocate; apply/solve calls do not.
+ *  - One host thread per handle. Each handle drives one GPU (the current CUDA
+ *    device when gb_gmg_create is called).
+ *  - Levels are numbered 0 (coarsest) .. n_levels-1 (finest = active mesh).
+ *  - Cell-local DoF order: velocity FE_Q(2)^dim with components blocked and
+ *    nodes lexicographic (x fastest): local = c*3^dim + lex(i,j[,k]), nodes at
+ *    {0,1/2,1}; pressure FE_Q(1): local = lex(i,j[,k]), nodes at {0,1}.
+ *  - Pressure is the scaled unknown p/s on input and output, as in the
+ *    reference (stokes_matrix_free_local_smoothing.cc:975,1421). Constraint
+ *    distribution, p *= s, nullspace removal and pressure normalisation stay on
+ *    the caller's side, as in the reference (:1406-1443).
+ */
+#ifndef GB_GMG_H
+#define GB_GMG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gb_gmg gb_gmg;
+
+enum gb_gmg_status {
+  GB_GMG_OK = 0,
+  GB_GMG_INVALID_ARGUMENT = 1,
+  GB_GMG_NOT_READY = 2,          /* a set-up step is missing */
+  GB_GMG_CUDA_ERROR = 3,
+  GB_GMG_NO_CONVERGENCE = 4,     /* SolverControl::NoConvergence equivalent */
+  GB_GMG_BREAKDOWN = 5,
+  GB_GMG_NAN_DETECTED = 6,
+  GB_GMG_OUT_OF_MEMORY = 7
+};
+
+enum gb_gmg_geometry {
+  GB_GMG_GEOM_BOX = 0, /* per cell: lower corner x0[dim], edge lengths h[dim] */
+  GB_GMG_GEOM_Q2 = 1   /* per cell: 3^dim Q2 mapping support points [node][dim] */
+};
+
+enum gb_gmg_operator {
+  GB_GMG_OP_STOKES = 0, /* [A  B^T; B 0] on (u, p): src/dst = [u; p]       */
+  GB_GMG_OP_A = 1,      /* velocity block                                  */
+  GB_GMG_OP_BT = 2,     /* p -> u                                          */
+  GB_GMG_OP_MASS = 3    /* pressure mass matrix scaled by s^2/eta          */
+};
+
+enum gb_gmg_precision { GB_GMG_FP64 = 0, GB_GMG_FP32 = 1 };
+
+enum gb_gmg_krylov {
+  GB_GMG_GMRES = 0,       /* reference: cheap GMRES, FGMRES fallback          */
+  GB_GMG_GMRES_IR = 1     /* FP64 iterative refinement around FP32 GMRES       */
+};
+
+enum gb_gmg_projection {
+  GB_GMG_VISC_DGQ0 = 0, /* one (averaged) value per cell; levels: cell means     */
+  GB_GMG_VISC_DGQ1 = 1  /* values per quadrature point, projected to Q1 per cell
+                           (project_to_Q1 averaging); levels: Q1 interpolation,
+                           clamped to the active-level range                    */
+};
+
+/* Mirrors "Solver parameters/Stokes solver parameters" and "Matrix Free"
+ * (source/simulator/parameters.cc:436-600, stokes_matrix_free_local_smoothing.cc:52-85). */
+typedef struct gb_gmg_options {
+  int verbose;                  /* Output details                                   */
+  int smoother_degree;          /* Chebyshev degree on levels > 0 (4)                */
+  double smoothing_range;       /* Chebyshev smoothing range on levels > 0 (15)      */
+  int eig_cg_iterations;        /* eigenvalue-estimate CG steps on levels > 0 (10)   */
+  int coarse_degree;            /* Chebyshev degree on level 0 (8)                   */
+  double coarse_range;          /* level-0 range (1e-3: use the CG minimum estimate) */
+  int coarse_eig_cg_iterations; /* level-0 eigenvalue CG steps (100)                 */
+  int schur_smoothing_steps;    /* SmootherRelaxation steps for the Schur block (4)  */
+  int force_indexed_layout;     /* 1: never use the lattice fast path (testing)      */
+} gb_gmg_options;
+
+typedef struct gb_gmg_solve_params {
+  double linear_solver_tolerance;  /* relative (1e-7); tolerance rule of :977-1041   */
+  double absolute_tolerance;       /* > 0: use this absolute tolerance instead        */
+  int n_cheap_steps;               /* Number of cheap Stokes solver steps (1000)      */
+  int n_expensive_steps;           /* Maximum number of expensive ... steps (1000)    */
+  int restart;                     /* GMRES solver restart length (100)               */
+  double tol_A;                    /* Linear solver A block tolerance (1e-2)          */
+  double tol_S;                    /* Linear solver S block tolerance (1e-6)          */
+  int mg_precision;                /* gb_gmg_precision of the V-cycle                 */
+  int krylov;                      /* gb_gmg_krylov                                   */
+  double ir_inner_tolerance;       /* GMRES_IR: relative tolerance of each inner solve */
+} gb_gmg_solve_params;
+
+/* StokesSolver::SolverOutputs plus the counters the reference prints. */
+typedef struct gb_gmg_outputs {
+  double initial_nonlinear_residual;
+  double final_linear_residual;
+  double solver_tolerance;
+  int cheap_iterations;
+  int expensive_iterations;
+  int A_preconditioner_applications;
+  int S_preconditioner_applications;
+  int fp64_stokes_applications;     /* FP64 Stokes operator applications in the solve */
+  int status;                       /* gb_gmg_status of the solve                     */
+  double solve_seconds;             /* device time of the solve                       */
+} gb_gmg_outputs;
+
+/* Defaults identical to the reference's parameter defaults. */
+void gb_gmg_default_options(gb_gmg_options* opt);
+void gb_gmg_default_solve_params(gb_gmg_solve_params* prm);
+
+/* Replaces create_matrix_free_solver (source/simulator/solver/stokes_matrix_free.cc:30-62). */
+int gb_gmg_create(const gb_gmg_options* opt, int dim, int degree_v, int n_levels, gb_gmg** out);
+void gb_gmg_destroy(gb_gmg* h);
+const char* gb_gmg_last_error(const gb_gmg* h);
+
+/* setup_dofs (stokes_matrix_free_global_coarsening.cc:1456-1636): one level's
+ * cell-to-DoF maps (n_cells x dim*3^dim and n_cells x 2^dim, in the caller's
+ * numbering) and geometry (gb_gmg_geometry). */
+int gb_gmg_set_level_mesh(gb_gmg* h, int level, int64_t n_cells, const int32_t* cell_dofs_u,
+                          const int32_t* cell_dofs_p, int geometry_kind, const double* cell_geometry,
+                          int64_t n_u, int64_t n_p);
+
+/* Closed AffineConstraints of one block (0 velocity, 1 pressure) of one level,
+ * CSR: row rows[i] = sum_{k in [ptr[i],ptr[i+1])} weights[k] x[cols[k]] + inhom[i].
+ * Lines without entries are Dirichlet lines (hanging nodes, no-normal-flux,
+ * Dirichlet boundary values). inhomogeneities may be NULL. */
+int gb_gmg_set_level_constraints(gb_gmg* h, int level, int block, int64_t n_lines, const int32_t* rows,
+                                 const int32_t* ptr, const int32_t* cols, const double* weights,
+                                 const double* inhomogeneities);
+
+/* Parent cell (on level-1) and child index (bit d = upper half in direction d)
+ * of every cell of `level` >= 1 (MGTwoLevelTransfer, :1701-1731). */
+int gb_gmg_set_transfer(gb_gmg* h, int level, const int32_t* child_to_parent, const uint8_t* child_index);
+
+/* Ends setup_dofs: builds colourings, internal numbering, transfer operators. */
+int gb_gmg_finalize_setup(gb_gmg* h);
+
+/* assemble() -> evaluate_material_model (stokes_matrix_free_local_smoothing.cc:174-294):
+ * finest-level viscosity, n_per_cell = 1 (averaged) or 3^dim (per quadrature
+ * point, QGauss(3) lexicographic), in the caller's cell order; the level tables
+ * follow from `projection`. */
+int gb_gmg_set_viscosity(gb_gmg* h, const double* eta, int n_per_cell, int projection,
+                         double pressure_scaling, int compressible);
+
+/* build_preconditioner (:1856-1867): level diagonals for both blocks and both
+ * precisions, eigenvalue estimates (:834-849) and the captured V-cycles. */
+int gb_gmg_build_preconditioner(gb_gmg* h);
+
+/* One operator application on one level (host arrays, caller numbering).
+ * Constrained rows act as the identity (MatrixFreeOperators::Base::vmult). */
+int gb_gmg_vmult(gb_gmg* h, int op, int level, int precision, const double* src, double* dst);
+
+/* Same, on device arrays of the finest level in the caller's numbering. */
+int gb_gmg_vmult_device(gb_gmg* h, int op, int precision, const double* d_src, double* d_dst);
+
+/* Inverse diagonal of block 0 (A) or 1 (mass) on a level (caller numbering). */
+int gb_gmg_get_diagonal_inverse(gb_gmg* h, int level, int block, int precision, double* out);
+
+/* Eigenvalue estimates (min, max) of D^-1 A / D^-1 M on a level. */
+int gb_gmg_get_eigenvalues(gb_gmg* h, int level, int block, int precision, double* minmax);
+int gb_gmg_set_eigenvalues(gb_gmg* h, int level, int block, int precision, const double* minmax);
+
+/* Level transfer on host arrays: restrict (fine -> coarse, P^T) or prolongate. */
+int gb_gmg_transfer(gb_gmg* h, int fine_level, int block, int precision, int restrict_, const double* src,
+                    double* dst);
+
+/* One V-cycle (PreconditionMG::vmult) of block 0 (A) or 1 (Schur mass). */
+int gb_gmg_vcycle(gb_gmg* h, int block, int precision, const double* src, double* dst);
+
+/* BlockSchurPreconditioner::vmult (block_stokes_preconditioner.h:220-255), cheap variant. */
+int gb_gmg_block_preconditioner(gb_gmg* h, int precision, const double* src, double* dst);
+
+/* StokesMatrixFreeHandler::solve (:760-1446): rhs = [F_u; F_p] (condensed),
+ * sol = initial guess in / solution out, both [u; p/s] in caller numbering. */
+int gb_gmg_solve(gb_gmg* h, const double* rhs, double* sol, const gb_gmg_solve_params* prm,
+                 gb_gmg_outputs* out);
+
+/* Same, with rhs/sol already resident in device memory (caller numbering). */
+int gb_gmg_solve_device(gb_gmg* h, const double* d_rhs, double* d_sol, const gb_gmg_solve_params* prm,
+                        gb_gmg_outputs* out);
+
+/* Adjoint viscosity gradient (no reference counterpart): per finest cell c,
+ * g_c = -int_c 2 eta eps(u) : eps(lambda) dx, the derivative of
+ * lambda . (F - K u) with respect to ln(eta_c) for cellwise (DGQ0) viscosity,
+ * i.e. dJ/d ln(eta_c) when lambda solves K lambda = dJ/du. */
+int gb_gmg_adjoint_gradient(gb_gmg* h, const double* u, const double* lambda, double* grad_lneta);
+
+/* Operations timed by gb_gmg_time_operation; the names follow the
+ * "Execute solver timings" diagnostics of the reference
+ * (stokes_matrix_free_local_smoothing.cc:1116-1260). */
+enum gb_gmg_timed_operation {
+  GB_GMG_TIME_STOKES_VMULT = 0,          /* stokes_vmult (finest level)          */
+  GB_GMG_TIME_A_VMULT = 1,               /* A-block vmult (finest level)         */
+  GB_GMG_TIME_MASS_VMULT = 2,            /* pressure mass vmult (finest level)   */
+  GB_GMG_TIME_STOKES_PRECONDITIONER = 3, /* stokes_preconditioner (cheap)        */
+  GB_GMG_TIME_A_PRECONDITIONER = 4,      /* A_preconditioner (one V-cycle)       */
+  GB_GMG_TIME_S_PRECONDITIONER = 5       /* S_preconditioner (one V-cycle)       */
+};
+
+/* Mean device time of one call of `what` in `precision`, over `repeats` calls
+ * after one warm-up call, measured with CUDA events on the library's stream. */
+int gb_gmg_time_operation(gb_gmg* h, int what, int precision, int repeats, double* seconds_per_call);
+
+/* Device memory held by the handle (get_*_memory_consumption of stokes_matrix_free.h:80-97). */
+int gb_gmg_memory_consumption(const gb_gmg* h, size_t* bytes);
+
+/* Number of kernel launches issued by this handle since creation. */
+int64_t gb_gmg_kernel_launches(const gb_gmg* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GB_GMG_H */

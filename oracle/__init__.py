@@ -44,7 +44,7 @@ def lib():
                      "orc_finalize", "orc_set_viscosity", "orc_get_level_viscosity",
                      "orc_build_preconditioner", "orc_vmult", "orc_get_diagonal", "orc_transfer",
                      "orc_estimate_eigenvalues", "orc_get_eigenvalues", "orc_set_eigenvalues",
-                     "orc_vcycle", "orc_block_preconditioner", "orc_solve"]:
+                     "orc_vcycle", "orc_block_preconditioner", "orc_solve", "orc_adjoint_gradient"]:
             getattr(L, name).restype = ctypes.c_int
         _lib = L
     return _lib
@@ -162,6 +162,12 @@ class Oracle:
         src = _d(src)
         out = np.zeros_like(src)
         self._chk(self.L.orc_block_preconditioner(self.h, int(expensive), _ptr(src, _dp), _ptr(out, _dp)))
+        return out
+
+    def adjoint_gradient(self, u, lam) -> np.ndarray:
+        u, lam = _d(u), _d(lam)
+        out = np.zeros(self.fine.n_cells)
+        self._chk(self.L.orc_adjoint_gradient(self.h, _ptr(u, _dp), _ptr(lam, _dp), _ptr(out, _dp)))
         return out
 
     def solve(self, rhs, x0=None, tol_rel=1e-7, abs_tol=0.0, n_cheap=1000, n_expensive=1000,

@@ -651,15 +651,6 @@ struct Oracle {
   struct Cheb { int degree; double range; int eig_its; };
   Cheb cheb_params(int lev) const { return lev > 0 ? Cheb{4, 15.0, 10} : Cheb{8, 1e-3, 100}; }
 
-  // deterministic start vector for the eigenvalue estimate
-  static double start_entry(long i) {
-    uint64_t z = (uint64_t)i + 0x9E3779B97F4A7C15ull;
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    z ^= z >> 31;
-    return (double)(z >> 11) * (1.0 / 9007199254740992.0) - 0.5;
-  }
-
   template <class T>
   void level_op(int lev, int block, const T* x, T* y) {
     if (block == 0) apply<T>(lev, OP_A, x, nullptr, y, nullptr, eta_table<T>(lev));
@@ -712,12 +703,17 @@ struct Oracle {
     const Constraints& C = block == 0 ? L.cu : L.cp;
     Cheb cp = cheb_params(lev);
     std::vector<T> b(n), x(n, 0), r(n), z(n), p(n), Ap(n);
+    // PreconditionChebyshev's start vector: a period-11 mode (i mod 11) with its
+    // mean removed, over all entries (the smoother data carries no constraints).
+    // The pressure mass matrix has no null space and its largest eigenvector on
+    // small coarse levels is the constant mode, so there the mean is kept.
     double mean = 0;
-    int cnt = 0;
-    for (int i = 0; i < n; ++i)
-      if (!C.constrained(i)) { b[i] = (T)start_entry(i); mean += b[i]; ++cnt; } else b[i] = 0;
-    mean /= std::max(cnt, 1);
-    for (int i = 0; i < n; ++i) if (!C.constrained(i)) b[i] -= (T)mean;
+    if (block == 0) {
+      for (int i = 0; i < n; ++i) mean += (double)(i % 11);
+      mean /= std::max(n, 1);
+    }
+    for (int i = 0; i < n; ++i) b[i] = (T)((double)(i % 11) - mean);
+    (void)C;
     const T* dinv = dinv_table<T>(lev, block);
     r = b;
     for (int i = 0; i < n; ++i) z[i] = dinv[i] * r[i];
@@ -733,13 +729,16 @@ struct Oracle {
       double alpha = rz / pAp;
       alphas.push_back(alpha);
       for (int i = 0; i < n; ++i) { x[i] += (T)alpha * p[i]; r[i] -= (T)alpha * Ap[i]; }
+      // SolverControl(eig_cg_n_iterations, eig_cg_residual = 1e-2), absolute
+      double res = 0;
+      for (int i = 0; i < n; ++i) res += (double)r[i] * r[i];
+      if (std::sqrt(res) < 1e-2) break;
       for (int i = 0; i < n; ++i) z[i] = dinv[i] * r[i];
       double rz_new = 0;
       for (int i = 0; i < n; ++i) rz_new += (double)r[i] * z[i];
       double beta = rz_new / rz;
       betas.push_back(beta);
       rz = rz_new;
-      if (rz <= 0 || !(std::sqrt(rz) > 1e-30)) break;
       for (int i = 0; i < n; ++i) p[i] = z[i] + (T)beta * p[i];
     }
     // Lanczos tridiagonal from CG coefficients
@@ -759,8 +758,9 @@ struct Oracle {
     Level& L = levels[lev];
     double* eig = block == 0 ? L.eigA : L.eigM;
     Cheb cp = cheb_params(lev);
-    double lmax = 1.2 * eig[1];
-    double alpha = cp.range > 1.0 ? lmax / cp.range : std::min(0.9 * lmax, eig[0]);
+    const double emax = eig[1] > 0 ? eig[1] : 1.0, emin = eig[1] > 0 ? eig[0] : 1.0;
+    double lmax = 1.2 * emax;
+    double alpha = cp.range > 1.0 ? lmax / cp.range : std::min(0.9 * lmax, emin);
     theta = 0.5 * (lmax + alpha);
     delta = 0.5 * (lmax - alpha);
   }
@@ -1241,6 +1241,46 @@ int orc_block_preconditioner(void* p, int expensive, const double* src, double* 
   Oracle* h = (Oracle*)p;
   GUARD({ h->estimate_all(); orc::Params P; h->block_prec(src, dst, expensive != 0, P); })
 }
+// FP64 CPU adjoint gradient: g_c = -int_c 2 eta eps(u) : eps(lambda) (deviatoric
+// strain if compressible), the derivative of lambda . (F - K u) w.r.t. ln(eta_c).
+int orc_adjoint_gradient(void* p, const double* u, const double* lam, double* grad) {
+  Oracle* h = (Oracle*)p;
+  GUARD({
+    auto& L = h->fine();
+    const auto& fe = h->fe;
+    const int d = L.dim, nq = fe.nq, nv = fe.nv, nu = fe.nu;
+    for (int c = 0; c < L.n_cells; ++c) {
+      double xu[81], xl[81];
+      for (int i = 0; i < nu; ++i) {
+        orc::Expansion e = orc::expand(L.cu, L.cdu[(size_t)c * nu + i]);
+        double a = 0, b = 0;
+        for (int m = 0; m < e.n; ++m) { a += e.w[m] * u[e.g[m]]; b += e.w[m] * lam[e.g[m]]; }
+        xu[i] = a; xl[i] = b;
+      }
+      double acc = 0;
+      for (int q = 0; q < nq; ++q) {
+        const double* iJ = &L.invJ[((size_t)c * nq + q) * d * d];
+        double Gu[3][3] = {{0}}, Gl[3][3] = {{0}};
+        for (int n = 0; n < nv; ++n)
+          for (int e = 0; e < d; ++e) {
+            double gp = 0;
+            for (int a = 0; a < d; ++a) gp += fe.vgrad[(q * nv + n) * d + a] * iJ[a * d + e];
+            for (int cc = 0; cc < d; ++cc) { Gu[cc][e] += xu[cc * nv + n] * gp; Gl[cc][e] += xl[cc * nv + n] * gp; }
+          }
+        double eta = L.eta[(size_t)c * L.eta_n + (L.eta_n == 1 ? 0 : q)];
+        double t = 0, du = 0, dl = 0;
+        for (int a = 0; a < d; ++a) {
+          du += Gu[a][a]; dl += Gl[a][a];
+          for (int b = 0; b < d; ++b) t += 0.25 * (Gu[a][b] + Gu[b][a]) * (Gl[a][b] + Gl[b][a]);
+        }
+        if (h->compressible) t -= du * dl / 3.0;
+        acc += 2.0 * eta * L.JxW[(size_t)c * nq + q] * t;
+      }
+      grad[c] = -acc;
+    }
+  })
+}
+
 // params: [tol_rel, abs_tol, n_cheap, n_expensive, restart, tol_A, tol_S]
 // outputs: [initial_res, final_res, tolerance, cheap_its, expensive_its, nA, nS, status]
 int orc_solve(void* p, const double* params, const double* rhs, double* sol, double* outputs) {

@@ -1,0 +1,126 @@
+"""GPU path (libgb_gmg.so through the C ABI) against the CPU oracle on the same
+seeded inputs. Tolerances: FP64 operator results within 1e-12 relative (2-norm),
+FP32 level operators within 2e-6 relative, FP32 V-cycles within 1e-4."""
+import numpy as np
+import pytest
+
+from aspect_gb300 import gmg, mesh, problems
+from oracle import Oracle
+from tests.gpu_util import hierarchy, random_eta, rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 2e-6
+
+CASES = [
+    # dim, n, geometry, permute, per_q, compressible, force_indexed
+    (2, 8, "box", False, False, 0, 0),
+    (2, 8, "box", True, True, 1, 0),
+    (2, 8, "q2-distorted", False, True, 0, 0),
+    (3, 4, "box", False, False, 0, 0),
+    (3, 8, "box", False, True, 0, 0),
+    (3, 4, "box", True, True, 1, 0),
+    (3, 4, "box", False, True, 0, 1),
+    (3, 4, "q2-distorted", False, True, 0, 0),
+]
+
+
+def _pair(case):
+    dim, n, geom, perm, per_q, comp, force = case
+    levels = hierarchy(dim, n, geom, perm)
+    eta = random_eta(levels[-1], per_q)
+    s = 2.5
+    g = gmg.StokesMatrixFreeGPU(dim, len(levels), {"force_indexed_layout": force})
+    g.setup_dofs(levels)
+    g.assemble(eta, 0, s, comp)
+    o = Oracle(levels)
+    o.set_viscosity(eta, 0, s, comp)
+    return levels, g, o
+
+
+@pytest.fixture(scope="module", params=CASES, ids=lambda c: "-".join(map(str, c)))
+def pair(request):
+    return _pair(request.param)
+
+
+def test_vmult_all_operators_all_levels(pair):
+    levels, g, o = pair
+    rng = np.random.default_rng(7)
+    for lev, m in enumerate(levels):
+        for op in range(4):
+            n_in = m.n_u + m.n_p if op == 0 else (m.n_u if op == 1 else m.n_p)
+            x = rng.normal(size=n_in)
+            y_ref = o.vmult(op, lev, x)
+            y64 = g.vmult(op, lev, x, gmg.FP64)
+            assert rel_err(y64, y_ref) < TOL64, (lev, op, rel_err(y64, y_ref))
+            y32 = g.vmult(op, lev, x, gmg.FP32)
+            assert rel_err(y32, y_ref) < TOL32 * 10, (lev, op, rel_err(y32, y_ref))
+
+
+def test_diagonals_and_transfers(pair):
+    levels, g, o = pair
+    g.build_preconditioner()
+    o.build_preconditioner(False)
+    for lev, m in enumerate(levels):
+        for block in (0, 1):
+            d_ref = o.diagonal_inverse(lev, block)
+            assert rel_err(g.diagonal_inverse(lev, block, gmg.FP64), d_ref) < TOL64
+            assert rel_err(g.diagonal_inverse(lev, block, gmg.FP32), d_ref) < TOL32 * 10
+    rng = np.random.default_rng(3)
+    for lev in range(1, len(levels)):
+        for block in (0, 1):
+            c, f = levels[lev - 1], levels[lev]
+            xc = rng.normal(size=c.n_u if block == 0 else c.n_p)
+            xf = rng.normal(size=f.n_u if block == 0 else f.n_p)
+            assert rel_err(g.transfer(lev, block, False, xc), o.transfer(lev, block, False, xc)) < 1e-13
+            assert rel_err(g.transfer(lev, block, True, xf), o.transfer(lev, block, True, xf)) < 1e-13
+            assert rel_err(g.transfer(lev, block, True, xf, gmg.FP32), o.transfer(lev, block, True, xf)) < 1e-6
+
+
+def test_eigenvalues_and_vcycles(pair):
+    levels, g, o = pair
+    g.build_preconditioner()
+    o.build_preconditioner(False)
+    o.estimate_eigenvalues()
+    for lev in range(len(levels)):
+        for block in (0, 1):
+            e_ref = o.eigenvalues(lev, block)
+            e64 = g.eigenvalues(lev, block, gmg.FP64)
+            assert abs(e64[1] - e_ref[1]) < 1e-8 * abs(e_ref[1]), (lev, block, e64, e_ref)
+            e32 = g.eigenvalues(lev, block, gmg.FP32)
+            assert abs(e32[1] - e_ref[1]) < 1e-3 * abs(e_ref[1]), (lev, block, e32, e_ref)
+            # use the GPU's FP64 estimates in the oracle so the V-cycles are comparable
+            o.set_eigenvalues(lev, block, e64)
+    rng = np.random.default_rng(11)
+    f = levels[-1]
+    for block in (0, 1):
+        r = rng.normal(size=f.n_u if block == 0 else f.n_p)
+        v_ref = o.vcycle(block, r)
+        assert rel_err(g.vcycle(block, r, gmg.FP64), v_ref) < 1e-10
+    r = rng.normal(size=f.n_u + f.n_p)
+    b_ref = o.block_preconditioner(r)
+    assert rel_err(g.block_preconditioner(r, gmg.FP64), b_ref) < 1e-10
+    # FP32 V-cycle against the FP64 one with the same smoother intervals
+    for lev in range(len(levels)):
+        for block in (0, 1):
+            g.set_eigenvalues(lev, block, gmg.FP32, g.eigenvalues(lev, block, gmg.FP64))
+    for block in (0, 1):
+        r = rng.normal(size=f.n_u if block == 0 else f.n_p)
+        assert rel_err(g.vcycle(block, r, gmg.FP32), g.vcycle(block, r, gmg.FP64)) < 1e-5
+
+
+def test_adjoint_gradient_matches_cpu_adjoint(pair):
+    levels, g, o = pair
+    f = levels[-1]
+    rng = np.random.default_rng(5)
+    u, lam = rng.normal(size=f.n_u), rng.normal(size=f.n_u)
+    assert rel_err(g.adjoint_gradient(u, lam), o.adjoint_gradient(u, lam)) < TOL64
+
+
+def test_vmult_is_bit_reproducible():
+    levels, g, o = _pair((3, 8, "box", False, True, 0, 0))
+    x = np.random.default_rng(0).normal(size=levels[-1].n_u + levels[-1].n_p)
+    a = g.vmult(0, len(levels) - 1, x)
+    b = g.vmult(0, len(levels) - 1, x)
+    assert np.array_equal(a, b)
