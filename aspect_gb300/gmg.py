@@ -28,7 +28,7 @@ GMRES, GMRES_IR = 0, 1
 VISC_DGQ0, VISC_DGQ1 = 0, 1
 
 STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "NOT_READY", 3: "CUDA_ERROR", 4: "NO_CONVERGENCE",
-          5: "BREAKDOWN", 6: "NAN_DETECTED", 7: "OUT_OF_MEMORY"}
+          5: "BREAKDOWN", 6: "NAN_DETECTED", 7: "OUT_OF_MEMORY", 8: "EXCEEDS_STATIC_SCRATCH"}
 
 
 class GmgError(RuntimeError):
@@ -74,7 +74,7 @@ EXPORTS = ["gb_gmg_default_options", "gb_gmg_default_solve_params", "gb_gmg_crea
            "gb_gmg_vmult_device", "gb_gmg_get_diagonal_inverse", "gb_gmg_get_eigenvalues",
            "gb_gmg_set_eigenvalues", "gb_gmg_transfer", "gb_gmg_vcycle", "gb_gmg_block_preconditioner",
            "gb_gmg_solve", "gb_gmg_solve_device", "gb_gmg_adjoint_gradient", "gb_gmg_memory_consumption",
-           "gb_gmg_kernel_launches", "gb_gmg_time_operation"]
+           "gb_gmg_kernel_launches", "gb_gmg_time_operation", "gb_gmg_ablock_apply_lattice_noalloc"]
 
 TIME_STOKES_VMULT, TIME_A_VMULT, TIME_MASS_VMULT = 0, 1, 2
 TIME_STOKES_PRECONDITIONER, TIME_A_PRECONDITIONER, TIME_S_PRECONDITIONER = 3, 4, 5
@@ -124,6 +124,8 @@ def load_library(path: str = LIB_PATH):
     L.gb_gmg_kernel_launches.restype = ctypes.c_int64
     L.gb_gmg_time_operation.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_double)]
+    L.gb_gmg_ablock_apply_lattice_noalloc.argtypes = [ctypes.c_int, vp, vp, ctypes.c_uint32, ctypes.c_int, vp, vp,
+                                                      vp, vp]
     _lib = L
     return L
 

@@ -48,7 +48,8 @@ enum gb_gmg_status {
   GB_GMG_NO_CONVERGENCE = 4,     /* SolverControl::NoConvergence equivalent */
   GB_GMG_BREAKDOWN = 5,
   GB_GMG_NAN_DETECTED = 6,
-  GB_GMG_OUT_OF_MEMORY = 7
+  GB_GMG_OUT_OF_MEMORY = 7,
+  GB_GMG_EXCEEDS_STATIC_SCRATCH = 8  /* level larger than GB_GMG_NOALLOC_MAX_CELLS */
 };
 
 enum gb_gmg_geometry {
@@ -220,6 +221,29 @@ int gb_gmg_memory_consumption(const gb_gmg* h, size_t* bytes);
 
 /* Number of kernel launches issued by this handle since creation. */
 int64_t gb_gmg_kernel_launches(const gb_gmg* h);
+
+/* Allocation-free FP32 A-block apply (no counterpart in the reference; ASPECT
+ * always owns its operator scratch). For callers that cannot call cudaMalloc
+ * when they need the operator: code recording its own CUDA graph, code under a
+ * device-memory budget owned by another allocator, or code that must not block
+ * on the driver's allocator. dst = A src on a uniform lattice box level in the
+ * lattice numbering (velocity components blocked, Q2 nodes lexicographic, x
+ * fastest; constrained rows act as the identity), with the per-cell scratch in
+ * a static device array of GB_GMG_NOALLOC_MAX_CELLS cells (1.33 MB, held by
+ * every GPU that loads the library until exit). n_cells_dir[dim]: cells per
+ * direction; cell_size[dim]: edge lengths; zero_faces: bit (2*d+side)*3+comp
+ * set when velocity component comp is Dirichlet-zero on that face; d_eta:
+ * n_cells x eta_per_cell (1 or 3^dim) viscosities in lexicographic cell order;
+ * d_eta, d_src and d_dst in device memory, n_cells_dir and cell_size on the
+ * host; stream (a cudaStream_t) may be NULL. Larger levels return
+ * GB_GMG_EXCEEDS_STATIC_SCRATCH. Calls share the one array: calls whose kernels
+ * overlap on the GPU race and must be serialised by the caller. The first call
+ * on a device looks up the array's address; make it before any stream capture.
+ * The result is written asynchronously on `stream`. */
+#define GB_GMG_NOALLOC_MAX_CELLS 4096
+int gb_gmg_ablock_apply_lattice_noalloc(int dim, const int32_t* n_cells_dir, const double* cell_size,
+                                        uint32_t zero_faces, int eta_per_cell, const float* d_eta,
+                                        const float* d_src, float* d_dst, void* stream);
 
 #ifdef __cplusplus
 }
