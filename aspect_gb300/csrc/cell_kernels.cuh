@@ -497,6 +497,115 @@ __device__ __forceinline__ void mass_cell_op(const LevelView<T>& L, int cell, co
   });
 }
 
+// FP32, 3D lattice levels: one thread per cell. All 81 nodal values stay in
+// registers with compile-time component indices, so no shuffles, selects or
+// runtime geometry branches are needed, and the viscosity is read once per
+// point. The per-cell contributions are written slot-major (E[slot][cell]), so
+// the stores of a warp are coalesced.
+template <int op, bool eta_per_q>
+__global__ void __launch_bounds__(128) lattice_cell_kernel_f32(LevelView<float> L, const float* __restrict__ src_u,
+                                                                const float* __restrict__ src_p,
+                                                                float* __restrict__ Eu, float* __restrict__ Ep) {
+  constexpr bool need_u = (op == OPK_STOKES || op == OPK_A);
+  constexpr bool need_p = (op == OPK_STOKES || op == OPK_BT);
+  using T = float;
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= L.n_cells) return;
+  StructuredCell<T, 3> sc;
+  structured_cell_lex<T, 3>(L, cell, sc);
+  T U[3][27], V[3][27], P[8], YP[8];
+  if constexpr (need_u) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int n = 0; n < 27; ++n)
+        U[c][n] = structured_zero<T, 3>(L, sc, c, n)
+                      ? T(0)
+                      : src_u[c * L.n_nodes + sc.node0 + structured_node_offset<3>(L.Nn, n)];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) interpolate<T, 3, false>(U[c]);
+  }
+  if constexpr (need_p) {
+#pragma unroll
+    for (int n = 0; n < 8; ++n) P[n] = src_p[sc.pnode0 + structured_pnode_offset<3>(L.Np, n)];
+#pragma unroll
+    for (int n = 0; n < 8; ++n) YP[n] = T(0);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int n = 0; n < 27; ++n) V[c][n] = T(0);
+  const T ih0 = L.inv_h[0], ih1 = L.inv_h[1], ih2 = L.inv_h[2];
+  const T s = L.s;
+  const T eta_cell = eta_per_q ? T(0) : L.eta[cell];
+  const T* __restrict__ eq = L.eta + (size_t)cell * 27;
+  static_for<27>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    const T jxw = L.det * T(qweight<3, q>());
+    const T eta = eta_per_q ? eq[q] : eta_cell;
+    T G[3][3] = {{T(0)}};
+    if constexpr (need_u) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        G[c][0] = colloc_d<T, 3, q, 0>(U[c]) * ih0;
+        G[c][1] = colloc_d<T, 3, q, 1>(U[c]) * ih1;
+        G[c][2] = colloc_d<T, 3, q, 2>(U[c]) * ih2;
+      }
+    }
+    T pq = T(0);
+    if constexpr (need_p) {
+      static_for<8>([&](auto nc) {
+        constexpr int n = decltype(nc)::value;
+        pq += T(psi_at<3, q, n>()) * P[n];
+      });
+    }
+    T F[3][3];
+    const T div = G[0][0] + G[1][1] + G[2][2];
+    if constexpr (need_u) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) F[a][b] = eta * (G[a][b] + G[b][a]);
+      if (L.compressible) {
+        const T t = T(2) * eta / T(3) * div;
+        F[0][0] -= t; F[1][1] -= t; F[2][2] -= t;
+      }
+    } else {
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) F[a][b] = T(0);
+    }
+    if constexpr (need_p) {
+      F[0][0] -= s * pq; F[1][1] -= s * pq; F[2][2] -= s * pq;
+    }
+    const T w0 = ih0 * jxw, w1 = ih1 * jxw, w2 = ih2 * jxw;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      colloc_dT<T, 3, q, 0>(V[c], F[c][0] * w0);
+      colloc_dT<T, 3, q, 1>(V[c], F[c][1] * w1);
+      colloc_dT<T, 3, q, 2>(V[c], F[c][2] * w2);
+    }
+    if constexpr (op == OPK_STOKES) {
+      const T f = -s * jxw * div;
+      static_for<8>([&](auto nc) {
+        constexpr int n = decltype(nc)::value;
+        YP[n] += T(psi_at<3, q, n>()) * f;
+      });
+    }
+  });
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    interpolate<T, 3, true>(V[c]);
+#pragma unroll
+    for (int n = 0; n < 27; ++n) Eu[(size_t)(c * 27 + n) * L.n_cells + cell] = V[c][n];
+  }
+  if constexpr (op == OPK_STOKES) {
+#pragma unroll
+    for (int n = 0; n < 8; ++n) Ep[(size_t)n * L.n_cells + cell] = YP[n];
+  }
+}
+
 template <typename T, int dim>
 __global__ void __launch_bounds__(128) mass_cell_kernel(LevelView<T> L, const T* __restrict__ src_p,
                                                          T* __restrict__ Ep) {
@@ -539,6 +648,9 @@ struct GatherArgs {
   const T* dinv;   // inverse diagonal (EPI_CHEB)
   T* d;            // Chebyshev update vector (EPI_CHEB)
   T f1, f2;
+  // layout of E on lattice levels: entry (cell, slot) at cell * cs + slot * ss;
+  // cell-major (cs = slots per cell, ss = 1) or slot-major (cs = 1, ss = n_cells)
+  long cs, ss;
 };
 
 // General levels: CSR of (cell-local slot, weight) per DoF, built at set-up
@@ -600,7 +712,7 @@ __global__ void __launch_bounds__(256) velocity_gather_structured(LevelView<T> L
         for (int kx = 0; kx < cnt[0]; ++kx) {
           const int cell = (cidx[2][kz] * L.nc[1] + cidx[1][ky]) * L.nc[0] + cidx[0][kx];
           const int l = loc[0][kx] + 3 * loc[1][ky] + 9 * loc[2][kz];
-          sum += a.E[((size_t)cell * dim + comp) * nv + l];
+          sum += a.E[(size_t)cell * a.cs + (size_t)(comp * nv + l) * a.ss];
         }
   }
   gather_epilogue<T, epi>(a, g, sum, constrained);
@@ -629,7 +741,7 @@ __global__ void __launch_bounds__(256) pressure_gather_structured(LevelView<T> L
       for (int kx = 0; kx < cnt[0]; ++kx) {
         const int cell = (cidx[2][kz] * L.nc[1] + cidx[1][ky]) * L.nc[0] + cidx[0][kx];
         const int l = loc[0][kx] + 2 * loc[1][ky] + 4 * loc[2][kz];
-        sum += a.E[(size_t)cell * np + l];
+        sum += a.E[(size_t)cell * a.cs + (size_t)l * a.ss];
       }
   gather_epilogue<T, epi>(a, g, sum, false);
 }

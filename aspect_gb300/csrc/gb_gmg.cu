@@ -119,7 +119,15 @@ double dot_host_T(Handle& H, long n, const T* a, const T* b) {
 
 // ---------------------------------------------------------------- operators
 template <typename T>
-void gather(Handle& H, Level& L, const LevelView<T>& v, int block, int epi, const GatherArgs<T>& a) {
+void gather(Handle& H, Level& L, const LevelView<T>& v, int block, int epi, GatherArgs<T> a, int op) {
+  const int nl = block == 0 ? L.dim * (L.dim == 3 ? 27 : 9) : (L.dim == 3 ? 8 : 4);
+  if (cell_pass_slot_major<T>(v, op)) {
+    a.cs = 1;
+    a.ss = L.n_cells;
+  } else {
+    a.cs = nl;
+    a.ss = 1;
+  }
   GatherCsr<T> csr;
   const GatherCsr<T>* pc = nullptr;
   if (!L.structured) {
@@ -143,14 +151,14 @@ void apply_op(Handle& H, int lev, int op, const T* su, const T* sp, T* du, T* dp
     a.E = D.Eu.p;
     a.x = const_cast<T*>(su);
     a.y = du;
-    gather<T>(H, L, v, 0, op == OPK_BT ? EPI_BT : EPI_STORE, a);
+    gather<T>(H, L, v, 0, op == OPK_BT ? EPI_BT : EPI_STORE, a, op);
   }
   if (op == OPK_STOKES || op == OPK_MASS) {
     GatherArgs<T> a{};
     a.E = D.Ep.p;
     a.x = const_cast<T*>(sp);
     a.y = dp;
-    gather<T>(H, L, v, 1, EPI_STORE, a);
+    gather<T>(H, L, v, 1, EPI_STORE, a, op);
   }
 }
 
@@ -176,7 +184,7 @@ void level_op_cheb(Handle& H, int lev, int block, T* x, const T* b, const T* din
   a.d = d;
   a.f1 = (T)f1;
   a.f2 = (T)f2;
-  gather<T>(H, L, v, block, EPI_CHEB, a);
+  gather<T>(H, L, v, block, EPI_CHEB, a, block == 0 ? OPK_A : OPK_MASS);
 }
 
 // residual fused into the gather: y = b - K x
@@ -192,7 +200,7 @@ void level_op_resid(Handle& H, int lev, int block, const T* x, const T* b, T* y)
   a.x = const_cast<T*>(x);
   a.y = y;
   a.b = b;
-  gather<T>(H, L, v, block, EPI_RESID, a);
+  gather<T>(H, L, v, block, EPI_RESID, a, block == 0 ? OPK_A : OPK_MASS);
 }
 
 // ---------------------------------------------------------------- diagonals

@@ -49,9 +49,30 @@ void gather_dim(const LevelView<GB_T>& L, int block, int epi, const GatherCsr<GB
 }  // namespace
 
 template <>
+bool cell_pass_slot_major<GB_T>(const LevelView<GB_T>& L, int op) {
+  return std::is_same<GB_T, float>::value && L.dim == 3 && L.structured && (op == OPK_A || op == OPK_STOKES);
+}
+
+template <>
 void launch_cell_pass<GB_T>(const LevelView<GB_T>& L, int op, const GB_T* su, const GB_T* sp, GB_T* Eu, GB_T* Ep,
                             cudaStream_t s) {
   if (L.n_cells <= 0) return;
+#if defined(GB_T_IS_FLOAT)
+  {
+    if (cell_pass_slot_major<GB_T>(L, op)) {
+      const int g = ceil_div(L.n_cells, kCellThreads);
+      const bool pq = L.eta_n != 1;
+      if (op == OPK_A) {
+        if (pq) lattice_cell_kernel_f32<OPK_A, true><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
+        else lattice_cell_kernel_f32<OPK_A, false><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
+      } else {
+        if (pq) lattice_cell_kernel_f32<OPK_STOKES, true><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
+        else lattice_cell_kernel_f32<OPK_STOKES, false><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
+      }
+      return;
+    }
+  }
+#endif
   if (L.dim == 3) cell_pass_dim<3>(L, op, su, sp, Eu, Ep, s);
   else cell_pass_dim<2>(L, op, su, sp, Eu, Ep, s);
 }

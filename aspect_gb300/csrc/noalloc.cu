@@ -51,6 +51,9 @@ cudaError_t run(const LevelView<float>& L, float* scratch, const float* src, flo
   a.E = scratch;
   a.x = const_cast<float*>(src);
   a.y = dst;
+  a.cs = 3 * 27;  // the shared-thread kernel writes cell-major
+  a.ss = 1;
+  if (dim == 2) a.cs = 2 * 9;
   velocity_gather_structured<float, dim, EPI_STORE><<<ceil_div(L.n_u, 256), 256, 0, s>>>(L, a);
   return cudaGetLastError();
 }

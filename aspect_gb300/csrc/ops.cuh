@@ -14,6 +14,10 @@ struct ProbesView {
   const T* w = nullptr;       // [n_entries]
 };
 
+// true when pass 1 of `op` writes its per-cell contributions slot-major
+// (E[slot][cell]) instead of cell-major (E[cell][slot])
+template <typename T>
+bool cell_pass_slot_major(const LevelView<T>& L, int op);
 // pass 1 of an operator (op: OPK_*), all cells of the level
 template <typename T>
 void launch_cell_pass(const LevelView<T>& L, int op, const T* src_u, const T* src_p, T* Eu, T* Ep, cudaStream_t s);
