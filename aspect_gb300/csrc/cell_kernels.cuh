@@ -633,10 +633,11 @@ __global__ void __launch_bounds__(128) mass_cell_kernel(LevelView<T> L, const T*
 // ---------------------------------------------------------------------------
 // Pass 2: per-DoF gather with a fused epilogue.
 enum Epilogue {
-  EPI_STORE = 0,  // y = K x; constrained rows y = x
-  EPI_BT = 1,     // y = B^T p; constrained velocity rows y = 0
-  EPI_RESID = 2,  // y = b - K x; constrained rows y = b - x
-  EPI_CHEB = 3    // t = K x; d = f1 d + f2 dinv (b - t); x += d (x updated in place)
+  EPI_STORE = 0,    // y = K x; constrained rows y = x
+  EPI_BT = 1,       // y = B^T p; constrained velocity rows y = 0
+  EPI_RESID = 2,    // y = b - K x; constrained rows y = b - x
+  EPI_CHEB = 3,     // t = K x; d = f1 d + f2 dinv (b - t); x += d (x updated in place)
+  EPI_CHEB_OUT = 4  // as EPI_CHEB, but the new iterate goes to y (x is only read)
 };
 
 template <typename T>
@@ -676,7 +677,8 @@ __device__ __forceinline__ void gather_epilogue(const GatherArgs<T>& a, long g, 
     const T t = constrained ? xg : sum;
     const T dn = a.f1 * a.d[g] + a.f2 * a.dinv[g] * (a.b[g] - t);
     a.d[g] = dn;
-    a.x[g] = xg + dn;
+    if (epi == EPI_CHEB) a.x[g] = xg + dn;
+    else a.y[g] = xg + dn;
   }
 }
 
@@ -742,6 +744,44 @@ __global__ void __launch_bounds__(256) pressure_gather_structured(LevelView<T> L
         const int cell = (cidx[2][kz] * L.nc[1] + cidx[1][ky]) * L.nc[0] + cidx[0][kx];
         const int l = loc[0][kx] + 2 * loc[1][ky] + 4 * loc[2][kz];
         sum += a.E[(size_t)cell * a.cs + (size_t)l * a.ss];
+      }
+  gather_epilogue<T, epi>(a, g, sum, false);
+}
+
+// Pressure mass operator of a lattice level in one pass: one thread per
+// pressure node multiplies the rows of its (at most 2^dim) cells' precomputed
+// local mass matrices (Mc[cell][i][j] = sum_q s^2/eta_q JxW_q psi_i psi_j)
+// with the cells' pressure values. It reads x at neighbouring nodes, so a
+// Chebyshev step writes its new iterate to a separate vector (EPI_CHEB_OUT).
+template <typename T, int dim, int epi>
+__global__ void __launch_bounds__(256) mass_apply_lattice(LevelView<T> L, const T* __restrict__ Mc,
+                                                           GatherArgs<T> a) {
+  constexpr int np = Shape<dim>::np;
+  const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (g >= L.n_p) return;
+  const int node = (int)g;
+  const int gc[3] = {node % L.Np[0], (node / L.Np[0]) % L.Np[1], dim == 3 ? node / (L.Np[0] * L.Np[1]) : 0};
+  int cidx[3][2], loc[3][2], cnt[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    cnt[d] = 0;
+    if (d >= dim) { cnt[d] = 1; cidx[d][0] = 0; loc[d][0] = 0; continue; }
+    const int x = gc[d];
+    if (x > 0) { cidx[d][cnt[d]] = x - 1; loc[d][cnt[d]] = 1; ++cnt[d]; }
+    if (x < L.Np[d] - 1) { cidx[d][cnt[d]] = x; loc[d][cnt[d]] = 0; ++cnt[d]; }
+  }
+  const T* __restrict__ xin = a.x;
+  T sum = T(0);
+  for (int kz = 0; kz < cnt[2]; ++kz)
+    for (int ky = 0; ky < cnt[1]; ++ky)
+      for (int kx = 0; kx < cnt[0]; ++kx) {
+        const int cz = cidx[2][kz], cy = cidx[1][ky], cx = cidx[0][kx];
+        const int cell = (cz * L.nc[1] + cy) * L.nc[0] + cx;
+        const int l = loc[0][kx] + 2 * loc[1][ky] + 4 * loc[2][kz];
+        const T* __restrict__ row = Mc + ((size_t)cell * np + l) * np;
+        const int p0 = (cz * L.Np[1] + cy) * L.Np[0] + cx;
+#pragma unroll
+        for (int j = 0; j < np; ++j) sum += row[j] * xin[p0 + structured_pnode_offset<dim>(L.Np, j)];
       }
   gather_epilogue<T, epi>(a, g, sum, false);
 }

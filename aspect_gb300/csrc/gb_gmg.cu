@@ -140,10 +140,23 @@ void gather(Handle& H, Level& L, const LevelView<T>& v, int block, int epi, Gath
 
 // y = op(x) on a level; constrained rows act as the identity (zero for B^T)
 template <typename T>
+void mass_lattice(Handle& H, Level& L, const LevelView<T>& v, int epi, GatherArgs<T> a) {
+  launch_mass_lattice<T>(v, L.dev<T>().Mp.p, epi, a, H.st);
+  ++H.cell_launches;
+}
+
+template <typename T>
 void apply_op(Handle& H, int lev, int op, const T* su, const T* sp, T* du, T* dp) {
   Level& L = H.levels[lev];
   LevelDev<T>& D = L.dev<T>();
   const LevelView<T> v = L.view<T>(H.s, H.compressible);
+  if (op == OPK_MASS && L.structured) {
+    GatherArgs<T> a{};
+    a.x = const_cast<T*>(sp);
+    a.y = dp;
+    mass_lattice<T>(H, L, v, EPI_STORE, a);
+    return;
+  }
   launch_cell_pass<T>(v, op, su, sp, D.Eu.p, D.Ep.p, H.st);
   ++H.cell_launches;
   if (op == OPK_STOKES || op == OPK_A || op == OPK_BT) {
@@ -193,6 +206,14 @@ void level_op_resid(Handle& H, int lev, int block, const T* x, const T* b, T* y)
   Level& L = H.levels[lev];
   LevelDev<T>& D = L.dev<T>();
   const LevelView<T> v = L.view<T>(H.s, H.compressible);
+  if (block == 1 && L.structured) {
+    GatherArgs<T> a{};
+    a.x = const_cast<T*>(x);
+    a.y = y;
+    a.b = b;
+    mass_lattice<T>(H, L, v, EPI_RESID, a);
+    return;
+  }
   launch_cell_pass<T>(v, block == 0 ? OPK_A : OPK_MASS, x, x, D.Eu.p, D.Ep.p, H.st);
   ++H.cell_launches;
   GatherArgs<T> a{};
@@ -336,20 +357,38 @@ void chebyshev(Handle& H, int lev, int block, T* x, const T* b, bool zero_start)
   const T* dinv = block == 0 ? D.dinvA.p : D.dinvM.p;
   T* d = block == 0 ? D.dA.p : D.dM.p;
   T* t = block == 0 ? D.tA.p : D.tM.p;
-  if (zero_start) {
-    v_cheb_first<T>(n, b, dinv, (T)(1.0 / theta), d, x, H.st);
-  } else {
-    level_op_cheb<T>(H, lev, block, x, b, dinv, d, 0.0, 1.0 / theta);
-  }
+  // the one-pass mass operator of lattice levels reads neighbouring entries of
+  // the iterate, so its Chebyshev steps alternate between x and t
+  const bool ping_pong = block == 1 && L.structured;
+  T* cur = x;
+  auto step = [&](double f1, double f2) {
+    if (!ping_pong) {
+      level_op_cheb<T>(H, lev, block, x, b, dinv, d, f1, f2);
+      return;
+    }
+    T* nxt = cur == x ? t : x;
+    GatherArgs<T> a{};
+    a.x = cur;
+    a.y = nxt;
+    a.b = b;
+    a.dinv = dinv;
+    a.d = d;
+    a.f1 = (T)f1;
+    a.f2 = (T)f2;
+    mass_lattice<T>(H, L, L.view<T>(H.s, H.compressible), EPI_CHEB_OUT, a);
+    cur = nxt;
+  };
+  if (zero_start) v_cheb_first<T>(n, b, dinv, (T)(1.0 / theta), d, x, H.st);
+  else step(0.0, 1.0 / theta);
   double rhok = delta / theta;
   const double sigma = theta / delta;
   for (int k = 1; k < cp.degree; ++k) {
     const double rhokp = 1.0 / (2.0 * sigma - rhok);
     const double f1 = rhokp * rhok, f2 = 2.0 * rhokp / delta;
     rhok = rhokp;
-    level_op_cheb<T>(H, lev, block, x, b, dinv, d, f1, f2);
+    step(f1, f2);
   }
-  (void)t;
+  if (cur != x) v_copy<T>(n, cur, x, H.st);
 }
 
 int smoothing_steps(const Handle& H, int block) { return block == 0 ? 1 : H.opt.schur_smoothing_steps; }
@@ -936,7 +975,7 @@ int gb_gmg_set_transfer(gb_gmg* g, int level, const int32_t* parent, const uint8
     GB_CHECK(L.n_cells > 0, 2, "set the level mesh before its transfer");
     L.parent.assign(parent, parent + L.n_cells);
     L.child.assign(child, child + L.n_cells);
-    for (unsigned char c : L.child) GB_CHECK(c < (1u << H.dim), 1, "child index out of range");
+    for (unsigned char c : L.child) GB_CHECK(c < (1u << H.dim) || c == gb::kSameCell, 1, "child index out of range");
     L.has_transfer = true;
     H.setup_done = false;
   })
@@ -970,10 +1009,28 @@ int gb_gmg_set_viscosity(gb_gmg* g, const double* eta, int n_per_cell, int proje
     H.compressible = compressible;
     H.projection = projection;
     gb::compute_level_viscosity(H.levels, eta, n_per_cell, projection, H.eta_min, H.eta_max);
-    for (auto& L : H.levels) gb::upload_viscosity(L);
+    for (auto& L : H.levels) gb::upload_viscosity(L, s);
     H.reset_graphs();
     H.visc_done = true;
     H.prec_done[0] = H.prec_done[1] = false;
+  })
+}
+
+int gb_gmg_update_viscosity(gb_gmg* g, const double* eta, int n_per_cell) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
+    const int nq = H.dim == 3 ? 27 : 9;
+    GB_CHECK(n_per_cell == 1 || n_per_cell == nq, 1, "n_per_cell must be 1 or 3^dim");
+    double mn, mx;
+    gb::compute_level_viscosity(H.levels, eta, n_per_cell, H.projection, mn, mx);
+    for (auto& L : H.levels) {
+      GB_CHECK(L.eta.size() == L.f64.eta.n, 1, "viscosity layout differs from the last set_viscosity");
+      gb::upload_viscosity(L, H.s);  // same sizes: device addresses (and captured graphs) stay valid
+    }
+    H.eta_min = mn;
+    H.eta_max = mx;
   })
 }
 

@@ -43,6 +43,7 @@ void gather_dim(const LevelView<GB_T>& L, int block, int epi, const GatherCsr<GB
     case EPI_STORE: gather_dim_epi<dim, EPI_STORE>(L, block, csr, a, s); break;
     case EPI_BT: gather_dim_epi<dim, EPI_BT>(L, block, csr, a, s); break;
     case EPI_RESID: gather_dim_epi<dim, EPI_RESID>(L, block, csr, a, s); break;
+    case EPI_CHEB_OUT: gather_dim_epi<dim, EPI_CHEB_OUT>(L, block, csr, a, s); break;
     default: gather_dim_epi<dim, EPI_CHEB>(L, block, csr, a, s); break;
   }
 }
@@ -82,6 +83,20 @@ void launch_gather<GB_T>(const LevelView<GB_T>& L, int block, int epi, const Gat
                          const GatherArgs<GB_T>& a, cudaStream_t s) {
   if (L.dim == 3) gather_dim<3>(L, block, epi, csr, a, s);
   else gather_dim<2>(L, block, epi, csr, a, s);
+}
+
+template <>
+void launch_mass_lattice<GB_T>(const LevelView<GB_T>& L, const GB_T* Mc, int epi, const GatherArgs<GB_T>& a,
+                               cudaStream_t s) {
+  const int g = ceil_div(L.n_p, kGatherThreads);
+#define GB_MASS_LATTICE(DIM)                                                                                \
+  switch (epi) {                                                                                            \
+    case EPI_STORE: mass_apply_lattice<GB_T, DIM, EPI_STORE><<<g, kGatherThreads, 0, s>>>(L, Mc, a); break;  \
+    case EPI_RESID: mass_apply_lattice<GB_T, DIM, EPI_RESID><<<g, kGatherThreads, 0, s>>>(L, Mc, a); break;  \
+    default: mass_apply_lattice<GB_T, DIM, EPI_CHEB_OUT><<<g, kGatherThreads, 0, s>>>(L, Mc, a); break;      \
+  }
+  if (L.dim == 3) { GB_MASS_LATTICE(3) } else { GB_MASS_LATTICE(2) }
+#undef GB_MASS_LATTICE
 }
 
 template <>

@@ -10,6 +10,9 @@
 
 namespace gb {
 
+// child index of a cell that is the same cell on the next coarser level
+constexpr int kSameCell = 255;
+
 // Closed constraints of one block, caller numbering.
 struct HostCons {
   std::vector<int> line_of;  // per DoF: -1 or line index
@@ -52,6 +55,7 @@ struct LevelDev {
   DevBuf<T> dinvA, dinvM;
   DevBuf<T> gu_w, gp_w;  // gather weights (general levels)
   DevBuf<T> Eu, Ep;      // per-cell contributions of pass 1
+  DevBuf<T> Mp;          // lattice levels: per-cell pressure mass matrices [cell][np][np]
   // V-cycle work vectors (A block: n_u, Schur block: n_p)
   DevBuf<T> solA, defA, tA, dA, solM, defM, tM, dM;
   double eigA[2] = {0, 0}, eigM[2] = {0, 0};
@@ -119,6 +123,6 @@ void setup_level(Level& L, bool force_indexed);
 void setup_transfer(Level& fine, const Level& coarse);
 void compute_level_viscosity(std::vector<Level>& levels, const double* eta_in, int n_per_cell, int projection,
                              double& eta_min, double& eta_max);
-void upload_viscosity(Level& L);
+void upload_viscosity(Level& L, double pressure_scaling);
 
 }  // namespace gb

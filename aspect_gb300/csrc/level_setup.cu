@@ -485,7 +485,7 @@ void setup_transfer(Level& F, const Level& C) {
           const int idx = block == 0 ? (e == 0 ? n % 3 : e == 1 ? (n / 3) % 3 : n / 9)
                                      : (e == 0 ? n % 2 : e == 1 ? (n / 2) % 2 : n / 4);
           const double loc = block == 0 ? 0.5 * idx : (double)idx;
-          xi[e] = 0.5 * (((ch >> e) & 1) + loc);
+          xi[e] = ch == kSameCell ? loc : 0.5 * (((ch >> e) & 1) + loc);
         }
         double phi[27];
         double vv[3][3], dd[3][3];
@@ -666,7 +666,11 @@ void compute_level_viscosity(std::vector<Level>& levels, const double* eta_in, i
       dg[l - 1].assign((size_t)levels[l - 1].n_cells * ncv, 0.0);
       for (long c = 0; c < F.n_cells; ++c) {
         const int ch = F.child[c], p = F.parent[c];
-        dg[l - 1][(size_t)p * ncv + ch] = dg[l][c * ncv + ch];
+        if (ch == kSameCell) {
+          for (int i = 0; i < ncv; ++i) dg[l - 1][(size_t)p * ncv + i] = dg[l][c * ncv + i];
+        } else {
+          dg[l - 1][(size_t)p * ncv + ch] = dg[l][c * ncv + ch];
+        }
       }
     }
     for (int l = 0; l < nlev; ++l) {
@@ -683,7 +687,7 @@ void compute_level_viscosity(std::vector<Level>& levels, const double* eta_in, i
   }
 }
 
-void upload_viscosity(Level& L) {
+void upload_viscosity(Level& L, double s) {
   std::vector<double> e((size_t)L.n_cells * L.eta_n);
   for (long c = 0; c < L.n_cells; ++c) {
     const long ic = L.internal_of_cell[c];
@@ -691,6 +695,37 @@ void upload_viscosity(Level& L) {
   }
   L.f64.eta.upload(e);
   L.f32.eta.upload(std::vector<float>(e.begin(), e.end()));
+  if (!L.structured) return;
+  // per-cell local pressure mass matrices of a lattice level:
+  // M[i][j] = sum_q s^2 / eta_q * |det J| w_q psi_i(q) psi_j(q)
+  const int d = L.dim, nq = nv_of(d), np = np_of(d);
+  const double g3[3] = {0.5 - std::sqrt(15.0) / 10, 0.5, 0.5 + std::sqrt(15.0) / 10};
+  const double w3[3] = {5.0 / 18, 8.0 / 18, 5.0 / 18};
+  double det = 1;
+  for (int k = 0; k < d; ++k) det *= L.h[k];
+  std::vector<double> psi(nq * np), wq(nq);
+  for (int q = 0; q < nq; ++q) {
+    const int qi[3] = {q % 3, (q / 3) % 3, q / 9};
+    wq[q] = 1;
+    for (int k = 0; k < d; ++k) wq[q] *= w3[qi[k]];
+    for (int n = 0; n < np; ++n) {
+      double t = 1;
+      for (int k = 0; k < d; ++k) t *= ((n >> k) & 1) ? g3[qi[k]] : 1 - g3[qi[k]];
+      psi[q * np + n] = t;
+    }
+  }
+  std::vector<double> M((size_t)L.n_cells * np * np, 0.0);
+  for (long ic = 0; ic < L.n_cells; ++ic) {
+    double* m = &M[(size_t)ic * np * np];
+    for (int q = 0; q < nq; ++q) {
+      const double eta = e[ic * L.eta_n + (L.eta_n == 1 ? 0 : q)];
+      const double f = s * s / eta * det * wq[q];
+      for (int i = 0; i < np; ++i)
+        for (int j = 0; j < np; ++j) m[i * np + j] += f * psi[q * np + i] * psi[q * np + j];
+    }
+  }
+  L.f64.Mp.upload(M);
+  L.f32.Mp.upload(std::vector<float>(M.begin(), M.end()));
 }
 
 template <typename T>
@@ -745,7 +780,7 @@ size_t Level::device_bytes() const {
          D.pprobe_w.bytes() + D.Pu_val.bytes() + D.PuT_val.bytes() + D.Pp_val.bytes() + D.PpT_val.bytes() +
          D.dinvA.bytes() + D.dinvM.bytes() + D.solA.bytes() + D.defA.bytes() + D.tA.bytes() + D.dA.bytes() +
          D.solM.bytes() + D.defM.bytes() + D.tM.bytes() + D.dM.bytes() + D.gu_w.bytes() + D.gp_w.bytes() +
-         D.Eu.bytes() + D.Ep.bytes();
+         D.Eu.bytes() + D.Ep.bytes() + D.Mp.bytes();
   };
   add(f32);
   add(f64);

@@ -25,6 +25,9 @@ void launch_cell_pass(const LevelView<T>& L, int op, const T* src_u, const T* sr
 template <typename T>
 void launch_gather(const LevelView<T>& L, int block, int epi, const GatherCsr<T>* csr, const GatherArgs<T>& a,
                    cudaStream_t s);
+// one-pass pressure mass operator of a lattice level (Mc: per-cell local matrices)
+template <typename T>
+void launch_mass_lattice(const LevelView<T>& L, const T* Mc, int epi, const GatherArgs<T>& a, cudaStream_t s);
 // diagonals, colour by colour (set-up only)
 template <typename T>
 void launch_velocity_diag(const LevelView<T>& L, int colour, int begin, int count, const ProbesView<T>& pr,

@@ -74,7 +74,8 @@ EXPORTS = ["gb_gmg_default_options", "gb_gmg_default_solve_params", "gb_gmg_crea
            "gb_gmg_vmult_device", "gb_gmg_get_diagonal_inverse", "gb_gmg_get_eigenvalues",
            "gb_gmg_set_eigenvalues", "gb_gmg_transfer", "gb_gmg_vcycle", "gb_gmg_block_preconditioner",
            "gb_gmg_solve", "gb_gmg_solve_device", "gb_gmg_adjoint_gradient", "gb_gmg_memory_consumption",
-           "gb_gmg_kernel_launches", "gb_gmg_time_operation", "gb_gmg_ablock_apply_lattice_noalloc"]
+           "gb_gmg_kernel_launches", "gb_gmg_time_operation", "gb_gmg_ablock_apply_lattice_noalloc",
+           "gb_gmg_update_viscosity"]
 
 TIME_STOKES_VMULT, TIME_A_VMULT, TIME_MASS_VMULT = 0, 1, 2
 TIME_STOKES_PRECONDITIONER, TIME_A_PRECONDITIONER, TIME_S_PRECONDITIONER = 3, 4, 5
@@ -108,6 +109,7 @@ def load_library(path: str = LIB_PATH):
     L.gb_gmg_finalize_setup.argtypes = [vp]
     L.gb_gmg_set_viscosity.argtypes = [vp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
     L.gb_gmg_build_preconditioner.argtypes = [vp]
+    L.gb_gmg_update_viscosity.argtypes = [vp, dp, ctypes.c_int]
     L.gb_gmg_vmult.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp]
     L.gb_gmg_vmult_device.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, dp]
     L.gb_gmg_get_diagonal_inverse.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
@@ -212,6 +214,11 @@ class StokesMatrixFreeGPU:
         n_per_cell = eta.size // self.levels[-1].n_cells
         self._chk(self.L.gb_gmg_set_viscosity(self.h, _p(eta), n_per_cell, projection,
                                               ctypes.c_double(pressure_scaling), compressible))
+
+    def update_viscosity(self, eta):
+        """New viscosity for the operators; keeps the last-built preconditioner."""
+        eta = _d(eta)
+        self._chk(self.L.gb_gmg_update_viscosity(self.h, _p(eta), eta.size // self.levels[-1].n_cells))
 
     def build_preconditioner(self):
         self._chk(self.L.gb_gmg_build_preconditioner(self.h))

@@ -235,3 +235,28 @@ def sinkers_3d(n: int = 32, seed: int = BASE_SEED + 2, projection: int = 1,
     s = pressure_scaling(fine, sinker_viscosity(mid, centres), 0.01)
     return StokesProblem(f"sinkers_{n}^3", levels, eta, projection, s, rhs, 2,
                          extra=dict(centres=centres, seed=seed))
+
+
+def adaptive_sphere(base_depth: int = 4, n_adaptive: int = 2, radius: float = 0.2,
+                    eta_in: float = 1e3, drho: float = 0.01) -> StokesProblem:
+    """3D unit cube, uniform depth base_depth (16^3 for 4) plus n_adaptive rounds
+    of refining the cells cut by the sphere |x - (1/2,1/2,1/2)| = radius, with 2:1
+    face/edge balance (hanging nodes). eta = eta_in and rho = 1 + drho inside the
+    sphere, eta = rho = 1 outside, evaluated per quadrature point with the Q1
+    projection; g = -z; free slip."""
+    from . import octree
+    leaves = octree.sphere_refined_leaves(3, base_depth, n_adaptive, (0.5, 0.5, 0.5), radius)
+    levels = octree.hierarchy(leaves, 3)
+    fine = levels[-1]
+    xq, jxw = q_points_real(fine)
+    inside = np.sum((xq - 0.5) ** 2, -1) < radius ** 2
+    eta = np.where(inside, eta_in, 1.0)
+    rho = np.where(inside, 1.0 + drho, 1.0)
+    force = np.zeros(xq.shape)
+    force[..., 2] = -rho
+    rhs = assemble_rhs(fine, force)
+    mid = fine.map_points(np.full((1, 3), 0.5))[:, 0, :]
+    s = pressure_scaling(fine, np.where(np.sum((mid - 0.5) ** 2, -1) < radius ** 2, eta_in, 1.0), 0.01)
+    return StokesProblem(f"adaptive_sphere_{2 ** base_depth}^3+{n_adaptive}", levels, eta, 1, s, rhs, 2,
+                         extra=dict(cells_per_depth={int(d): int(np.sum(fine.cell_level == d))
+                                                     for d in np.unique(fine.cell_level)}))

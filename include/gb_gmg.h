@@ -144,7 +144,10 @@ int gb_gmg_set_level_constraints(gb_gmg* h, int level, int block, int64_t n_line
                                  const double* inhomogeneities);
 
 /* Parent cell (on level-1) and child index (bit d = upper half in direction d)
- * of every cell of `level` >= 1 (MGTwoLevelTransfer, :1701-1731). */
+ * of every cell of `level` >= 1 (MGTwoLevelTransfer, :1701-1731). A cell that
+ * is itself a cell of level-1 (not coarsened) has child index GB_GMG_SAME_CELL
+ * and its own index on level-1 as parent. */
+#define GB_GMG_SAME_CELL 255
 int gb_gmg_set_transfer(gb_gmg* h, int level, const int32_t* child_to_parent, const uint8_t* child_index);
 
 /* Ends setup_dofs: builds colourings, internal numbering, transfer operators. */
@@ -156,6 +159,14 @@ int gb_gmg_finalize_setup(gb_gmg* h);
  * follow from `projection`. */
 int gb_gmg_set_viscosity(gb_gmg* h, const double* eta, int n_per_cell, int projection,
                          double pressure_scaling, int compressible);
+
+/* Same as gb_gmg_set_viscosity with the projection and pressure scaling of the
+ * last call, but keeps the preconditioner of the last gb_gmg_build_preconditioner
+ * (diagonals, Chebyshev intervals, captured V-cycles): the operators see the new
+ * viscosity, the smoothers keep the old diagonals. For nearby coefficient fields,
+ * e.g. finite-difference checks or nonlinear iterations that reuse a
+ * preconditioner; ASPECT itself rebuilds after every assemble(). */
+int gb_gmg_update_viscosity(gb_gmg* h, const double* eta, int n_per_cell);
 
 /* build_preconditioner (:1856-1867): level diagonals for both blocks and both
  * precisions, eigenvalue estimates (:834-849) and the captured V-cycles. */

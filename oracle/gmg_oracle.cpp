@@ -494,7 +494,7 @@ struct Oracle {
             int idx = block == 0 ? (e == 0 ? n % 3 : e == 1 ? (n / 3) % 3 : n / 9)
                                  : (e == 0 ? n % 2 : e == 1 ? (n / 2) % 2 : n / 4);
             double loc = block == 0 ? 0.5 * idx : (double)idx;
-            xi[e] = 0.5 * (((ch >> e) & 1) + loc);
+            xi[e] = ch == 255 ? loc : 0.5 * (((ch >> e) & 1) + loc);  // 255: the same cell
           }
           double phi[27];
           if (block == 0) q2_basis_at(d, xi, phi); else q1_basis_at(d, xi, phi);
@@ -627,8 +627,11 @@ struct Oracle {
         for (int c = 0; c < F.n_cells; ++c) {
           int ch = F.child[c], p = F.parent[c];
           // the parent vertex lying at this child's corner "ch" is parent vertex ch,
-          // and it is the child's own vertex ch
-          dg[l - 1][(size_t)p * nc_v + ch] = dg[l][(size_t)c * nc_v + ch];
+          // and it is the child's own vertex ch; an unchanged cell keeps all four/eight
+          if (ch == 255)
+            for (int i = 0; i < nc_v; ++i) dg[l - 1][(size_t)p * nc_v + i] = dg[l][(size_t)c * nc_v + i];
+          else
+            dg[l - 1][(size_t)p * nc_v + ch] = dg[l][(size_t)c * nc_v + ch];
         }
       }
       for (int l = 0; l < nlev; ++l) {
