@@ -56,14 +56,23 @@ struct DevBuf {
   void zero(cudaStream_t s) {
     if (n) GB_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
   }
+  // Host copies are set-up operations and are ordered against ALL device work:
+  // the library's streams are non-blocking, so a plain cudaMemcpy (legacy
+  // stream) neither waits for their kernels nor, from pageable memory, is
+  // guaranteed to have landed before a kernel launched next on them reads it.
   void upload(const T* h, size_t count) {
     alloc(count);
-    if (count) GB_CUDA(cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice));
+    if (!count) return;
+    GB_CUDA(cudaDeviceSynchronize());  // no kernel still reads the old contents
+    GB_CUDA(cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaDeviceSynchronize());  // the DMA has landed before later launches
   }
   void upload(const std::vector<T>& h) { upload(h.data(), h.size()); }
   std::vector<T> download() const {
     std::vector<T> h(n);
-    if (n) GB_CUDA(cudaMemcpy(h.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost));
+    if (!n) return h;
+    GB_CUDA(cudaDeviceSynchronize());  // producers on any stream have finished
+    GB_CUDA(cudaMemcpy(h.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost));
     return h;
   }
   size_t bytes() const { return n * sizeof(T); }

@@ -22,6 +22,9 @@
 #include <string>
 #include <vector>
 
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
 #include "../../include/gb_gmg.h"
 #include "level.cuh"
 
@@ -55,6 +58,9 @@ struct Handle {
   cudaGraphExec_t vgraph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
   long long vgraph_kernels[2][2] = {{0, 0}, {0, 0}};
   DevBuf<double> vin, vout;
+  // FP64 dense coarse solve: pseudo-inverses of the level-0 A and mass matrices
+  DevBuf<double> coarse_pinv[2], coarse_x, coarse_y;
+  bool coarse_ready = false;
 
   Level& top() { return levels.back(); }
   void reset_graphs() {
@@ -403,6 +409,21 @@ void smoother_smooth(Handle& H, int lev, int block, T* x, const T* b) {
   for (int k = 0; k < smoothing_steps(H, block); ++k) chebyshev<T>(H, lev, block, x, b, false);
 }
 
+// FP64 coarse-grid solve: sol = pinv(A_0) def, with the V-cycle's own precision at
+// the boundary (the coarse vectors are cast to FP64 and back)
+template <typename T>
+void coarse_dense(Handle& H, int block, T* sol, const T* def) {
+  Level& L = H.levels[0];
+  const long n = block == 0 ? L.n_u : L.n_p;
+  if constexpr (std::is_same<T, double>::value) {
+    v_symv_dense(n, H.coarse_pinv[block].p, def, sol, H.st);
+  } else {
+    v_cast<float, double>(n, def, H.coarse_x.p, H.st);
+    v_symv_dense(n, H.coarse_pinv[block].p, H.coarse_x.p, H.coarse_y.p, H.st);
+    v_cast<double, float>(n, H.coarse_y.p, sol, H.st);
+  }
+}
+
 template <typename T>
 void vcycle_level(Handle& H, int lev, int block) {
   Level& L = H.levels[lev];
@@ -412,7 +433,8 @@ void vcycle_level(Handle& H, int lev, int block) {
   T* t = block == 0 ? D.tA.p : D.tM.p;
   const long n = block == 0 ? L.n_u : L.n_p;
   if (lev == 0) {
-    smoother_apply<T>(H, 0, block, sol, def);
+    if (H.opt.coarse_solver == GB_GMG_COARSE_DENSE_FP64) coarse_dense<T>(H, block, sol, def);
+    else smoother_apply<T>(H, 0, block, sol, def);
     return;
   }
   Level& C = H.levels[lev - 1];
@@ -714,6 +736,93 @@ void alloc_level_work(Level& L, cudaStream_t st) {
   for (DevBuf<T>* b : {&D.solM, &D.defM, &D.tM, &D.dM}) { b->alloc(L.n_p); b->zero(st); }
 }
 
+__global__ void k_symmetrize(long n, double* M) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n * n) return;
+  const long r = i % n, c = i / n;
+  if (r < c) {
+    const double v = 0.5 * (M[r + c * n] + M[c + r * n]);
+    M[r + c * n] = v;
+    M[c + r * n] = v;
+  }
+}
+__global__ void k_scale_columns(long n, const double* V, const double* sc, double* U) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n * n) return;
+  U[i] = V[i] * sc[i / n];
+}
+
+#define GB_CUSOLVER(x)                                                                     \
+  do {                                                                                     \
+    if ((x) != CUSOLVER_STATUS_SUCCESS) throw ::gb::Error(3, "cuSOLVER error in " #x);     \
+  } while (0)
+#define GB_CUBLAS(x)                                                                       \
+  do {                                                                                     \
+    if ((x) != CUBLAS_STATUS_SUCCESS) throw ::gb::Error(3, "cuBLAS error in " #x);         \
+  } while (0)
+
+// Dense FP64 pseudo-inverses of the level-0 A and mass matrices: the matrices are
+// assembled column by column from the FP64 level operator, eigendecomposed once
+// (cuSOLVER syevd), and eigenvalues below 1e-10 lambda_max (null spaces) dropped.
+void build_dense_coarse(Handle& H) {
+  Level& L = H.levels[0];
+  cusolverDnHandle_t sol = nullptr;
+  cublasHandle_t blas = nullptr;
+  GB_CUSOLVER(cusolverDnCreate(&sol));
+  GB_CUBLAS(cublasCreate(&blas));
+  try {
+    GB_CUSOLVER(cusolverDnSetStream(sol, H.st));
+    GB_CUBLAS(cublasSetStream(blas, H.st));
+    const long nmax = std::max(L.n_u, L.n_p);
+    H.coarse_x.alloc(nmax);
+    H.coarse_y.alloc(nmax);
+    for (int block = 0; block < 2; ++block) {
+      const long n = block == 0 ? L.n_u : L.n_p;
+      DevBuf<double> M, U, W, work;
+      M.alloc((size_t)n * n);
+      U.alloc((size_t)n * n);
+      W.alloc(n);
+      double* e = H.coarse_x.p;
+      GB_CUDA(cudaMemsetAsync(e, 0, n * sizeof(double), H.st));
+      const double one = 1.0, zero = 0.0;
+      for (long j = 0; j < n; ++j) {
+        GB_CUDA(cudaMemcpyAsync(e + j, &one, sizeof(double), cudaMemcpyHostToDevice, H.st));
+        level_op<double>(H, 0, block, e, M.p + (size_t)j * n);
+        GB_CUDA(cudaMemcpyAsync(e + j, &zero, sizeof(double), cudaMemcpyHostToDevice, H.st));
+        GB_CUDA(cudaStreamSynchronize(H.st));  // the host scalars above must outlive the copies
+      }
+      k_symmetrize<<<ceil_div(n * n, 256), 256, 0, H.st>>>(n, M.p);
+      int lwork = 0;
+      GB_CUSOLVER(cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, (int)n, M.p,
+                                             (int)n, W.p, &lwork));
+      work.alloc(lwork);
+      DevBuf<int> info;
+      info.alloc(1);
+      GB_CUSOLVER(cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, (int)n, M.p, (int)n, W.p,
+                                  work.p, lwork, info.p));
+      std::vector<double> w = W.download();
+      const int inf = info.download()[0];
+      GB_CHECK(inf == 0, GB_GMG_CUDA_ERROR, "coarse eigendecomposition failed");
+      const double wmax = w.back();
+      for (double& v : w) v = v > 1e-10 * wmax ? 1.0 / v : 0.0;
+      W.upload(w);
+      k_scale_columns<<<ceil_div(n * n, 256), 256, 0, H.st>>>(n, M.p, W.p, U.p);
+      H.coarse_pinv[block].alloc((size_t)n * n);
+      // pinv = (V diag(s)) V^T
+      GB_CUBLAS(cublasDgemm(blas, CUBLAS_OP_N, CUBLAS_OP_T, (int)n, (int)n, (int)n, &one, U.p, (int)n, M.p, (int)n,
+                            &zero, H.coarse_pinv[block].p, (int)n));
+      GB_CUDA(cudaStreamSynchronize(H.st));
+    }
+  } catch (...) {
+    cusolverDnDestroy(sol);
+    cublasDestroy(blas);
+    throw;
+  }
+  cusolverDnDestroy(sol);
+  cublasDestroy(blas);
+  H.coarse_ready = true;
+}
+
 template <typename T>
 void build_preconditioner_T(Handle& H) {
   for (int l = 0; l < H.n_levels; ++l) {
@@ -866,6 +975,7 @@ void gb_gmg_default_options(gb_gmg_options* o) {
   o->coarse_eig_cg_iterations = 100;
   o->schur_smoothing_steps = 4;
   o->force_indexed_layout = 0;
+  o->coarse_solver = GB_GMG_COARSE_CHEBYSHEV;
 }
 
 void gb_gmg_default_solve_params(gb_gmg_solve_params* p) {
@@ -1041,6 +1151,7 @@ int gb_gmg_build_preconditioner(gb_gmg* g) {
     GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
     H.reset_graphs();
     gb::build_preconditioner_T<double>(H);
+    if (H.opt.coarse_solver == GB_GMG_COARSE_DENSE_FP64) gb::build_dense_coarse(H);
     H.prec_done[0] = true;
     gb::build_preconditioner_T<float>(H);
     H.prec_done[1] = true;

@@ -261,6 +261,25 @@ void v_multiaxpy(long n, int k, const double* coef_dev, const double* V, long ld
   count();
 }
 
+__global__ void k_symv_dense(long n, const double* __restrict__ S, const double* __restrict__ x,
+                             double* __restrict__ y) {
+  const long row = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  // S is symmetric: row `row` is read as column `row` (contiguous)
+  const double* col = S + row * n;
+  double t = 0;
+  for (long i = lane; i < n; i += 32) t += col[i] * x[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if (lane == 0) y[row] = t;
+}
+void v_symv_dense(long n, const double* S, const double* x, double* y, cudaStream_t s) {
+  if (n <= 0) return;
+  k_symv_dense<<<ceil_div(n * 32, 256), 256, 0, s>>>(n, S, x, y);
+  count();
+}
+
 template <typename T>
 __global__ void k_check_finite(long n, const T* __restrict__ x, int* flag) {
   int bad = 0;

@@ -55,6 +55,8 @@ template <typename T>
 void v_dot(long n, const T* a, const T* b, double* out_dev, double* partial, cudaStream_t s);
 // w += sum_j coef[j] V_j  (coef on the device)
 void v_multiaxpy(long n, int k, const double* coef_dev, const double* V, long ld, double* w, cudaStream_t s);
+// y = S x for a dense symmetric n x n matrix S (FP64), one warp per row
+void v_symv_dense(long n, const double* S, const double* x, double* y, cudaStream_t s);
 // NaN / Inf check: flag[0] |= 1 if any non-finite entry
 template <typename T>
 void v_check_finite(long n, const T* x, int* flag, cudaStream_t s);

@@ -260,3 +260,54 @@ def adaptive_sphere(base_depth: int = 4, n_adaptive: int = 2, radius: float = 0.
     return StokesProblem(f"adaptive_sphere_{2 ** base_depth}^3+{n_adaptive}", levels, eta, 1, s, rhs, 2,
                          extra=dict(cells_per_depth={int(d): int(np.sum(fine.cell_level == d))
                                                      for d in np.unique(fine.cell_level)}))
+
+
+def real_spherical_harmonics_field(x: np.ndarray, max_degree: int, seed: int) -> np.ndarray:
+    """sum_{l=1..max_degree} sum_m c_lm Y_lm(theta, phi) with seeded standard-normal
+    coefficients, real harmonics P_l^|m|(cos theta) {cos, sin}(|m| phi) normalised
+    per (l, m); returned divided by its maximum modulus over the points."""
+    from scipy.special import lpmv
+    r = np.linalg.norm(x, axis=-1)
+    ct = np.clip(x[..., 2] / r, -1, 1)
+    phi = np.arctan2(x[..., 1], x[..., 0])
+    rng = SplitMix64(seed)
+    out = np.zeros(x.shape[:-1])
+    for l in range(1, max_degree + 1):
+        for m in range(-l, l + 1):
+            c = rng.normal(1)[0]
+            am = abs(m)
+            norm = math.sqrt((2 * l + 1) / (4 * math.pi) * math.factorial(l - am) / math.factorial(l + am))
+            ang = np.cos(am * phi) if m >= 0 else np.sin(am * phi)
+            out += c * norm * lpmv(am, l, ct) * ang
+    return out / np.abs(out).max()
+
+
+def spherical_shell(n_refinements: int = 3, Ra: float = 1e5, contrast: float = 1e4,
+                    amplitude: float = 0.01, max_degree: int = 8, seed: int = BASE_SEED + 3,
+                    r_in: float = 0.55, r_out: float = 1.0) -> StokesProblem:
+    """Spherical shell r in [0.55, 1], the 96-cell cube-sphere refined n times,
+    T = conductive profile + amplitude sin(pi (r-r_in)/(r_out-r_in)) Y(theta, phi)
+    with Y a seeded real spherical-harmonic field of degree <= 8, eta =
+    exp(-ln(contrast) T) per quadrature point (Q1 projection), buoyancy
+    Ra T r_hat, free slip on both spheres (rotation null space)."""
+    from . import shell
+    levels = shell.hierarchy(n_refinements, 4, r_in, r_out)
+    fine = levels[-1]
+    xq, jxw = q_points_real(fine)
+    r = np.linalg.norm(xq, axis=-1)
+
+    def temperature(x, r):
+        t = (1 / r - 1 / r_out) / (1 / r_in - 1 / r_out)
+        env = np.sin(np.pi * (r - r_in) / (r_out - r_in))
+        return t + amplitude * env * real_spherical_harmonics_field(x, max_degree, seed)
+
+    T = temperature(xq, r)
+    eta = np.exp(-math.log(contrast) * T)
+    force = Ra * T[..., None] * xq / r[..., None]
+    rhs = assemble_rhs(fine, force)
+    mid = fine.map_points(np.full((1, 3), 0.5))[:, 0, :]
+    rm = np.linalg.norm(mid, axis=-1)
+    length = 1e4 / (6336000.0 - 3481000.0) * (r_out - r_in)
+    s = pressure_scaling(fine, np.exp(-math.log(contrast) * temperature(mid, rm)), length)
+    return StokesProblem(f"spherical_shell_ref{n_refinements}", levels, eta, 1, s, rhs, -1,
+                         extra=dict(temperature_q=T))

@@ -90,7 +90,14 @@ typedef struct gb_gmg_options {
   int coarse_eig_cg_iterations; /* level-0 eigenvalue CG steps (100)                 */
   int schur_smoothing_steps;    /* SmootherRelaxation steps for the Schur block (4)  */
   int force_indexed_layout;     /* 1: never use the lattice fast path (testing)      */
+  int coarse_solver;            /* gb_gmg_coarse_solver (Chebyshev as the reference)  */
 } gb_gmg_options;
+
+enum gb_gmg_coarse_solver {
+  GB_GMG_COARSE_CHEBYSHEV = 0,  /* one smoother application (MGCoarseGridApplySmoother) */
+  GB_GMG_COARSE_DENSE_FP64 = 1  /* FP64 pseudo-inverse of the level-0 matrices (handles
+                                   null spaces such as the rotations of a free-slip shell) */
+};
 
 typedef struct gb_gmg_solve_params {
   double linear_solver_tolerance;  /* relative (1e-7); tolerance rule of :977-1041   */
