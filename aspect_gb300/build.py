@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgb_gmg.so")
-SOURCES = ["kernels_f32.cu", "kernels_f64.cu", "adjoint.cu", "vec.cu", "level_setup.cu", "gb_gmg.cu", "noalloc.cu"]
+SOURCES = ["kernels_f32.cu", "kernels_f64.cu", "adjoint.cu", "vec.cu", "level_setup.cu", "gb_gmg.cu", "noalloc.cu", "mass_bottom.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

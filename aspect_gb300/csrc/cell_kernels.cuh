@@ -606,6 +606,131 @@ __global__ void __launch_bounds__(128) lattice_cell_kernel_f32(LevelView<float> 
   }
 }
 
+// FP32 A-block cell pass for small 3D lattice levels (the coarse levels of the
+// V-cycle): one cell per block, one thread per (component, node). The
+// register-resident kernel above runs each cell's ~5k straight-line
+// instructions on one thread, and with only a few hundred cells nothing hides
+// that chain (about 8-14 us per launch whatever the level's size). Here every
+// sum-factorisation sweep is a 3-term dot per thread followed by a barrier, so
+// the chain is a few dozen operations. Same arithmetic as the lattice kernel up
+// to the order of the sums; slot-major output, so the gather pass is shared.
+struct SmallLatticeTables {
+  float S[3][3];   // S[q][n]: node n -> Gauss point q (1D)
+  float D[3][3];   // D[q][a]: collocation derivative at Gauss point q
+  float W[27];     // 3D Gauss weights
+};
+__constant__ SmallLatticeTables c_small_tables = {
+    {{(float)fe::Sv(0, 0), (float)fe::Sv(0, 1), (float)fe::Sv(0, 2)},
+     {(float)fe::Sv(1, 0), (float)fe::Sv(1, 1), (float)fe::Sv(1, 2)},
+     {(float)fe::Sv(2, 0), (float)fe::Sv(2, 1), (float)fe::Sv(2, 2)}},
+    {{(float)fe::Dv(0, 0), (float)fe::Dv(0, 1), (float)fe::Dv(0, 2)},
+     {(float)fe::Dv(1, 0), (float)fe::Dv(1, 1), (float)fe::Dv(1, 2)},
+     {(float)fe::Dv(2, 0), (float)fe::Dv(2, 1), (float)fe::Dv(2, 2)}},
+    {(float)qweight<3, 0>(),  (float)qweight<3, 1>(),  (float)qweight<3, 2>(),  (float)qweight<3, 3>(),
+     (float)qweight<3, 4>(),  (float)qweight<3, 5>(),  (float)qweight<3, 6>(),  (float)qweight<3, 7>(),
+     (float)qweight<3, 8>(),  (float)qweight<3, 9>(),  (float)qweight<3, 10>(), (float)qweight<3, 11>(),
+     (float)qweight<3, 12>(), (float)qweight<3, 13>(), (float)qweight<3, 14>(), (float)qweight<3, 15>(),
+     (float)qweight<3, 16>(), (float)qweight<3, 17>(), (float)qweight<3, 18>(), (float)qweight<3, 19>(),
+     (float)qweight<3, 20>(), (float)qweight<3, 21>(), (float)qweight<3, 22>(), (float)qweight<3, 23>(),
+     (float)qweight<3, 24>(), (float)qweight<3, 25>(), (float)qweight<3, 26>()}};
+
+constexpr int kSmallCellThreads = 96;  // 81 active: (component, node)
+
+template <bool eta_per_q>
+__global__ void __launch_bounds__(kSmallCellThreads) lattice_cell_kernel_small(LevelView<float> L,
+                                                                               const float* __restrict__ src_u,
+                                                                               float* __restrict__ Eu) {
+  __shared__ float A[2][81];   // nodal / Gauss-point values, ping-pong between sweeps
+  __shared__ float G[9][27];   // G[c*3+d][q] = d u_c / d x_d, then the fluxes R in place
+  const SmallLatticeTables& K = c_small_tables;
+  const int cell = blockIdx.x;
+  const int t = threadIdx.x;
+  const bool act = t < 81;
+  const int c = act ? t / 27 : 0;
+  const int n = act ? t - 27 * c : 0;
+  const int dig[3] = {n % 3, (n / 3) % 3, n / 9};
+  const int st[3] = {1, 3, 9};
+  StructuredCell<float, 3> sc;
+  structured_cell_lex<float, 3>(L, cell, sc);
+  if (act)
+    A[0][t] = structured_zero<float, 3>(L, sc, c, n) ? 0.0f
+                                                     : src_u[c * L.n_nodes + sc.node0 + structured_node_offset<3>(L.Nn, n)];
+  __syncthreads();
+  // nodes -> Gauss points, directions 0, 1, 2
+  int cur = 0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (act) {
+      const int k = dig[d];
+      const float* a = &A[cur][c * 27 + n - k * st[d]];
+      A[cur ^ 1][t] = K.S[k][0] * a[0] + K.S[k][1] * a[st[d]] + K.S[k][2] * a[2 * st[d]];
+    }
+    cur ^= 1;
+    __syncthreads();
+  }
+  // gradient of component c at point q = n
+  if (act) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int k = dig[d];
+      const float* a = &A[cur][c * 27 + n - k * st[d]];
+      G[c * 3 + d][n] = (K.D[k][0] * a[0] + K.D[k][1] * a[st[d]] + K.D[k][2] * a[2 * st[d]]) * L.inv_h[d];
+    }
+  }
+  __syncthreads();
+  // fluxes at point q (27 threads): R[a][b] = eta (G[a][b] + G[b][a]) (deviatoric if compressible) * JxW / h_b
+  if (t < 27) {
+    const int q = t;
+    const float jxw = L.det * K.W[q];
+    const float eta = eta_per_q ? L.eta[(size_t)cell * 27 + q] : L.eta[cell];
+    float g[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) g[a][b] = G[a * 3 + b][q];
+    const float div = g[0][0] + g[1][1] + g[2][2];
+    float F[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) F[a][b] = eta * (g[a][b] + g[b][a]);
+    if (L.compressible) {
+      const float tr = 2.0f * eta / 3.0f * div;
+      F[0][0] -= tr; F[1][1] -= tr; F[2][2] -= tr;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) G[a * 3 + b][q] = F[a][b] * (L.inv_h[b] * jxw);
+  }
+  __syncthreads();
+  // transposed derivative: value at node-position n of component c
+  if (act) {
+    float v = 0.0f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int k = dig[d];
+      const int base = n - k * st[d];
+      const float* r = &G[c * 3 + d][base];
+      v += K.D[0][k] * r[0] + K.D[1][k] * r[st[d]] + K.D[2][k] * r[2 * st[d]];
+    }
+    A[cur][t] = v;
+  }
+  __syncthreads();
+  // Gauss points -> nodes (transposed interpolation), directions 0, 1, 2
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (act) {
+      const int k = dig[d];
+      const float* a = &A[cur][c * 27 + n - k * st[d]];
+      A[cur ^ 1][t] = K.S[0][k] * a[0] + K.S[1][k] * a[st[d]] + K.S[2][k] * a[2 * st[d]];
+    }
+    cur ^= 1;
+    __syncthreads();
+  }
+  if (act) Eu[(size_t)(c * 27 + n) * L.n_cells + cell] = A[cur][t];
+}
+
 template <typename T, int dim>
 __global__ void __launch_bounds__(128) mass_cell_kernel(LevelView<T> L, const T* __restrict__ src_p,
                                                          T* __restrict__ Ep) {
@@ -748,42 +873,80 @@ __global__ void __launch_bounds__(256) pressure_gather_structured(LevelView<T> L
   gather_epilogue<T, epi>(a, g, sum, false);
 }
 
-// Pressure mass operator of a lattice level in one pass: one thread per
-// pressure node multiplies the rows of its (at most 2^dim) cells' precomputed
-// local mass matrices (Mc[cell][i][j] = sum_q s^2/eta_q JxW_q psi_i psi_j)
-// with the cells' pressure values. It reads x at neighbouring nodes, so a
-// Chebyshev step writes its new iterate to a separate vector (EPI_CHEB_OUT).
-template <typename T, int dim, int epi>
-__global__ void __launch_bounds__(256) mass_apply_lattice(LevelView<T> L, const T* __restrict__ Mc,
-                                                           GatherArgs<T> a) {
-  constexpr int np = Shape<dim>::np;
-  const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (g >= L.n_p) return;
-  const int node = (int)g;
-  const int gc[3] = {node % L.Np[0], (node / L.Np[0]) % L.Np[1], dim == 3 ? node / (L.Np[0] * L.Np[1]) : 0};
-  int cidx[3][2], loc[3][2], cnt[3];
+// Pressure mass operator of a lattice level in one pass, from the cells'
+// precomputed local mass matrices (Mc[cell][i][j] = sum_q s^2/eta_q JxW_q
+// psi_i psi_j). A pressure node touches at most 2^dim cells; each (node, cell)
+// pair gets its own thread (2^dim consecutive lanes per node), which reads the
+// node's row of that cell's matrix with vector loads and dots it with the
+// cell's pressure values; the lanes of a node are summed with xor shuffles and
+// the first lane runs the epilogue. (One thread per node left too few warps to
+// hide the L2 latency of the 2^dim rows.) The operator reads x at neighbouring
+// nodes, so a Chebyshev step writes its new iterate to a separate vector
+// (EPI_CHEB_OUT).
+constexpr int kMassLatticeThreads = 256;
+
+// (generic loads: the rows may live in global or in shared memory)
+template <typename T, int np>
+__device__ __forceinline__ void load_row(const T* __restrict__ row, T (&r)[np]) {
+  if constexpr (sizeof(T) == 4 && np % 4 == 0) {
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    cnt[d] = 0;
-    if (d >= dim) { cnt[d] = 1; cidx[d][0] = 0; loc[d][0] = 0; continue; }
-    const int x = gc[d];
-    if (x > 0) { cidx[d][cnt[d]] = x - 1; loc[d][cnt[d]] = 1; ++cnt[d]; }
-    if (x < L.Np[d] - 1) { cidx[d][cnt[d]] = x; loc[d][cnt[d]] = 0; ++cnt[d]; }
+    for (int j = 0; j < np; j += 4) {
+      const float4 v = *reinterpret_cast<const float4*>(row + j);
+      r[j] = v.x; r[j + 1] = v.y; r[j + 2] = v.z; r[j + 3] = v.w;
+    }
+  } else if constexpr (sizeof(T) == 8 && np % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < np; j += 2) {
+      const double2 v = *reinterpret_cast<const double2*>(row + j);
+      r[j] = v.x; r[j + 1] = v.y;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < np; ++j) r[j] = row[j];
   }
-  const T* __restrict__ xin = a.x;
-  T sum = T(0);
-  for (int kz = 0; kz < cnt[2]; ++kz)
-    for (int ky = 0; ky < cnt[1]; ++ky)
-      for (int kx = 0; kx < cnt[0]; ++kx) {
-        const int cz = cidx[2][kz], cy = cidx[1][ky], cx = cidx[0][kx];
-        const int cell = (cz * L.nc[1] + cy) * L.nc[0] + cx;
-        const int l = loc[0][kx] + 2 * loc[1][ky] + 4 * loc[2][kz];
-        const T* __restrict__ row = Mc + ((size_t)cell * np + l) * np;
-        const int p0 = (cz * L.Np[1] + cy) * L.Np[0] + cx;
+}
+
+// Task t = (node t / 2^dim, cell slot t % 2^dim). All 32 lanes of a warp must
+// call it together (the lanes of a node are summed with shuffles); tasks past
+// the last node only take part in the shuffles.
+template <typename T, int dim, int epi>
+__device__ __forceinline__ void mass_lattice_task(const LevelView<T>& L, const T* __restrict__ Mc,
+                                                  const GatherArgs<T>& a, long t) {
+  constexpr int np = Shape<dim>::np;  // = lanes per node
+  const long g = t / np;
+  const int s = (int)(t % np);
+  const bool node_ok = g < L.n_p;
+  const int node = node_ok ? (int)g : 0;
+  const int gc[3] = {node % L.Np[0], (node / L.Np[0]) % L.Np[1], dim == 3 ? node / (L.Np[0] * L.Np[1]) : 0};
+  // slot bit d = 0: the cell below the node along d (node at its local 1), 1: above (local 0)
+  int c[3] = {0, 0, 0}, l = 0;
+  bool ok = node_ok;
 #pragma unroll
-        for (int j = 0; j < np; ++j) sum += row[j] * xin[p0 + structured_pnode_offset<dim>(L.Np, j)];
-      }
-  gather_epilogue<T, epi>(a, g, sum, false);
+  for (int d = 0; d < dim; ++d) {
+    const int bit = (s >> d) & 1;
+    c[d] = gc[d] - 1 + bit;
+    ok = ok && c[d] >= 0 && c[d] < L.nc[d];
+    l += (bit ? 0 : 1) << d;
+  }
+  T sum = T(0);
+  if (ok) {
+    const int cell = (c[2] * L.nc[1] + c[1]) * L.nc[0] + c[0];
+    T r[np];
+    load_row<T, np>(Mc + ((size_t)cell * np + l) * np, r);
+    const int p0 = (c[2] * L.Np[1] + c[1]) * L.Np[0] + c[0];
+    const T* __restrict__ xin = a.x;
+#pragma unroll
+    for (int j = 0; j < np; ++j) sum += r[j] * xin[p0 + structured_pnode_offset<dim>(L.Np, j)];
+  }
+#pragma unroll
+  for (int o = 1; o < np; o <<= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if (node_ok && s == 0) gather_epilogue<T, epi>(a, g, sum, false);
+}
+
+template <typename T, int dim, int epi>
+__global__ void __launch_bounds__(kMassLatticeThreads) mass_apply_lattice(LevelView<T> L, const T* __restrict__ Mc,
+                                                                          GatherArgs<T> a) {
+  mass_lattice_task<T, dim, epi>(L, Mc, a, blockIdx.x * (long)blockDim.x + threadIdx.x);
 }
 
 template <typename T, int epi>

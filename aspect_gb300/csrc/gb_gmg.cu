@@ -27,6 +27,7 @@
 
 #include "../../include/gb_gmg.h"
 #include "level.cuh"
+#include "mass_bottom.cuh"
 
 namespace gb {
 
@@ -49,6 +50,8 @@ struct Handle {
   DevBuf<double> stage_a, stage_b, partial, dots_d;
   double* dots_h = nullptr;
   DevBuf<double> V, Z, wv, xv, rv, bv, tv, t2v, coef_d;
+  DevBuf<double> hcol_d, arn_d;  // Arnoldi column and scalars (|w|^2, |w| before) on the device
+  DevBuf<int> arn_flag;          // 1: the step needs its second Gram-Schmidt pass
   DevBuf<double> cg_r, cg_z, cg_p, cg_q, cg_x;
   DevBuf<float> f32_a, f32_b;
   int restart_alloc = -1;
@@ -61,6 +64,8 @@ struct Handle {
   // FP64 dense coarse solve: pseudo-inverses of the level-0 A and mass matrices
   DevBuf<double> coarse_pinv[2], coarse_x, coarse_y;
   bool coarse_ready = false;
+  // levels 0..mass_bottom_top of the FP32 mass V-cycle run in one single-block launch (-1: none)
+  int mass_bottom_top = -1;
 
   Level& top() { return levels.back(); }
   void reset_graphs() {
@@ -424,8 +429,81 @@ void coarse_dense(Handle& H, int block, T* sol, const T* def) {
   }
 }
 
+// Levels 0..K of the FP32 mass V-cycle as one launch (see mass_bottom.cu): the
+// same steps, coefficients and vectors as the multi-launch recursion below.
+void mass_bottom(Handle& H, int K) {
+  MassBottomArgs A{};
+  A.n_levels = K + 1;
+  for (int l = 0; l <= K; ++l) {
+    Level& L = H.levels[l];
+    LevelDev<float>& D = L.f32;
+    MassBottomLevel& V = A.lev[l];
+    V.L = L.view<float>(H.s, H.compressible);
+    V.Mc = D.Mp.p;
+    V.dinv = D.dinvM.p;
+    V.sol = D.solM.p;
+    V.def = D.defM.p;
+    V.d = D.dM.p;
+    V.t = D.tM.p;
+    if (l >= 1) {
+      V.pt_rows = (int)L.PpT_rows;
+      V.pt_ptr = L.PpT_ptr.p;
+      V.pt_col = L.PpT_col.p;
+      V.pt_val = D.PpT_val.p;
+      V.p_rows = (int)L.Pp_rows;
+      V.p_ptr = L.Pp_ptr.p;
+      V.p_col = L.Pp_col.p;
+      V.p_val = D.Pp_val.p;
+    }
+    const ChebParams cp = cheb_params(H, l);
+    double theta, delta;
+    chebyshev_bounds<float>(H, l, 1, theta, delta);
+    V.degree = cp.degree;
+    V.steps = smoothing_steps(H, 1);
+    V.inv_theta = (float)(1.0 / theta);
+    double rhok = delta / theta;
+    const double sigma = theta / delta;
+    for (int k = 1; k < cp.degree; ++k) {
+      const double rhokp = 1.0 / (2.0 * sigma - rhok);
+      V.f1[k] = (float)(rhokp * rhok);
+      V.f2[k] = (float)(2.0 * rhokp / delta);
+      rhok = rhokp;
+    }
+  }
+  launch_mass_vcycle_bottom(A, mass_bottom_layout(A), H.st);
+  ++H.cell_launches;
+}
+
+// the highest level K such that levels 0..K qualify for mass_bottom: 3D lattice
+// levels of at most kMaxBottomNodes pressure nodes whose shared-memory copies
+// fit one block, the Chebyshev coarse solver, degrees that fit the argument
+// block
+int plan_mass_bottom(const Handle& H) {
+  if (H.opt.coarse_solver != GB_GMG_COARSE_CHEBYSHEV) return -1;
+  const int smem_limit = mass_bottom_reserve();
+  MassBottomArgs A{};
+  int K = -1;
+  for (int l = 0; l < H.n_levels && l < kMaxBottomLevels; ++l) {
+    const Level& L = H.levels[l];
+    const int degree = cheb_params(H, l).degree;
+    if (!L.structured || L.dim != 3 || L.n_p > kMaxBottomNodes || degree < 1 || degree > kMaxBottomDegree) break;
+    A.n_levels = l + 1;
+    A.lev[l].L.n_cells = (int)L.n_cells;
+    A.lev[l].L.n_p = (int)L.n_p;
+    if (mass_bottom_layout(A) > smem_limit) break;
+    K = l;
+  }
+  return K;
+}
+
 template <typename T>
 void vcycle_level(Handle& H, int lev, int block) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (block == 1 && lev <= H.mass_bottom_top) {
+      mass_bottom(H, lev);
+      return;
+    }
+  }
   Level& L = H.levels[lev];
   LevelDev<T>& D = L.dev<T>();
   T* sol = block == 0 ? D.solA.p : D.solM.p;
@@ -547,7 +625,17 @@ void block_preconditioner(Handle& H, int prec, bool expensive, const gb_gmg_solv
     if (sn > 1e-50) H.nS += cg_solve(H, 1, prec, np, dst + nu, src + nu, sn * P->tol_S, 100) - 0;
   }
   v_scale<double>(np, -1.0, dst + nu, H.st);
-  apply_op<double>(H, H.n_levels - 1, OPK_BT, nullptr, dst + nu, H.t2v.p, nullptr);
+  if (prec == GB_GMG_FP32) {
+    // with FP32 V-cycles the B^T product of the preconditioner is FP32 as well:
+    // its result only feeds the FP32 velocity V-cycle
+    float* p32 = H.f32_a.p + nu;
+    float* bt32 = H.f32_b.p;
+    v_cast<double, float>(np, dst + nu, p32, H.st);
+    apply_op<float>(H, H.n_levels - 1, OPK_BT, nullptr, p32, bt32, nullptr);
+    v_cast<float, double>(nu, bt32, H.t2v.p, H.st);
+  } else {
+    apply_op<double>(H, H.n_levels - 1, OPK_BT, nullptr, dst + nu, H.t2v.p, nullptr);
+  }
   v_axpby<double>(nu, 1.0, src, -1.0, H.t2v.p, H.st);  // t = src_u - B^T p
   if (!expensive) {
     vcycle(H, 0, prec, H.t2v.p, dst);
@@ -599,6 +687,9 @@ void ensure_krylov(Handle& H, int restart) {
   H.V.alloc((size_t)(restart + 1) * n);
   H.Z.alloc((size_t)restart * n);
   H.coef_d.alloc(restart + 2);
+  H.hcol_d.alloc(restart + 2);
+  H.arn_d.alloc(2);
+  H.arn_flag.alloc(1);
   if (H.dots_d.n < (size_t)restart + 2) {
     H.dots_d.alloc(restart + 2);
     if (H.dots_h) cudaFreeHost(H.dots_h);
@@ -606,6 +697,37 @@ void ensure_krylov(Handle& H, int restart) {
     GB_CUDA(cudaMallocHost(&H.dots_h, (restart + 2) * sizeof(double)));
   }
   H.restart_alloc = restart;
+}
+
+// Device-side bookkeeping of classical Gram-Schmidt for Arnoldi step j.
+// pass 0: h[0..j] = dots, coef = -dots, arn[1] = sqrt(dots[j+1]) (|w| before);
+// pass 1 (only while *need2): h += dots, coef = -dots.
+__global__ void k_cgs_coef(int j, int pass, const double* __restrict__ dots, double* __restrict__ h,
+                           double* __restrict__ coef, double* __restrict__ arn, const int* __restrict__ need2) {
+  if (pass == 1 && *need2 == 0) return;
+  for (int i = threadIdx.x; i <= j; i += blockDim.x) {
+    const double v = dots[i];
+    h[i] = pass == 0 ? v : h[i] + v;
+    coef[i] = -v;
+  }
+  if (pass == 0 && threadIdx.x == 0) arn[1] = sqrt(dots[j + 1]);
+}
+// after w -= V coef and arn[0] = <w, w>: h[j+1] = |w|; pass 0 decides whether
+// the second pass runs (|w| <= 0.7 |w before|)
+__global__ void k_cgs_norm(int j, int pass, double* __restrict__ h, const double* __restrict__ arn,
+                           int* __restrict__ need2) {
+  if (pass == 1 && *need2 == 0) return;
+  const double nw = sqrt(arn[0]);
+  h[j + 1] = nw;
+  if (pass == 0) *need2 = nw > 0.7 * arn[1] ? 0 : 1;
+}
+// next basis vector v = w / h[j+1] (w itself when h[j+1] = 0)
+__global__ void k_next_basis(long n, const double* __restrict__ h, int j, const double* __restrict__ w,
+                             double* __restrict__ v) {
+  const double hn = h[j + 1];
+  const double sc = 1.0 / (hn > 0 ? hn : 1.0);
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    v[i] = sc * w[i];
 }
 
 // Solves K x = b (right preconditioning). Returns iterations.
@@ -625,7 +747,6 @@ int gmres(Handle& H, double* x, const double* b, double tol, int maxit, int rest
   };
   int it = 0;
   converged = false;
-  std::vector<double> hbuf(restart + 2);
   while (true) {
     K(x, tmp);
     v_copy<double>(n, b, r, H.st);
@@ -646,28 +767,29 @@ int gmres(Handle& H, double* x, const double* b, double tol, int maxit, int rest
       block_preconditioner(H, prec, expensive, P, vj, zj);
       K(zj, w);
       ++it;
-      std::vector<double> h(j + 2, 0.0);
-      // classical Gram-Schmidt with one conditional re-orthogonalisation
+      // classical Gram-Schmidt with one conditional re-orthogonalisation, all
+      // scalars on the device: the second pass runs only if the device finds
+      // |w| <= 0.7 |w before|, and the one round trip per step is the copy of
+      // the finished Hessenberg column for the Givens update below
+      double* hcol = H.hcol_d.p;
+      double* arn = H.arn_d.p;
+      int* need2 = H.arn_flag.p;
+      double* vnext = V + (size_t)(j + 1) * n;
       v_multidot(n, w, V, n, j + 1, true, H.dots_d.p, H.partial.p, H.st);
-      GB_CUDA(cudaMemcpyAsync(H.dots_h, H.dots_d.p, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, H.st));
+      k_cgs_coef<<<1, 128, 0, H.st>>>(j, 0, H.dots_d.p, hcol, H.coef_d.p, arn, need2);
+      v_multiaxpy(n, j + 1, H.coef_d.p, V, n, w, H.st);
+      v_dot<double>(n, w, w, arn, H.partial.p, H.st);
+      k_cgs_norm<<<1, 1, 0, H.st>>>(j, 0, hcol, arn, need2);
+      v_multidot(n, w, V, n, j + 1, false, H.dots_d.p, H.partial.p, H.st, need2);
+      k_cgs_coef<<<1, 128, 0, H.st>>>(j, 1, H.dots_d.p, hcol, H.coef_d.p, arn, need2);
+      v_multiaxpy(n, j + 1, H.coef_d.p, V, n, w, H.st, need2);
+      v_dot<double>(n, w, w, arn, H.partial.p, H.st, need2);
+      k_cgs_norm<<<1, 1, 0, H.st>>>(j, 1, hcol, arn, need2);
+      k_next_basis<<<ceil_div(n, 256), 256, 0, H.st>>>(n, hcol, j, w, vnext);
+      VecCounter::launches() += 5;
+      GB_CUDA(cudaMemcpyAsync(H.dots_h, hcol, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, H.st));
       GB_CUDA(cudaStreamSynchronize(H.st));
-      const double norm_before = std::sqrt(H.dots_h[j + 1]);
-      for (int pass = 0; pass < 2; ++pass) {
-        if (pass == 1) {
-          v_multidot(n, w, V, n, j + 1, false, H.dots_d.p, H.partial.p, H.st);
-          GB_CUDA(cudaMemcpyAsync(H.dots_h, H.dots_d.p, (j + 1) * sizeof(double), cudaMemcpyDeviceToHost, H.st));
-          GB_CUDA(cudaStreamSynchronize(H.st));
-        }
-        for (int i = 0; i <= j; ++i) {
-          hbuf[i] = -H.dots_h[i];
-          h[i] += H.dots_h[i];
-        }
-        GB_CUDA(cudaMemcpyAsync(H.coef_d.p, hbuf.data(), (j + 1) * sizeof(double), cudaMemcpyHostToDevice, H.st));
-        v_multiaxpy(n, j + 1, H.coef_d.p, V, n, w, H.st);
-        const double nw = std::sqrt(dot_host(H, n, w, w));
-        h[j + 1] = nw;
-        if (pass == 0 && nw > 0.7 * norm_before) break;
-      }
+      std::vector<double> h(H.dots_h, H.dots_h + j + 2);
       const double hn = h[j + 1];
       for (int i = 0; i < j; ++i) {
         const double t = cs[i] * h[i] + sn[i] * h[i + 1];
@@ -684,8 +806,7 @@ int gmres(Handle& H, double* x, const double* b, double tol, int maxit, int rest
       g.push_back(-s_ * g[j]);
       g[j] = c_ * g[j];
       Hc.push_back(h);
-      v_copy<double>(n, w, V + (size_t)(j + 1) * n, H.st);
-      v_scale<double>(n, 1.0 / (hn > 0 ? hn : 1.0), V + (size_t)(j + 1) * n, H.st);
+      (void)hn;
       final_res = std::fabs(g[j + 1]);
       if (final_res <= tol) { ++j; break; }
     }
@@ -1154,6 +1275,7 @@ int gb_gmg_build_preconditioner(gb_gmg* g) {
     if (H.opt.coarse_solver == GB_GMG_COARSE_DENSE_FP64) gb::build_dense_coarse(H);
     H.prec_done[0] = true;
     gb::build_preconditioner_T<float>(H);
+    H.mass_bottom_top = gb::plan_mass_bottom(H);
     H.prec_done[1] = true;
   })
 }
@@ -1427,8 +1549,8 @@ int gb_gmg_time_operation(gb_gmg* g, int what, int precision, int repeats, doubl
   ABI_TRY(g, {
     Handle& H = g->h;
     const int pi = precision == GB_GMG_FP32 ? 1 : 0;
-    GB_CHECK(what >= 0 && what <= 5, 1, "unknown operation");
-    if (what >= 3) GB_CHECK(H.prec_done[pi], GB_GMG_NOT_READY, "build_preconditioner has not been called");
+    GB_CHECK(what >= 0 && what <= 6, 1, "unknown operation");
+    if (what >= 3 && what <= 5) GB_CHECK(H.prec_done[pi], GB_GMG_NOT_READY, "build_preconditioner has not been called");
     else GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
     const int top = H.n_levels - 1;
     gb::Level& F = H.levels[top];
@@ -1462,6 +1584,18 @@ int gb_gmg_time_operation(gb_gmg* g, int what, int precision, int repeats, doubl
         }
         case 4: gb::vcycle(H, 0, precision, a, b); break;
         case 5: gb::vcycle(H, 1, precision, a + nu, b + nu); break;
+        case 6: {
+          if (pi) {
+            gb::LevelDev<float>& D = F.f32;
+            gb::launch_cell_pass<float>(F.view<float>(H.s, H.compressible), gb::OPK_A, H.f32_a.p, nullptr, D.Eu.p,
+                                        D.Ep.p, H.st);
+          } else {
+            gb::LevelDev<double>& D = F.f64;
+            gb::launch_cell_pass<double>(F.view<double>(H.s, H.compressible), gb::OPK_A, a, nullptr, D.Eu.p, D.Ep.p,
+                                         H.st);
+          }
+          break;
+        }
       }
     };
     call();

@@ -1,0 +1,57 @@
+// Arguments of the single-block kernel that runs the lower levels of the FP32
+// pressure-mass V-cycle (mass_bottom.cu).
+#pragma once
+#include "cell_kernels.cuh"
+
+namespace gb {
+
+constexpr int kMaxBottomLevels = 4;
+constexpr int kMaxBottomDegree = 16;
+// Levels above this many pressure nodes keep the per-step launches. Measured on
+// the 32^3 lattice hierarchy (Schur V-cycle, FP32, one GB300): nothing fused
+// 0.474 ms, levels of <= 27 nodes 0.470 ms, <= 125 nodes 0.445 ms, <= 729 nodes
+// 0.555 ms -- one block is slower than the whole GPU on the 729-node level.
+constexpr int kMaxBottomNodes = 200;
+
+struct MassBottomLevel {
+  LevelView<float> L;  // lattice geometry (n_p, Np, nc)
+  // device vectors of the level; the kernel replaces them by shared-memory
+  // copies (the defect of the top level is its input, the solution its output)
+  const float* Mc;     // per-cell 8x8 mass matrices
+  const float* dinv;
+  float* sol;
+  float* def;
+  float* d;
+  float* t;
+  // transfers to the next coarser level (levels >= 1): restriction P^T, prolongation P
+  int pt_rows, p_rows;
+  const int* pt_ptr;
+  const int* pt_col;
+  const float* pt_val;
+  const int* p_ptr;
+  const int* p_col;
+  const float* p_val;
+  // Chebyshev: degree, sweeps per smoothing call, f2 of the first step (1/theta),
+  // and (f1, f2) of steps 1 .. degree-1
+  int degree, steps;
+  float inv_theta;
+  float f1[kMaxBottomDegree], f2[kMaxBottomDegree];
+  // offsets (in floats, multiples of 4) of this level's shared-memory copies:
+  // Mc, dinv, sol, def, d, t
+  int off[6];
+};
+
+struct MassBottomArgs {
+  int n_levels;  // levels 0 .. n_levels-1 of the hierarchy
+  MassBottomLevel lev[kMaxBottomLevels];
+};
+
+// Fills lev[l].off for levels 0..n_levels-1 and returns the dynamic shared
+// memory the launch needs, in bytes.
+int mass_bottom_layout(MassBottomArgs& A);
+// Largest dynamic shared memory a launch may use, in bytes (sets the kernel
+// attribute the first time; call outside stream capture).
+int mass_bottom_reserve();
+void launch_mass_vcycle_bottom(const MassBottomArgs& A, int smem_bytes, cudaStream_t s);
+
+}  // namespace gb

@@ -184,7 +184,9 @@ __device__ __forceinline__ void block_reduce_store(double (&acc)[K], int nk, dou
 
 __global__ void __launch_bounds__(kDotThreads) k_multidot(long n, const double* __restrict__ w,
                                                           const double* __restrict__ V, long ld, int k,
-                                                          int with_norm, double* __restrict__ partial) {
+                                                          int with_norm, double* __restrict__ partial,
+                                                          const int* __restrict__ active) {
+  if (active && *active == 0) return;
   double acc[kDotChunk + 1];
 #pragma unroll
   for (int j = 0; j <= kDotChunk; ++j) acc[j] = 0;
@@ -199,7 +201,9 @@ __global__ void __launch_bounds__(kDotThreads) k_multidot(long n, const double* 
   block_reduce_store<kDotChunk + 1>(acc, k + with_norm, partial, kDotBlocks);
 }
 
-__global__ void k_finish(const double* __restrict__ partial, int nk, double* __restrict__ out) {
+__global__ void k_finish(const double* __restrict__ partial, int nk, double* __restrict__ out,
+                         const int* __restrict__ active) {
+  if (active && *active == 0) return;
   const int j = blockIdx.x;
   if (j >= nk) return;
   __shared__ double sh[32];
@@ -215,49 +219,52 @@ __global__ void k_finish(const double* __restrict__ partial, int nk, double* __r
 }
 
 void v_multidot(long n, const double* w, const double* V, long ld, int k, bool with_norm, double* out_dev,
-                double* partial, cudaStream_t s) {
+                double* partial, cudaStream_t s, const int* active) {
   if (k == 0) {
     if (!with_norm) return;
-    k_multidot<<<kDotBlocks, kDotThreads, 0, s>>>(n, w, V, ld, 0, 1, partial);
-    k_finish<<<1, 32, 0, s>>>(partial, 1, out_dev);
+    k_multidot<<<kDotBlocks, kDotThreads, 0, s>>>(n, w, V, ld, 0, 1, partial, active);
+    k_finish<<<1, 32, 0, s>>>(partial, 1, out_dev, active);
     VecCounter::launches() += 2;
     return;
   }
   for (int done = 0; done < k; done += kDotChunk) {
     const int kk = k - done < kDotChunk ? k - done : kDotChunk;
     const int norm = (with_norm && done + kk == k) ? 1 : 0;
-    k_multidot<<<kDotBlocks, kDotThreads, 0, s>>>(n, w, V + done * ld, ld, kk, norm, partial);
-    k_finish<<<kk + norm, 32, 0, s>>>(partial, kk + norm, out_dev + done);
+    k_multidot<<<kDotBlocks, kDotThreads, 0, s>>>(n, w, V + done * ld, ld, kk, norm, partial, active);
+    k_finish<<<kk + norm, 32, 0, s>>>(partial, kk + norm, out_dev + done, active);
     VecCounter::launches() += 2;
   }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kDotThreads) k_dot(long n, const T* __restrict__ a, const T* __restrict__ b,
-                                                     double* __restrict__ partial) {
+                                                     double* __restrict__ partial, const int* __restrict__ active) {
+  if (active && *active == 0) return;
   double acc[1] = {0};
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     acc[0] += (double)a[i] * (double)b[i];
   block_reduce_store<1>(acc, 1, partial, kDotBlocks);
 }
 template <typename T>
-void v_dot(long n, const T* a, const T* b, double* out_dev, double* partial, cudaStream_t s) {
-  k_dot<T><<<kDotBlocks, kDotThreads, 0, s>>>(n, a, b, partial);
-  k_finish<<<1, 32, 0, s>>>(partial, 1, out_dev);
+void v_dot(long n, const T* a, const T* b, double* out_dev, double* partial, cudaStream_t s, const int* active) {
+  k_dot<T><<<kDotBlocks, kDotThreads, 0, s>>>(n, a, b, partial, active);
+  k_finish<<<1, 32, 0, s>>>(partial, 1, out_dev, active);
   VecCounter::launches() += 2;
 }
 
 __global__ void k_multiaxpy(long n, int k, const double* __restrict__ coef, const double* __restrict__ V, long ld,
-                            double* __restrict__ w) {
+                            double* __restrict__ w, const int* __restrict__ active) {
+  if (active && *active == 0) return;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     double t = w[i];
     for (int j = 0; j < k; ++j) t += coef[j] * V[j * ld + i];
     w[i] = t;
   }
 }
-void v_multiaxpy(long n, int k, const double* coef_dev, const double* V, long ld, double* w, cudaStream_t s) {
+void v_multiaxpy(long n, int k, const double* coef_dev, const double* V, long ld, double* w, cudaStream_t s,
+                 const int* active) {
   if (n <= 0 || k <= 0) return;
-  k_multiaxpy<<<grid_for(n), kThreads, 0, s>>>(n, k, coef_dev, V, ld, w);
+  k_multiaxpy<<<grid_for(n), kThreads, 0, s>>>(n, k, coef_dev, V, ld, w, active);
   count();
 }
 
@@ -304,7 +311,7 @@ void v_check_finite(long n, const T* x, int* flag, cudaStream_t s) {
   template void v_copy_indexed<T>(long, const int*, const T*, T*, cudaStream_t);                  \
   template void v_zero_indexed<T>(long, const int*, T*, cudaStream_t);                            \
   template void v_spmv_add<T>(long, const int*, const int*, const T*, const T*, T*, cudaStream_t); \
-  template void v_dot<T>(long, const T*, const T*, double*, double*, cudaStream_t);               \
+  template void v_dot<T>(long, const T*, const T*, double*, double*, cudaStream_t, const int*);               \
   template void v_check_finite<T>(long, const T*, int*, cudaStream_t);
 INST(float)
 INST(double)

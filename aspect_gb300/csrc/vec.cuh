@@ -47,14 +47,19 @@ void v_permute_gather(long n, const int* perm, const Ts* in, Td* out, cudaStream
 // y += A x (CSR)
 template <typename T>
 void v_spmv_add(long rows, const int* ptr, const int* col, const T* val, const T* x, T* y, cudaStream_t s);
+// The reductions and the multi-axpy take an optional device flag `active`: when
+// it points to 0 the launches return at once (a step that the device decided to
+// skip without a round trip to the host).
 // out[j] = <w, V_j> for j < k (V rows of stride ld), plus out[k] = <w, w> if with_norm
 // partial: workspace of (kDotChunk+1) * kDotBlocks doubles
 void v_multidot(long n, const double* w, const double* V, long ld, int k, bool with_norm, double* out_dev,
-                double* partial, cudaStream_t s);
+                double* partial, cudaStream_t s, const int* active = nullptr);
 template <typename T>
-void v_dot(long n, const T* a, const T* b, double* out_dev, double* partial, cudaStream_t s);
+void v_dot(long n, const T* a, const T* b, double* out_dev, double* partial, cudaStream_t s,
+           const int* active = nullptr);
 // w += sum_j coef[j] V_j  (coef on the device)
-void v_multiaxpy(long n, int k, const double* coef_dev, const double* V, long ld, double* w, cudaStream_t s);
+void v_multiaxpy(long n, int k, const double* coef_dev, const double* V, long ld, double* w, cudaStream_t s,
+                 const int* active = nullptr);
 // y = S x for a dense symmetric n x n matrix S (FP64), one warp per row
 void v_symv_dense(long n, const double* S, const double* x, double* y, cudaStream_t s);
 // NaN / Inf check: flag[0] |= 1 if any non-finite entry

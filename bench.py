@@ -8,6 +8,10 @@ averaging for GMG), free slip, FGMRES (restart 100) with the block-Schur
 preconditioner and an FP32 V-cycle, FP64 outer residual, relative tolerance 1e-8.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+    python bench.py --profile-op a_cell_pass_fp32|stokes_vmult_fp64|mass_vmult_fp32|a_vmult_fp32
+
+(--profile-op runs one operation of the workload three times between
+cudaProfilerStart/Stop, for `ncu --profile-from-start off` captures.)
 
 `value` is DoFs solved per second with inputs resident in HBM (device-timed);
 `e2e` is the same through the host-array C ABI (gb_gmg_solve) with the host<->device
@@ -36,6 +40,20 @@ WORKLOAD = "sinkers_32^3_Q2Q1_eta1e6_q1proj_fgmres_fp32mg_tol1e-8"
 TOL = 1e-8
 N_CELLS_1D = 32
 CPU_SAMPLE_ITERATIONS = 12
+# Arithmetic per cell of the two cell kernels, counted from their source (an FMA
+# counts 2): the FP32 lattice A-block cell pass (3 x 270 interpolation, 27 x 141
+# per point, 3 x 270 transposed interpolation) and the FP64 Stokes cell pass
+# (3 threads x (270 + 27 x 86 + 270)).
+FLOPS_A_CELL_F32 = 5427
+FLOPS_STOKES_CELL_F64 = 8586
+# nominal CUDA-core peaks (no measured figure is recorded for them): FP32 =
+# 152 SMs x 128 lanes x 2 x 2.07 GHz; FP64 = GB300's published 1.25 TFLOP/s
+FP32_PEAK_TFLOPS = 80.5
+FP64_PEAK_TFLOPS = 1.25
+# dram__bytes_read.sum + dram__bytes_write.sum of one finest-level launch of the
+# FP32 A-block cell pass (ncu --set full of `bench.py --profile-op
+# a_cell_pass_fp32`, summarised in profiles/); None until captured
+CELL_PASS_DRAM_BYTES = None
 
 
 def log(*a):
@@ -182,7 +200,7 @@ def run_reference(args):
 
 # iterations of the FP64-MG solve of this workload to 1e-8 (measured on the GPU
 # path, which runs the same algorithm as the oracle; used to scale CPU samples)
-REFERENCE_FP64_ITERATIONS = 400
+REFERENCE_FP64_ITERATIONS = 56
 
 
 def run_gpu(args):
@@ -308,24 +326,18 @@ def run_gpu(args):
              "stokes_vmult_fp32": n / ops["stokes_vmult_fp32"] / 1e9,
              "A_vmult_fp32": f.n_u / ops["A_vmult_fp32"] / 1e9,
              "A_vmult_fp64": f.n_u / ops["A_vmult_fp64"] / 1e9}
-    # share of the mixed solve: FP64 Stokes applications vs finest-level FP32 A-block
-    # applications (8 per A V-cycle on the finest level: 3 + 4 smoothing, 1 residual)
-    t_stokes64 = mixed["fp64_stokes_applications"] * ops["stokes_vmult_fp64"]
-    t_a32 = 8 * mixed["A_preconditioner_applications"] * ops["A_vmult_fp32"]
-    if t_stokes64 >= t_a32:
-        dom, t_dom, b_dom = "velocity_apply_kernel<double,3,STOKES>", ops["stokes_vmult_fp64"], \
-            algorithmic_bytes(P, "stokes", 8)
-    else:
-        dom, t_dom, b_dom = "velocity_apply_kernel<float,3,A>", ops["A_vmult_fp32"], algorithmic_bytes(P, "A", 4)
+    # --- roofline of the dominant kernel: the FP32 lattice cell pass of the
+    # velocity block (most launches of every V-cycle level; timed here on the
+    # finest level with CUDA events on the library's stream), and beside it the
+    # FP64 Stokes operator of the outer residual
+    t_cell = g.time_operation(gmg.TIME_A_CELL_PASS, gmg.FP32, 20)
+    eta_words = f.n_cells * (27 if P.projection == 1 else 1)
+    b_cell = 4 * (f.n_u + eta_words + 81 * f.n_cells)  # reads x and eta, writes 81 contributions per cell
     peak, peak_kind = peaks()
-    achieved = b_dom / t_dom / 1e9
-    traffic = None
-    try:
-        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as fh:
-            tr = json.load(fh).get(dom)
-            traffic = tr["bytes_per_application"] if tr else None
-    except Exception:
-        pass
+    achieved = b_cell / t_cell / 1e9
+    tflops_cell = FLOPS_A_CELL_F32 * f.n_cells / t_cell / 1e12
+    t_s64 = ops["stokes_vmult_fp64"]
+    tflops_s64 = FLOPS_STOKES_CELL_F64 * f.n_cells / t_s64 / 1e12
     clocks = clk.summary()
 
     if rank != 0:
@@ -345,9 +357,21 @@ def run_gpu(args):
                    "l2": "flushed between timed solves (256 MiB write)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "MDoF/s", "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": n * 8},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                     "algorithmic_bytes_per_application": b_dom, "seconds_per_application": t_dom},
+        "roofline": {"bound": "hbm", "kernel": "lattice_cell_kernel_f32<A> (FP32 velocity-block cell pass, "
+                                                "32^3 finest level)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": CELL_PASS_DRAM_BYTES,
+                     "algorithmic_bytes_per_launch": b_cell, "seconds_per_launch": t_cell,
+                     "fp32": {"achieved_tflops": tflops_cell, "peak_tflops": FP32_PEAK_TFLOPS,
+                              "frac": tflops_cell / FP32_PEAK_TFLOPS, "peak_kind": "nominal",
+                              "flops_per_cell": FLOPS_A_CELL_F32},
+                     "note": "one thread per cell, 32768 cells: a single partial wave bound by each "
+                             "thread's dependent arithmetic chain; the inputs are L2-resident within a solve"},
+        "roofline_fp64_stokes": {"bound": "fp64", "kernel": "velocity_cell_kernel<double,3,STOKES> + gathers "
+                                                            "(FP64 Stokes operator, 32^3)",
+                                 "seconds_per_application": t_s64, "achieved_tflops": tflops_s64,
+                                 "peak_tflops": FP64_PEAK_TFLOPS, "frac": tflops_s64 / FP64_PEAK_TFLOPS,
+                                 "peak_kind": "nominal", "flops_per_cell": FLOPS_STOKES_CELL_F64},
         "cpu_baseline": {"value": cpu["dofs_per_s"] / 1e6, "unit": "MDoF/s", "cores": os.cpu_count(), "kind": "port",
                          "sample": f"{cpu['iterations_sample']} GMRES iterations of the same 32^3 solve, FP64-MG "
                                    f"CPU oracle ({cpu['seconds_sample']:.1f} s), scaled to {its64} iterations"},
@@ -364,10 +388,31 @@ def run_gpu(args):
                          "speedup_vs_fp64_mg": t64 / tir},
             "velocity_rel_l2_vs_fp64_mg": {"mixed": rel(x32, x64), "gmres_ir": rel(xir, x64)},
             "operator_seconds": ops, "operator_gdofs": gdofs,
-            "solve_share_seconds": {"stokes_vmult_fp64": t_stokes64, "A_vmult_fp32_finest": t_a32},
+            "solve_share_seconds": {"stokes_vmult_fp64": mixed["fp64_stokes_applications"] * t_s64},
         },
     }
     print(json.dumps(line), flush=True)
+
+
+PROFILE_OPS = {"a_cell_pass_fp32": ("TIME_A_CELL_PASS", "FP32"), "a_vmult_fp32": ("TIME_A_VMULT", "FP32"),
+               "stokes_vmult_fp64": ("TIME_STOKES_VMULT", "FP64"), "mass_vmult_fp32": ("TIME_MASS_VMULT", "FP32")}
+
+
+def run_profile_op(name: str):
+    """One operation of the workload, three times inside cudaProfilerStart/Stop."""
+    import torch
+    from aspect_gb300 import gmg
+    torch.cuda.init()
+    P = build_problem()
+    g = gmg.from_problem(P)
+    what, prec = getattr(gmg, PROFILE_OPS[name][0]), getattr(gmg, PROFILE_OPS[name][1])
+    g.time_operation(what, prec, 3)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    sec = g.time_operation(what, prec, 3)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print(json.dumps({"profile_op": name, "seconds_per_call": sec, "cells": P.fine.n_cells}), flush=True)
 
 
 def main():
@@ -376,8 +421,11 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--profile-op", default=None, choices=sorted(PROFILE_OPS))
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_op:
+        run_profile_op(args.profile_op)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)
