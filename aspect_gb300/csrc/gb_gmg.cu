@@ -50,7 +50,7 @@ struct Handle {
   DevBuf<double> stage_a, stage_b, partial, dots_d;
   double* dots_h = nullptr;
   DevBuf<double> V, Z, wv, xv, rv, bv, tv, t2v, coef_d;
-  DevBuf<double> hcol_d, arn_d;  // Arnoldi column and scalars (|w|^2, |w| before) on the device
+  DevBuf<double> hcol_d, arn_d;  // Arnoldi column and scalars (|w|^2, |w| before, 1/|w|) on the device
   DevBuf<int> arn_flag;          // 1: the step needs its second Gram-Schmidt pass
   DevBuf<double> cg_r, cg_z, cg_p, cg_q, cg_x;
   DevBuf<float> f32_a, f32_b;
@@ -688,7 +688,7 @@ void ensure_krylov(Handle& H, int restart) {
   H.Z.alloc((size_t)restart * n);
   H.coef_d.alloc(restart + 2);
   H.hcol_d.alloc(restart + 2);
-  H.arn_d.alloc(2);
+  H.arn_d.alloc(3);
   H.arn_flag.alloc(1);
   if (H.dots_d.n < (size_t)restart + 2) {
     H.dots_d.alloc(restart + 2);
@@ -712,20 +712,20 @@ __global__ void k_cgs_coef(int j, int pass, const double* __restrict__ dots, dou
   }
   if (pass == 0 && threadIdx.x == 0) arn[1] = sqrt(dots[j + 1]);
 }
-// after w -= V coef and arn[0] = <w, w>: h[j+1] = |w|; pass 0 decides whether
-// the second pass runs (|w| <= 0.7 |w before|)
-__global__ void k_cgs_norm(int j, int pass, double* __restrict__ h, const double* __restrict__ arn,
+// after w -= V coef and arn[0] = <w, w>: h[j+1] = |w| and arn[2] = 1 / |w| (1
+// when |w| = 0); pass 0 decides whether the second pass runs (|w| <= 0.7 |w before|)
+__global__ void k_cgs_norm(int j, int pass, double* __restrict__ h, double* __restrict__ arn,
                            int* __restrict__ need2) {
   if (pass == 1 && *need2 == 0) return;
   const double nw = sqrt(arn[0]);
   h[j + 1] = nw;
+  arn[2] = 1.0 / (nw > 0 ? nw : 1.0);
   if (pass == 0) *need2 = nw > 0.7 * arn[1] ? 0 : 1;
 }
-// next basis vector v = w / h[j+1] (w itself when h[j+1] = 0)
-__global__ void k_next_basis(long n, const double* __restrict__ h, int j, const double* __restrict__ w,
+// next basis vector v = w / h[j+1] (the reciprocal is formed once, in k_cgs_norm)
+__global__ void k_next_basis(long n, const double* __restrict__ arn, const double* __restrict__ w,
                              double* __restrict__ v) {
-  const double hn = h[j + 1];
-  const double sc = 1.0 / (hn > 0 ? hn : 1.0);
+  const double sc = arn[2];
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     v[i] = sc * w[i];
 }
@@ -785,7 +785,7 @@ int gmres(Handle& H, double* x, const double* b, double tol, int maxit, int rest
       v_multiaxpy(n, j + 1, H.coef_d.p, V, n, w, H.st, need2);
       v_dot<double>(n, w, w, arn, H.partial.p, H.st, need2);
       k_cgs_norm<<<1, 1, 0, H.st>>>(j, 1, hcol, arn, need2);
-      k_next_basis<<<ceil_div(n, 256), 256, 0, H.st>>>(n, hcol, j, w, vnext);
+      k_next_basis<<<ceil_div(n, 256), 256, 0, H.st>>>(n, arn, w, vnext);
       VecCounter::launches() += 5;
       GB_CUDA(cudaMemcpyAsync(H.dots_h, hcol, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, H.st));
       GB_CUDA(cudaStreamSynchronize(H.st));
@@ -844,7 +844,10 @@ void ensure_workspace(Handle& H) {
   H.f32_b.alloc(n);
   H.vin.alloc(n);
   H.vout.alloc(n);
-  H.partial.alloc((kDotChunk + 1) * kDotBlocks);
+  if (H.partial.n != (size_t)kDotWorkspaceDoubles) {
+    H.partial.alloc(kDotWorkspaceDoubles);
+    H.partial.zero(H.st);  // the arrival counters start at zero
+  }
   H.dots_d.alloc(256);
   if (!H.dots_h) GB_CUDA(cudaMallocHost(&H.dots_h, 256 * sizeof(double)));
   if (!H.flag_d) GB_CUDA(cudaMalloc(&H.flag_d, sizeof(int)));

@@ -163,8 +163,12 @@ void v_spmv_add(long rows, const int* ptr, const int* col, const T* val, const T
 }
 
 // ---------------------------------------------------------------- reductions
+// Block sums of acc[0..K) into partial[i * slot_stride + blockIdx.x] for output
+// slots i < nk; slot i takes accumulator i, except that slot `moved` (when >= 0)
+// takes accumulator K-1 (so callers never index acc at run time).
 template <int K>
-__device__ __forceinline__ void block_reduce_store(double (&acc)[K], int nk, double* partial, int slot_stride) {
+__device__ __forceinline__ void block_reduce_store(double (&acc)[K], int nk, double* partial, int slot_stride,
+                                                   int moved = -1) {
   __shared__ double sh[K][kDotThreads / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -176,17 +180,56 @@ __device__ __forceinline__ void block_reduce_store(double (&acc)[K], int nk, dou
   }
   __syncthreads();
   if (threadIdx.x < nk) {
+    const int src = (int)threadIdx.x == moved ? K - 1 : (int)threadIdx.x;
     double t = 0;
-    for (int w = 0; w < kDotThreads / 32; ++w) t += sh[threadIdx.x][w];
+    for (int w = 0; w < kDotThreads / 32; ++w) t += sh[src][w];
     partial[threadIdx.x * slot_stride + blockIdx.x] = t;
   }
 }
 
+// The block of a reduction that arrives last (a counter per chunk, reset by
+// that block) sums the per-block partials itself, in the same fixed order a
+// separate finishing launch would: lane l of a warp adds blocks l, l+32, ...,
+// then lane 0 adds the 32 lane sums in lane order. Deterministic, one launch.
+__device__ __forceinline__ bool arrive_last(unsigned* counter) {
+  __shared__ bool last;
+  __threadfence();  // this block's partials are visible before its arrival counts
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+__device__ __forceinline__ void finish_partials(const double* part, int nk, double* out, unsigned* counter) {
+  __shared__ double sh[kDotThreads / 32][32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int j = wid; j < nk; j += kDotThreads / 32) {
+    double t = 0;
+    for (int b = lane; b < kDotBlocks; b += 32) t += __ldcg(part + (size_t)j * kDotBlocks + b);
+    sh[wid][lane] = t;
+    __syncwarp();
+    if (lane == 0) {
+      double v = 0;
+      for (int l = 0; l < 32; ++l) v += sh[wid][l];
+      out[j] = v;
+    }
+    __syncwarp();
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+// blockIdx.y = chunk of kDotChunk vectors; the chunk that ends at k also forms <w, w>
 __global__ void __launch_bounds__(kDotThreads) k_multidot(long n, const double* __restrict__ w,
                                                           const double* __restrict__ V, long ld, int k,
-                                                          int with_norm, double* __restrict__ partial,
+                                                          int with_norm, double* __restrict__ out,
+                                                          double* __restrict__ partial, unsigned* counters,
                                                           const int* __restrict__ active) {
   if (active && *active == 0) return;
+  const int chunk = blockIdx.y;
+  const int j0 = chunk * kDotChunk;
+  const int kk = k - j0 < kDotChunk ? k - j0 : kDotChunk;
+  const int norm = (with_norm && j0 + kk == k) ? 1 : 0;
+  const double* __restrict__ Vc = V + (size_t)j0 * ld;
   double acc[kDotChunk + 1];
 #pragma unroll
   for (int j = 0; j <= kDotChunk; ++j) acc[j] = 0;
@@ -194,62 +237,50 @@ __global__ void __launch_bounds__(kDotThreads) k_multidot(long n, const double* 
     const double wi = w[i];
 #pragma unroll
     for (int j = 0; j < kDotChunk; ++j)
-      if (j < k) acc[j] += wi * V[j * ld + i];
-    if (with_norm) acc[kDotChunk] += wi * wi;
+      if (j < kk) acc[j] += wi * Vc[j * ld + i];
+    if (norm) acc[kDotChunk] += wi * wi;
   }
-  if (with_norm) acc[k] = acc[kDotChunk];
-  block_reduce_store<kDotChunk + 1>(acc, k + with_norm, partial, kDotBlocks);
-}
-
-__global__ void k_finish(const double* __restrict__ partial, int nk, double* __restrict__ out,
-                         const int* __restrict__ active) {
-  if (active && *active == 0) return;
-  const int j = blockIdx.x;
-  if (j >= nk) return;
-  __shared__ double sh[32];
-  double t = 0;
-  for (int b = threadIdx.x; b < kDotBlocks; b += 32) t += partial[j * kDotBlocks + b];
-  sh[threadIdx.x] = t;
-  __syncwarp();
-  if (threadIdx.x == 0) {
-    double s = 0;
-    for (int l = 0; l < 32; ++l) s += sh[l];
-    out[j] = s;
-  }
+  double* part = partial + (size_t)chunk * (kDotChunk + 1) * kDotBlocks;
+  block_reduce_store<kDotChunk + 1>(acc, kk + norm, part, kDotBlocks, norm ? kk : -1);
+  if (arrive_last(counters + chunk)) finish_partials(part, kk + norm, out + j0, counters + chunk);
 }
 
 void v_multidot(long n, const double* w, const double* V, long ld, int k, bool with_norm, double* out_dev,
                 double* partial, cudaStream_t s, const int* active) {
+  unsigned* counters = reinterpret_cast<unsigned*>(partial + kDotPartialDoubles);
   if (k == 0) {
     if (!with_norm) return;
-    k_multidot<<<kDotBlocks, kDotThreads, 0, s>>>(n, w, V, ld, 0, 1, partial, active);
-    k_finish<<<1, 32, 0, s>>>(partial, 1, out_dev, active);
-    VecCounter::launches() += 2;
+    k_multidot<<<dim3(kDotBlocks, 1), kDotThreads, 0, s>>>(n, w, V, ld, 0, 1, out_dev, partial, counters, active);
+    VecCounter::launches() += 1;
     return;
   }
-  for (int done = 0; done < k; done += kDotChunk) {
-    const int kk = k - done < kDotChunk ? k - done : kDotChunk;
-    const int norm = (with_norm && done + kk == k) ? 1 : 0;
-    k_multidot<<<kDotBlocks, kDotThreads, 0, s>>>(n, w, V + done * ld, ld, kk, norm, partial, active);
-    k_finish<<<kk + norm, 32, 0, s>>>(partial, kk + norm, out_dev + done, active);
-    VecCounter::launches() += 2;
+  constexpr int per_launch = kDotMaxChunks * kDotChunk;
+  for (int done = 0; done < k; done += per_launch) {
+    const int kl = k - done < per_launch ? k - done : per_launch;
+    const int norm = (with_norm && done + kl == k) ? 1 : 0;
+    const int chunks = (kl + kDotChunk - 1) / kDotChunk;
+    k_multidot<<<dim3(kDotBlocks, chunks), kDotThreads, 0, s>>>(n, w, V + (size_t)done * ld, ld, kl, norm,
+                                                                out_dev + done, partial, counters, active);
+    VecCounter::launches() += 1;
   }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kDotThreads) k_dot(long n, const T* __restrict__ a, const T* __restrict__ b,
-                                                     double* __restrict__ partial, const int* __restrict__ active) {
+                                                     double* __restrict__ out, double* __restrict__ partial,
+                                                     unsigned* counter, const int* __restrict__ active) {
   if (active && *active == 0) return;
   double acc[1] = {0};
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     acc[0] += (double)a[i] * (double)b[i];
   block_reduce_store<1>(acc, 1, partial, kDotBlocks);
+  if (arrive_last(counter)) finish_partials(partial, 1, out, counter);
 }
 template <typename T>
 void v_dot(long n, const T* a, const T* b, double* out_dev, double* partial, cudaStream_t s, const int* active) {
-  k_dot<T><<<kDotBlocks, kDotThreads, 0, s>>>(n, a, b, partial, active);
-  k_finish<<<1, 32, 0, s>>>(partial, 1, out_dev, active);
-  VecCounter::launches() += 2;
+  unsigned* counter = reinterpret_cast<unsigned*>(partial + kDotPartialDoubles) + kDotMaxChunks;
+  k_dot<T><<<kDotBlocks, kDotThreads, 0, s>>>(n, a, b, out_dev, partial, counter, active);
+  VecCounter::launches() += 1;
 }
 
 __global__ void k_multiaxpy(long n, int k, const double* __restrict__ coef, const double* __restrict__ V, long ld,

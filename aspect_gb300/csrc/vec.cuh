@@ -8,7 +8,14 @@ namespace gb {
 // summed in a fixed order, so every dot product is bit-reproducible.
 constexpr int kDotBlocks = 304;  // 2 x 152 SMs
 constexpr int kDotThreads = 256;
-constexpr int kDotChunk = 8;     // vectors per multi-dot launch
+constexpr int kDotChunk = 8;     // vectors per multi-dot block
+constexpr int kDotMaxChunks = 16;  // chunks per multi-dot launch (128 vectors)
+// reduction workspace: per-block partials, then the arrival counters (kDotMaxChunks
+// for the multi-dot chunks and one for dots) in the following kDotCounterDoubles;
+// allocate kDotWorkspaceDoubles and zero it once
+constexpr long kDotPartialDoubles = (long)kDotMaxChunks * (kDotChunk + 1) * kDotBlocks;
+constexpr long kDotCounterDoubles = kDotMaxChunks + 1;
+constexpr long kDotWorkspaceDoubles = kDotPartialDoubles + kDotCounterDoubles;
 
 struct VecCounter {
   static long long& launches() {
@@ -51,7 +58,7 @@ void v_spmv_add(long rows, const int* ptr, const int* col, const T* val, const T
 // it points to 0 the launches return at once (a step that the device decided to
 // skip without a round trip to the host).
 // out[j] = <w, V_j> for j < k (V rows of stride ld), plus out[k] = <w, w> if with_norm
-// partial: workspace of (kDotChunk+1) * kDotBlocks doubles
+// partial: the reduction workspace (kDotWorkspaceDoubles, zeroed once)
 void v_multidot(long n, const double* w, const double* V, long ld, int k, bool with_norm, double* out_dev,
                 double* partial, cudaStream_t s, const int* active = nullptr);
 template <typename T>

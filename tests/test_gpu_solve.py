@@ -75,3 +75,15 @@ def test_no_convergence_is_reported():
     g = gmg.from_problem(P)
     with pytest.raises(gmg.NoConvergence):
         g.solve(P.rhs, absolute_tolerance=1e-300, n_cheap_steps=5, n_expensive_steps=3)
+
+
+def test_solve_is_bit_reproducible():
+    """Every reduction has a fixed summation order (the last-arriving block of a
+    reduction sums the per-block partials in block order), so repeated mixed-
+    precision solves give bit-identical solutions and iteration counts."""
+    P = problems.sinkers_3d(8)
+    g = gmg.from_problem(P)
+    x1, o1 = g.solve(P.rhs, linear_solver_tolerance=1e-8, mg_precision=gmg.FP32)
+    x2, o2 = g.solve(P.rhs, linear_solver_tolerance=1e-8, mg_precision=gmg.FP32)
+    assert o1["cheap_iterations"] == o2["cheap_iterations"]
+    assert np.array_equal(x1, x2)
