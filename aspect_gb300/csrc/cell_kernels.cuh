@@ -845,6 +845,66 @@ __global__ void __launch_bounds__(256) velocity_gather_structured(LevelView<T> L
   gather_epilogue<T, epi>(a, g, sum, constrained);
 }
 
+// Velocity DoFs of a 3D lattice level, one thread per Q2 node for all three
+// components: the node's (at most 2 per direction) cells and local positions
+// are found once and the 3 x 8 candidate contributions are predicated loads in
+// registers (no run-time indexed arrays, so no local memory). Candidates are
+// summed in the same order as velocity_gather_structured (z, y, x; the lower
+// cell along a direction first), so the two give bit-identical sums.
+template <typename T, int epi>
+__global__ void __launch_bounds__(256) velocity_gather_lattice3(LevelView<T> L, GatherArgs<T> a) {
+  const int node = blockIdx.x * blockDim.x + threadIdx.x;
+  if (node >= L.n_nodes) return;
+  const int nxy = L.Nn[0] * L.Nn[1];
+  const int gz = node / nxy;
+  const int rem = node - gz * nxy;
+  const int gy = rem / L.Nn[0];
+  const int gx = rem - gy * L.Nn[0];
+  const int g3[3] = {gx, gy, gz};
+  // per direction: candidate 0 (lower cell / the cell of an odd node) and 1 (upper cell)
+  int c0[3], l0[3], c1[3], l1[3];
+  bool v0[3], v1[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const int x = g3[d];
+    if (x & 1) {
+      c0[d] = (x - 1) >> 1; l0[d] = 1; v0[d] = true;
+      c1[d] = 0; l1[d] = 0; v1[d] = false;
+    } else {
+      c0[d] = (x >> 1) - 1; l0[d] = 2; v0[d] = x > 0;
+      c1[d] = x >> 1; l1[d] = 0; v1[d] = x < L.Nn[d] - 1;
+    }
+  }
+  bool cons[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    bool z = false;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (g3[d] == 0 && ((L.zero_faces >> ((2 * d) * 3 + c)) & 1u)) z = true;
+      if (g3[d] == L.Nn[d] - 1 && ((L.zero_faces >> ((2 * d + 1) * 3 + c)) & 1u)) z = true;
+    }
+    cons[c] = z;
+  }
+  T sum[3] = {T(0), T(0), T(0)};
+#pragma unroll
+  for (int kz = 0; kz < 2; ++kz)
+#pragma unroll
+    for (int ky = 0; ky < 2; ++ky)
+#pragma unroll
+      for (int kx = 0; kx < 2; ++kx) {
+        const bool ok = (kz ? v1[2] : v0[2]) && (ky ? v1[1] : v0[1]) && (kx ? v1[0] : v0[0]);
+        if (!ok) continue;
+        const int cell = ((kz ? c1[2] : c0[2]) * L.nc[1] + (ky ? c1[1] : c0[1])) * L.nc[0] + (kx ? c1[0] : c0[0]);
+        const int l = (kx ? l1[0] : l0[0]) + 3 * (ky ? l1[1] : l0[1]) + 9 * (kz ? l1[2] : l0[2]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          if (!cons[c]) sum[c] += a.E[(size_t)cell * a.cs + (size_t)(c * 27 + l) * a.ss];
+      }
+#pragma unroll
+  for (int c = 0; c < 3; ++c) gather_epilogue<T, epi>(a, (long)c * L.n_nodes + node, sum[c], cons[c]);
+}
+
 // Pressure DoFs of a lattice level (never constrained there).
 template <typename T, int dim, int epi>
 __global__ void __launch_bounds__(256) pressure_gather_structured(LevelView<T> L, GatherArgs<T> a) {

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -551,10 +552,27 @@ void vcycle_T(Handle& H, int block, const double* src, double* dst) {
 // Chebyshev coefficients are known once the eigenvalues are), so it is captured
 // once into a CUDA graph and replayed; the FP64 input and output go through
 // staging vectors whose addresses are baked into the graph.
+//
+// GB_GMG_VCYCLE_GRAPHS=0 in the environment (read once per process) issues the
+// same launch sequence directly on the stream instead, so that profilers that
+// replay kernels one at a time see ordinary launches.
+bool vcycle_graphs_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("GB_GMG_VCYCLE_GRAPHS");
+    return !(e && std::strcmp(e, "0") == 0);
+  }();
+  return on;
+}
+
 void vcycle_exec(Handle& H, int block, int prec, const double* src, double* dst) {
   const int pi = prec == GB_GMG_FP32 ? 1 : 0;
   Level& F = H.top();
   const long n = block == 0 ? F.n_u : F.n_p;
+  if (!vcycle_graphs_enabled()) {
+    if (pi) vcycle_T<float>(H, block, src, dst);
+    else vcycle_T<double>(H, block, src, dst);
+    return;
+  }
   if (!H.vgraph[block][pi]) {
     const long long c0 = H.cell_launches, v0 = VecCounter::launches();
     cudaGraph_t graph = nullptr;

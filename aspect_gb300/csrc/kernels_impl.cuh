@@ -36,6 +36,8 @@ void gather_dim_epi(const LevelView<GB_T>& L, int block, const GatherCsr<GB_T>* 
   const long n = block == 0 ? L.n_u : L.n_p;
   const int g = ceil_div(n, kGatherThreads);
   if (csr) gather_csr<GB_T, epi><<<g, kGatherThreads, 0, s>>>(n, *csr, a);
+  else if (block == 0 && dim == 3)
+    velocity_gather_lattice3<GB_T, epi><<<ceil_div(L.n_nodes, kGatherThreads), kGatherThreads, 0, s>>>(L, a);
   else if (block == 0) velocity_gather_structured<GB_T, dim, epi><<<g, kGatherThreads, 0, s>>>(L, a);
   else pressure_gather_structured<GB_T, dim, epi><<<g, kGatherThreads, 0, s>>>(L, a);
 }

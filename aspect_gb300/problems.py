@@ -284,22 +284,46 @@ def real_spherical_harmonics_field(x: np.ndarray, max_degree: int, seed: int) ->
 
 def spherical_shell(n_refinements: int = 3, Ra: float = 1e5, contrast: float = 1e4,
                     amplitude: float = 0.01, max_degree: int = 8, seed: int = BASE_SEED + 3,
-                    r_in: float = 0.55, r_out: float = 1.0) -> StokesProblem:
+                    r_in: float = 0.55, r_out: float = 1.0, n_adaptive: int = 0,
+                    refinement_fraction: float = 0.3) -> StokesProblem:
     """Spherical shell r in [0.55, 1], the 96-cell cube-sphere refined n times,
     T = conductive profile + amplitude sin(pi (r-r_in)/(r_out-r_in)) Y(theta, phi)
     with Y a seeded real spherical-harmonic field of degree <= 8, eta =
     exp(-ln(contrast) T) per quadrature point (Q1 projection), buoyancy
-    Ra T r_hat, free slip on both spheres (rotation null space)."""
+    Ra T r_hat, free slip on both spheres (rotation null space).
+
+    n_adaptive rounds of refinement on the temperature gradient follow the global
+    ones: cell indicator |grad T(centre)| sqrt(|K|) (an L2 norm of grad T over the
+    cell at one point), the cells holding `refinement_fraction` of the indicator
+    sum refined (ASPECT's default fixed-fraction strategy with fraction 0.3);
+    hanging nodes on the coarse/fine interfaces."""
     from . import shell
-    levels = shell.hierarchy(n_refinements, 4, r_in, r_out)
-    fine = levels[-1]
-    xq, jxw = q_points_real(fine)
-    r = np.linalg.norm(xq, axis=-1)
 
     def temperature(x, r):
         t = (1 / r - 1 / r_out) / (1 / r_in - 1 / r_out)
         env = np.sin(np.pi * (r - r_in) / (r_out - r_in))
         return t + amplitude * env * real_spherical_harmonics_field(x, max_degree, seed)
+
+    if n_adaptive == 0:
+        levels = shell.hierarchy(n_refinements, 4, r_in, r_out)
+    else:
+        cells = shell.all_cells(4, n_refinements)
+        for _ in range(n_adaptive):
+            arr = np.array(cells, dtype=np.int64)
+            xc = shell.cell_centres(cells, 4, r_in, r_out)
+            rc = np.linalg.norm(xc, axis=-1)
+            hgt = 1e-6
+            st = np.concatenate([xc[None]] + [xc[None] + s * hgt * np.eye(3)[e] for e in range(3) for s in (1, -1)])
+            Ts = temperature(st.reshape(-1, 3), np.linalg.norm(st.reshape(-1, 3), axis=-1)).reshape(7, -1)
+            grad = np.stack([(Ts[1 + 2 * e] - Ts[2 + 2 * e]) / (2 * hgt) for e in range(3)], -1)
+            d = arr[:, 1]
+            vol = rc ** 2 * (1.0 / (4 * (1 << d))) ** 2 * ((r_out - r_in) / (1 << d))
+            cells = shell.refine_fixed_fraction(cells, np.linalg.norm(grad, axis=-1) * np.sqrt(vol),
+                                                refinement_fraction)
+        levels = shell.adaptive_hierarchy(cells, 4, r_in, r_out)
+    fine = levels[-1]
+    xq, jxw = q_points_real(fine)
+    r = np.linalg.norm(xq, axis=-1)
 
     T = temperature(xq, r)
     eta = np.exp(-math.log(contrast) * T)
@@ -309,5 +333,5 @@ def spherical_shell(n_refinements: int = 3, Ra: float = 1e5, contrast: float = 1
     rm = np.linalg.norm(mid, axis=-1)
     length = 1e4 / (6336000.0 - 3481000.0) * (r_out - r_in)
     s = pressure_scaling(fine, np.exp(-math.log(contrast) * temperature(mid, rm)), length)
-    return StokesProblem(f"spherical_shell_ref{n_refinements}", levels, eta, 1, s, rhs, -1,
-                         extra=dict(temperature_q=T))
+    name = f"spherical_shell_ref{n_refinements}" + (f"+{n_adaptive}" if n_adaptive else "")
+    return StokesProblem(name, levels, eta, 1, s, rhs, -1, extra=dict(temperature_q=T))

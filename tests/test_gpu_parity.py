@@ -142,3 +142,25 @@ def test_vmult_is_bit_reproducible():
     a = g.vmult(0, len(levels) - 1, x)
     b = g.vmult(0, len(levels) - 1, x)
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("per_q,comp", [(False, 0), (True, 0), (True, 1)])
+def test_fp32_a_block_on_large_lattice_level(per_q, comp):
+    """16^3 box (4,096 cells on the finest level, above the small-level kernel's
+    512): the FP32 A-block cell pass of large lattice levels against the oracle,
+    with cellwise and per-point viscosity, incompressible and compressible, and
+    the free-slip constraints of all six walls."""
+    levels = hierarchy(3, 16)
+    eta = random_eta(levels[-1], per_q)
+    g = gmg.StokesMatrixFreeGPU(3, len(levels))
+    g.setup_dofs(levels)
+    g.assemble(eta, 0, 2.5, comp)
+    o = Oracle(levels)
+    o.set_viscosity(eta, 0, 2.5, comp)
+    rng = np.random.default_rng(31)
+    top = len(levels) - 1
+    for _ in range(2):
+        x = rng.normal(size=levels[-1].n_u)
+        y_ref = o.vmult(1, top, x)
+        assert rel_err(g.vmult(1, top, x, gmg.FP32), y_ref) < TOL32 * 10
+        assert rel_err(g.vmult(1, top, x, gmg.FP64), y_ref) < TOL64

@@ -126,3 +126,55 @@ def test_shell_solve_dense_coarse(n_ref):
     u32 = _remove_rotations(f, x32[: f.n_u])
     u64 = _remove_rotations(f, x64[: f.n_u])
     assert rel_err(u32, u64) < 1e-5
+
+
+@pytest.fixture(scope="module")
+def adaptive_pair():
+    """Shell refined once globally plus one round on the temperature gradient:
+    curved cells of two depths, hanging-node lines (Q2 velocity, Q1 pressure)
+    across patch boundaries, no-normal-flux lines on hanging boundary nodes, and
+    transfers with cells that are their own parent."""
+    P = problems.spherical_shell(1, n_adaptive=1)
+    levels = P.levels
+    f = levels[-1]
+    rng = np.random.default_rng(6)
+    eta = np.exp(rng.uniform(-2, 2, size=(f.n_cells, 27)))
+    g = gmg.StokesMatrixFreeGPU(3, len(levels))
+    g.setup_dofs(levels)
+    g.assemble(eta, 0, 2.0)
+    o = Oracle(levels)
+    o.set_viscosity(eta, 0, 2.0)
+    return levels, g, o
+
+
+def test_adaptive_shell_parity(adaptive_pair):
+    levels, g, o = adaptive_pair
+    assert levels[-1].constraints_p.n_lines > 0
+    test_shell_parity(adaptive_pair)
+    f = levels[-1]
+    rng = np.random.default_rng(2)
+    xc = rng.normal(size=levels[-2].n_u)
+    assert rel_err(g.transfer(len(levels) - 1, 0, False, xc), o.transfer(len(levels) - 1, 0, False, xc)) < 1e-13
+    xp = rng.normal(size=f.n_p)
+    assert rel_err(g.transfer(len(levels) - 1, 1, True, xp), o.transfer(len(levels) - 1, 1, True, xp)) < 1e-13
+
+
+def test_adaptive_shell_solve_dense_coarse():
+    """The shell workload's adaptive form at reduced size (refinement 2 plus one
+    round on the temperature gradient), FP64 dense coarse solve, mixed and FP64
+    precision; residuals checked by the oracle in FP64. With hanging nodes the
+    rigid rotations are no longer exact null vectors (the fine nodes lie on the
+    spheres, the coarse faces are Q2 interpolants), so velocities are compared
+    after removing them."""
+    P = problems.spherical_shell(2, n_adaptive=1)
+    g = gmg.from_problem(P, options={"coarse_solver": gmg.COARSE_DENSE_FP64})
+    x32, o32 = g.solve(P.rhs, linear_solver_tolerance=1e-8, mg_precision=gmg.FP32)
+    x64, o64 = g.solve(P.rhs, linear_solver_tolerance=1e-8, mg_precision=gmg.FP64)
+    assert o32["status"] == 0 and o64["status"] == 0, (o32, o64)
+    o = Oracle(P.levels)
+    o.set_viscosity(P.eta, P.projection, P.pressure_scaling)
+    top = len(P.levels) - 1
+    for x, out in ((x32, o32), (x64, o64)):
+        assert np.linalg.norm(P.rhs - o.vmult(0, top, x)) <= 1.01 * out["solver_tolerance"]
+    f = P.fine
+    assert rel_err(_remove_rotations(f, x32[: f.n_u]), _remove_rotations(f, x64[: f.n_u])) < 1e-4
