@@ -14,6 +14,7 @@ __global__ void __launch_bounds__(128) adjoint_gradient_kernel(LevelView<double>
                                                                 int colour_count, const double* __restrict__ u,
                                                                 const double* __restrict__ lam,
                                                                 double* __restrict__ grad) {
+  pdl_wait();
   using T = double;
   constexpr int nv = Shape<dim>::nv, cpw = Shape<dim>::cpw;
   const unsigned full = 0xffffffffu;

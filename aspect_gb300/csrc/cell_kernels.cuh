@@ -391,6 +391,7 @@ template <typename T, int dim, int op>
 __global__ void __launch_bounds__(128) velocity_cell_kernel(LevelView<T> L, const T* __restrict__ src_u,
                                                              const T* __restrict__ src_p, T* __restrict__ Eu,
                                                              T* __restrict__ Ep) {
+  pdl_wait();
   constexpr int nv = Shape<dim>::nv, np = Shape<dim>::np, cpw = Shape<dim>::cpw;
   constexpr bool need_u = (op == OPK_STOKES || op == OPK_A);
   constexpr bool need_p = (op == OPK_STOKES || op == OPK_BT);
@@ -506,6 +507,7 @@ template <int op, bool eta_per_q>
 __global__ void __launch_bounds__(128) lattice_cell_kernel_f32(LevelView<float> L, const float* __restrict__ src_u,
                                                                 const float* __restrict__ src_p,
                                                                 float* __restrict__ Eu, float* __restrict__ Ep) {
+  pdl_wait();
   constexpr bool need_u = (op == OPK_STOKES || op == OPK_A);
   constexpr bool need_p = (op == OPK_STOKES || op == OPK_BT);
   using T = float;
@@ -640,6 +642,7 @@ template <bool eta_per_q>
 __global__ void __launch_bounds__(kSmallCellThreads) lattice_cell_kernel_small(LevelView<float> L,
                                                                                const float* __restrict__ src_u,
                                                                                float* __restrict__ Eu) {
+  pdl_wait();
   __shared__ float A[2][81];   // nodal / Gauss-point values, ping-pong between sweeps
   __shared__ float G[9][27];   // G[c*3+d][q] = d u_c / d x_d, then the fluxes R in place
   const SmallLatticeTables& K = c_small_tables;
@@ -734,6 +737,7 @@ __global__ void __launch_bounds__(kSmallCellThreads) lattice_cell_kernel_small(L
 template <typename T, int dim>
 __global__ void __launch_bounds__(128) mass_cell_kernel(LevelView<T> L, const T* __restrict__ src_p,
                                                          T* __restrict__ Ep) {
+  pdl_wait();
   constexpr int np = Shape<dim>::np;
   const int cell = blockIdx.x * blockDim.x + threadIdx.x;
   if (cell >= L.n_cells) return;
@@ -810,6 +814,7 @@ __device__ __forceinline__ void gather_epilogue(const GatherArgs<T>& a, long g, 
 // Velocity DoFs of a lattice level: a node's cells follow from its coordinates.
 template <typename T, int dim, int epi>
 __global__ void __launch_bounds__(256) velocity_gather_structured(LevelView<T> L, GatherArgs<T> a) {
+  pdl_wait();
   constexpr int nv = Shape<dim>::nv;
   const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (g >= L.n_u) return;
@@ -853,6 +858,7 @@ __global__ void __launch_bounds__(256) velocity_gather_structured(LevelView<T> L
 // cell along a direction first), so the two give bit-identical sums.
 template <typename T, int epi>
 __global__ void __launch_bounds__(256) velocity_gather_lattice3(LevelView<T> L, GatherArgs<T> a) {
+  pdl_wait();
   const int node = blockIdx.x * blockDim.x + threadIdx.x;
   if (node >= L.n_nodes) return;
   const int nxy = L.Nn[0] * L.Nn[1];
@@ -908,6 +914,7 @@ __global__ void __launch_bounds__(256) velocity_gather_lattice3(LevelView<T> L, 
 // Pressure DoFs of a lattice level (never constrained there).
 template <typename T, int dim, int epi>
 __global__ void __launch_bounds__(256) pressure_gather_structured(LevelView<T> L, GatherArgs<T> a) {
+  pdl_wait();
   constexpr int np = Shape<dim>::np;
   const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (g >= L.n_p) return;
@@ -1006,11 +1013,13 @@ __device__ __forceinline__ void mass_lattice_task(const LevelView<T>& L, const T
 template <typename T, int dim, int epi>
 __global__ void __launch_bounds__(kMassLatticeThreads) mass_apply_lattice(LevelView<T> L, const T* __restrict__ Mc,
                                                                           GatherArgs<T> a) {
+  pdl_wait();
   mass_lattice_task<T, dim, epi>(L, Mc, a, blockIdx.x * (long)blockDim.x + threadIdx.x);
 }
 
 template <typename T, int epi>
 __global__ void __launch_bounds__(256) gather_csr(long n, GatherCsr<T> G, GatherArgs<T> a) {
+  pdl_wait();
   const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (g >= n) return;
   const bool constrained = G.cmask[g] != 0;
@@ -1032,6 +1041,7 @@ __global__ void __launch_bounds__(128) velocity_diag_kernel(LevelView<T> L, int 
                                                              const int* __restrict__ probe_eptr,
                                                              const int* __restrict__ probe_li,
                                                              const T* __restrict__ probe_w, T* __restrict__ diag) {
+  pdl_wait();
   constexpr int nv = Shape<dim>::nv, cpw = Shape<dim>::cpw;
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1118,6 +1128,7 @@ __global__ void __launch_bounds__(128) mass_diag_kernel(LevelView<T> L, int colo
                                                          const int* __restrict__ probe_eptr,
                                                          const int* __restrict__ probe_li,
                                                          const T* __restrict__ probe_w, T* __restrict__ diag) {
+  pdl_wait();
   constexpr int np = Shape<dim>::np;
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= colour_count) return;

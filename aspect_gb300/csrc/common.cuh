@@ -80,4 +80,12 @@ struct DevBuf {
 
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
 
+// Every kernel of the library starts with this wait. Inside the captured
+// V-cycle graphs consecutive kernels are joined by programmatic edges, so a
+// kernel's blocks may be resident before its predecessor has finished; the
+// wait returns once every predecessor grid has completed and its memory
+// operations are visible. Launched any other way (no programmatic edge) it
+// returns at once.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 }  // namespace gb

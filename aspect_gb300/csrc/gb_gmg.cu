@@ -523,10 +523,10 @@ void vcycle_level(Handle& H, int lev, int block) {
   const long nc = block == 0 ? C.n_u : C.n_p;
   smoother_apply<T>(H, lev, block, sol, def);
   level_op_resid<T>(H, lev, block, sol, def, t);
-  GB_CUDA(cudaMemsetAsync(cdef, 0, nc * sizeof(T), H.st));
+  v_zero<T>(nc, cdef, H.st);
   if (block == 0) v_spmv_add<T>(L.PuT_rows, L.PuT_ptr.p, L.PuT_col.p, D.PuT_val.p, t, cdef, H.st);
   else v_spmv_add<T>(L.PpT_rows, L.PpT_ptr.p, L.PpT_col.p, D.PpT_val.p, t, cdef, H.st);
-  GB_CUDA(cudaMemsetAsync(csol, 0, nc * sizeof(T), H.st));
+  v_zero<T>(nc, csol, H.st);
   vcycle_level<T>(H, lev - 1, block);
   if (block == 0) v_spmv_add<T>(L.Pu_rows, L.Pu_ptr.p, L.Pu_col.p, D.Pu_val.p, csol, sol, H.st);
   else v_spmv_add<T>(L.Pp_rows, L.Pp_ptr.p, L.Pp_col.p, D.Pp_val.p, csol, sol, H.st);
@@ -564,6 +564,33 @@ bool vcycle_graphs_enabled() {
   return on;
 }
 
+// Turns every kernel -> kernel edge of a captured graph into a programmatic
+// dependency on the launch completion of the upstream kernel: the downstream
+// kernel may be scheduled once all blocks of its predecessor have started, and
+// its blocks wait in pdl_wait() until the predecessor has finished. This hides
+// the launch latency between the ~100 short kernels of a V-cycle; the order and
+// the arithmetic are unchanged.
+void programmatic_kernel_edges(cudaGraph_t g) {
+  size_t ne = 0;
+  GB_CUDA(cudaGraphGetEdges(g, nullptr, nullptr, nullptr, &ne));
+  if (!ne) return;
+  std::vector<cudaGraphNode_t> from(ne), to(ne);
+  std::vector<cudaGraphEdgeData> data(ne);
+  GB_CUDA(cudaGraphGetEdges(g, from.data(), to.data(), data.data(), &ne));
+  for (size_t i = 0; i < ne; ++i) {
+    cudaGraphNodeType tf, tt;
+    GB_CUDA(cudaGraphNodeGetType(from[i], &tf));
+    GB_CUDA(cudaGraphNodeGetType(to[i], &tt));
+    if (tf != cudaGraphNodeTypeKernel || tt != cudaGraphNodeTypeKernel) continue;
+    if (data[i].type != cudaGraphDependencyTypeDefault || data[i].from_port != cudaGraphKernelNodePortDefault) continue;
+    GB_CUDA(cudaGraphRemoveDependencies(g, &from[i], &to[i], &data[i], 1));
+    cudaGraphEdgeData e{};
+    e.from_port = cudaGraphKernelNodePortLaunchCompletion;
+    e.type = cudaGraphDependencyTypeProgrammatic;
+    GB_CUDA(cudaGraphAddDependencies(g, &from[i], &to[i], &e, 1));
+  }
+}
+
 void vcycle_exec(Handle& H, int block, int prec, const double* src, double* dst) {
   const int pi = prec == GB_GMG_FP32 ? 1 : 0;
   Level& F = H.top();
@@ -586,6 +613,7 @@ void vcycle_exec(Handle& H, int block, int prec, const double* src, double* dst)
       throw;
     }
     GB_CUDA(cudaStreamEndCapture(H.st, &graph));
+    programmatic_kernel_edges(graph);
     GB_CUDA(cudaGraphInstantiate(&H.vgraph[block][pi], graph, 0));
     size_t nn = 0;
     GB_CUDA(cudaGraphGetNodes(graph, nullptr, &nn));
@@ -722,6 +750,7 @@ void ensure_krylov(Handle& H, int restart) {
 // pass 1 (only while *need2): h += dots, coef = -dots.
 __global__ void k_cgs_coef(int j, int pass, const double* __restrict__ dots, double* __restrict__ h,
                            double* __restrict__ coef, double* __restrict__ arn, const int* __restrict__ need2) {
+  pdl_wait();
   if (pass == 1 && *need2 == 0) return;
   for (int i = threadIdx.x; i <= j; i += blockDim.x) {
     const double v = dots[i];
@@ -734,6 +763,7 @@ __global__ void k_cgs_coef(int j, int pass, const double* __restrict__ dots, dou
 // when |w| = 0); pass 0 decides whether the second pass runs (|w| <= 0.7 |w before|)
 __global__ void k_cgs_norm(int j, int pass, double* __restrict__ h, double* __restrict__ arn,
                            int* __restrict__ need2) {
+  pdl_wait();
   if (pass == 1 && *need2 == 0) return;
   const double nw = sqrt(arn[0]);
   h[j + 1] = nw;
@@ -743,6 +773,7 @@ __global__ void k_cgs_norm(int j, int pass, double* __restrict__ h, double* __re
 // next basis vector v = w / h[j+1] (the reciprocal is formed once, in k_cgs_norm)
 __global__ void k_next_basis(long n, const double* __restrict__ arn, const double* __restrict__ w,
                              double* __restrict__ v) {
+  pdl_wait();
   const double sc = arn[2];
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     v[i] = sc * w[i];
@@ -879,6 +910,7 @@ void alloc_level_work(Level& L, cudaStream_t st) {
 }
 
 __global__ void k_symmetrize(long n, double* M) {
+  pdl_wait();
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n * n) return;
   const long r = i % n, c = i / n;
@@ -889,6 +921,7 @@ __global__ void k_symmetrize(long n, double* M) {
   }
 }
 __global__ void k_scale_columns(long n, const double* V, const double* sc, double* U) {
+  pdl_wait();
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= n * n) return;
   U[i] = V[i] * sc[i / n];
@@ -1570,7 +1603,7 @@ int gb_gmg_time_operation(gb_gmg* g, int what, int precision, int repeats, doubl
   ABI_TRY(g, {
     Handle& H = g->h;
     const int pi = precision == GB_GMG_FP32 ? 1 : 0;
-    GB_CHECK(what >= 0 && what <= 6, 1, "unknown operation");
+    GB_CHECK(what >= 0 && what <= 7, 1, "unknown operation");
     if (what >= 3 && what <= 5) GB_CHECK(H.prec_done[pi], GB_GMG_NOT_READY, "build_preconditioner has not been called");
     else GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
     const int top = H.n_levels - 1;
@@ -1614,6 +1647,18 @@ int gb_gmg_time_operation(gb_gmg* g, int what, int precision, int repeats, doubl
             gb::LevelDev<double>& D = F.f64;
             gb::launch_cell_pass<double>(F.view<double>(H.s, H.compressible), gb::OPK_A, a, nullptr, D.Eu.p, D.Ep.p,
                                          H.st);
+          }
+          break;
+        }
+        case 7: {
+          if (pi) {
+            gb::LevelDev<float>& D = F.f32;
+            gb::launch_cell_pass<float>(F.view<float>(H.s, H.compressible), gb::OPK_STOKES, H.f32_a.p,
+                                        H.f32_a.p + nu, D.Eu.p, D.Ep.p, H.st);
+          } else {
+            gb::LevelDev<double>& D = F.f64;
+            gb::launch_cell_pass<double>(F.view<double>(H.s, H.compressible), gb::OPK_STOKES, a, a + nu, D.Eu.p,
+                                         D.Ep.p, H.st);
           }
           break;
         }

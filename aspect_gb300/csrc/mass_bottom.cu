@@ -86,6 +86,7 @@ __device__ void bottom_zero(int n, float* y) {
 }
 
 __global__ void __launch_bounds__(kBottomThreads) mass_vcycle_bottom(const MassBottomArgs args) {
+  pdl_wait();
   // levels are indexed at run time: keep the arguments in shared memory rather
   // than a per-thread local copy of the parameter block
   __shared__ MassBottomArgs A;

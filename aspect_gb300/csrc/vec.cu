@@ -16,6 +16,7 @@ inline void count() { ++VecCounter::launches(); }
 
 template <typename T>
 __global__ void k_axpby(long n, T a, const T* __restrict__ x, T b, T* __restrict__ y) {
+  pdl_wait();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     y[i] = a * x[i] + b * y[i];
 }
@@ -34,6 +35,7 @@ void v_copy(long n, const T* x, T* y, cudaStream_t s) {
 
 template <typename T>
 __global__ void k_scale(long n, T a, T* __restrict__ y) {
+  pdl_wait();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) y[i] *= a;
 }
 template <typename T>
@@ -43,8 +45,21 @@ void v_scale(long n, T a, T* y, cudaStream_t s) {
   count();
 }
 
+template <typename T>
+__global__ void k_zero(long n, T* __restrict__ y) {
+  pdl_wait();
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) y[i] = T(0);
+}
+template <typename T>
+void v_zero(long n, T* y, cudaStream_t s) {
+  if (n <= 0) return;
+  k_zero<<<grid_for(n), kThreads, 0, s>>>(n, y);
+  count();
+}
+
 template <typename Ts, typename Td>
 __global__ void k_cast(long n, const Ts* __restrict__ x, Td* __restrict__ y) {
+  pdl_wait();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     y[i] = (Td)x[i];
 }
@@ -58,6 +73,7 @@ void v_cast(long n, const Ts* x, Td* y, cudaStream_t s) {
 template <typename T>
 __global__ void k_cheb_first(long n, const T* __restrict__ b, const T* __restrict__ dinv, T f2, T* __restrict__ d,
                              T* __restrict__ x) {
+  pdl_wait();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const T v = f2 * dinv[i] * b[i];
     d[i] = v;
@@ -74,6 +90,7 @@ void v_cheb_first(long n, const T* b, const T* dinv, T f2, T* d, T* x, cudaStrea
 template <typename T>
 __global__ void k_cheb_step(long n, const T* __restrict__ b, const T* __restrict__ t, const T* __restrict__ dinv,
                             T f1, T f2, T* __restrict__ d, T* __restrict__ x) {
+  pdl_wait();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const T v = f1 * d[i] + f2 * dinv[i] * (b[i] - t[i]);
     d[i] = v;
@@ -89,6 +106,7 @@ void v_cheb_step(long n, const T* b, const T* t, const T* dinv, T f1, T f2, T* d
 
 template <typename T>
 __global__ void k_sub(long n, const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ o) {
+  pdl_wait();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     o[i] = a[i] - b[i];
 }
@@ -101,6 +119,7 @@ void v_sub(long n, const T* a, const T* b, T* out, cudaStream_t s) {
 
 template <typename T>
 __global__ void k_copy_indexed(long m, const int* __restrict__ idx, const T* __restrict__ src, T* __restrict__ dst) {
+  pdl_wait();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < m; i += (long)gridDim.x * blockDim.x)
     dst[idx[i]] = src[idx[i]];
 }
@@ -112,6 +131,7 @@ void v_copy_indexed(long m, const int* idx, const T* src, T* dst, cudaStream_t s
 }
 template <typename T>
 __global__ void k_zero_indexed(long m, const int* __restrict__ idx, T* __restrict__ dst) {
+  pdl_wait();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < m; i += (long)gridDim.x * blockDim.x)
     dst[idx[i]] = T(0);
 }
@@ -124,6 +144,7 @@ void v_zero_indexed(long m, const int* idx, T* dst, cudaStream_t s) {
 
 template <typename Ts, typename Td>
 __global__ void k_perm_scatter(long n, const int* __restrict__ perm, const Ts* __restrict__ in, Td* __restrict__ out) {
+  pdl_wait();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     out[perm[i]] = (Td)in[i];
 }
@@ -135,6 +156,7 @@ void v_permute_scatter(long n, const int* perm, const Ts* in, Td* out, cudaStrea
 }
 template <typename Ts, typename Td>
 __global__ void k_perm_gather(long n, const int* __restrict__ perm, const Ts* __restrict__ in, Td* __restrict__ out) {
+  pdl_wait();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     out[i] = (Td)in[perm[i]];
 }
@@ -148,6 +170,7 @@ void v_permute_gather(long n, const int* perm, const Ts* in, Td* out, cudaStream
 template <typename T>
 __global__ void k_spmv_add(long rows, const int* __restrict__ ptr, const int* __restrict__ col,
                            const T* __restrict__ val, const T* __restrict__ x, T* __restrict__ y) {
+  pdl_wait();
   for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < rows; r += (long)gridDim.x * blockDim.x) {
     T t = T(0);
     const int e = ptr[r + 1];
@@ -224,6 +247,7 @@ __global__ void __launch_bounds__(kDotThreads) k_multidot(long n, const double* 
                                                           int with_norm, double* __restrict__ out,
                                                           double* __restrict__ partial, unsigned* counters,
                                                           const int* __restrict__ active) {
+  pdl_wait();
   if (active && *active == 0) return;
   const int chunk = blockIdx.y;
   const int j0 = chunk * kDotChunk;
@@ -269,6 +293,7 @@ template <typename T>
 __global__ void __launch_bounds__(kDotThreads) k_dot(long n, const T* __restrict__ a, const T* __restrict__ b,
                                                      double* __restrict__ out, double* __restrict__ partial,
                                                      unsigned* counter, const int* __restrict__ active) {
+  pdl_wait();
   if (active && *active == 0) return;
   double acc[1] = {0};
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
@@ -285,6 +310,7 @@ void v_dot(long n, const T* a, const T* b, double* out_dev, double* partial, cud
 
 __global__ void k_multiaxpy(long n, int k, const double* __restrict__ coef, const double* __restrict__ V, long ld,
                             double* __restrict__ w, const int* __restrict__ active) {
+  pdl_wait();
   if (active && *active == 0) return;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     double t = w[i];
@@ -301,6 +327,7 @@ void v_multiaxpy(long n, int k, const double* coef_dev, const double* V, long ld
 
 __global__ void k_symv_dense(long n, const double* __restrict__ S, const double* __restrict__ x,
                              double* __restrict__ y) {
+  pdl_wait();
   const long row = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (row >= n) return;
@@ -320,6 +347,7 @@ void v_symv_dense(long n, const double* S, const double* x, double* y, cudaStrea
 
 template <typename T>
 __global__ void k_check_finite(long n, const T* __restrict__ x, int* flag) {
+  pdl_wait();
   int bad = 0;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     if (!isfinite(x[i])) bad = 1;
@@ -336,6 +364,7 @@ void v_check_finite(long n, const T* x, int* flag, cudaStream_t s) {
   template void v_axpby<T>(long, T, const T*, T, T*, cudaStream_t);                               \
   template void v_copy<T>(long, const T*, T*, cudaStream_t);                                      \
   template void v_scale<T>(long, T, T*, cudaStream_t);                                            \
+  template void v_zero<T>(long, T*, cudaStream_t);                                                \
   template void v_cheb_first<T>(long, const T*, const T*, T, T*, T*, cudaStream_t);               \
   template void v_cheb_step<T>(long, const T*, const T*, const T*, T, T, T*, T*, cudaStream_t);   \
   template void v_sub<T>(long, const T*, const T*, T*, cudaStream_t);                             \

@@ -30,6 +30,9 @@ template <typename T>
 void v_copy(long n, const T* x, T* y, cudaStream_t s);
 template <typename T>
 void v_scale(long n, T a, T* y, cudaStream_t s);
+// y = 0 by a kernel (not a memset node, so captured kernel chains stay kernel-to-kernel)
+template <typename T>
+void v_zero(long n, T* y, cudaStream_t s);
 template <typename Ts, typename Td>
 void v_cast(long n, const Ts* x, Td* y, cudaStream_t s);
 // Chebyshev: zero start  d = f2 * dinv * b, x = d

@@ -8,7 +8,7 @@ averaging for GMG), free slip, FGMRES (restart 100) with the block-Schur
 preconditioner and an FP32 V-cycle, FP64 outer residual, relative tolerance 1e-8.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-    python bench.py --profile-op a_cell_pass_fp32|stokes_vmult_fp64|mass_vmult_fp32|a_vmult_fp32
+    python bench.py --profile-op a_cell_pass_fp32|stokes_cell_pass_fp64|stokes_vmult_fp64|mass_vmult_fp32|a_vmult_fp32
 
 (--profile-op runs one operation of the workload three times between
 cudaProfilerStart/Stop, for `ncu --profile-from-start off` captures.)
@@ -50,10 +50,12 @@ FLOPS_STOKES_CELL_F64 = 8586
 # 152 SMs x 128 lanes x 2 x 2.07 GHz; FP64 = GB300's published 1.25 TFLOP/s
 FP32_PEAK_TFLOPS = 80.5
 FP64_PEAK_TFLOPS = 1.25
-# dram__bytes_read.sum + dram__bytes_write.sum of one finest-level launch of the
-# FP32 A-block cell pass (ncu --set full of `bench.py --profile-op
-# a_cell_pass_fp32`, summarised in profiles/); None until captured
-CELL_PASS_DRAM_BYTES = None
+# dram__bytes_read.sum + dram__bytes_write.sum of one finest-level launch of each
+# cell pass (ncu --set full of `bench.py --profile-op stokes_cell_pass_fp64` /
+# `a_cell_pass_fp32`, cold cache, summarised in profiles/): the reads of u, p
+# and eta; the per-cell outputs stay in L2
+STOKES_CELL_PASS_F64_DRAM_BYTES = 14206720
+A_CELL_PASS_F32_DRAM_BYTES = 6853888
 
 
 def log(*a):
@@ -326,10 +328,9 @@ def run_gpu(args):
              "stokes_vmult_fp32": n / ops["stokes_vmult_fp32"] / 1e9,
              "A_vmult_fp32": f.n_u / ops["A_vmult_fp32"] / 1e9,
              "A_vmult_fp64": f.n_u / ops["A_vmult_fp64"] / 1e9}
-    # --- roofline of the dominant kernel: the FP32 lattice cell pass of the
-    # velocity block (most launches of every V-cycle level; timed here on the
-    # finest level with CUDA events on the library's stream), and beside it the
-    # FP64 Stokes operator of the outer residual
+    # --- rooflines, each kernel timed alone on the finest level with CUDA events
+    # on the library's stream: the FP32 lattice cell pass of the velocity block
+    # (every V-cycle level), the FP64 Stokes operator and its cell pass
     t_cell = g.time_operation(gmg.TIME_A_CELL_PASS, gmg.FP32, 20)
     eta_words = f.n_cells * (27 if P.projection == 1 else 1)
     b_cell = 4 * (f.n_u + eta_words + 81 * f.n_cells)  # reads x and eta, writes 81 contributions per cell
@@ -338,6 +339,11 @@ def run_gpu(args):
     tflops_cell = FLOPS_A_CELL_F32 * f.n_cells / t_cell / 1e12
     t_s64 = ops["stokes_vmult_fp64"]
     tflops_s64 = FLOPS_STOKES_CELL_F64 * f.n_cells / t_s64 / 1e12
+    # the dominant kernel of the solve (largest share of the launch list): the FP64
+    # Stokes cell pass of the FGMRES matrix-vector product, timed alone
+    t_sc = g.time_operation(gmg.TIME_STOKES_CELL_PASS, gmg.FP64, 20)
+    b_sc = 8 * (n + eta_words + 89 * f.n_cells)  # reads u, p and eta, writes 81 + 8 contributions per cell
+    tflops_sc = FLOPS_STOKES_CELL_F64 * f.n_cells / t_sc / 1e12
     clocks = clk.summary()
 
     if rank != 0:
@@ -357,16 +363,26 @@ def run_gpu(args):
                    "l2": "flushed between timed solves (256 MiB write)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "MDoF/s", "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": n * 8},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": "lattice_cell_kernel_f32<A> (FP32 velocity-block cell pass, "
-                                                "32^3 finest level)",
-                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "traffic": CELL_PASS_DRAM_BYTES,
-                     "algorithmic_bytes_per_launch": b_cell, "seconds_per_launch": t_cell,
-                     "fp32": {"achieved_tflops": tflops_cell, "peak_tflops": FP32_PEAK_TFLOPS,
-                              "frac": tflops_cell / FP32_PEAK_TFLOPS, "peak_kind": "nominal",
-                              "flops_per_cell": FLOPS_A_CELL_F32},
-                     "note": "one thread per cell, 32768 cells: a single partial wave bound by each "
-                             "thread's dependent arithmetic chain; the inputs are L2-resident within a solve"},
+        "roofline": {"bound": "hbm", "kernel": "velocity_cell_kernel<double,3,STOKES> (FP64 Stokes cell pass, "
+                                                "32^3 finest level, 3 threads per cell)",
+                     "achieved": b_sc / t_sc / 1e9, "peak": peak, "unit": "GB/s", "frac": b_sc / t_sc / 1e9 / peak,
+                     "peak_kind": peak_kind, "traffic": STOKES_CELL_PASS_F64_DRAM_BYTES,
+                     "algorithmic_bytes_per_launch": b_sc, "seconds_per_launch": t_sc,
+                     "fp64": {"achieved_tflops": tflops_sc, "peak_tflops": FP64_PEAK_TFLOPS,
+                              "frac": tflops_sc / FP64_PEAK_TFLOPS, "peak_kind": "nominal",
+                              "flops_per_cell": FLOPS_STOKES_CELL_F64},
+                     "note": "bound by the FP64 pipe (1/64 of the FP32 rate on GB300), not by HBM: its inputs and "
+                             "outputs are L2-resident within a solve"},
+        "roofline_fp32_a_cell_pass": {
+            "bound": "hbm", "kernel": "lattice_cell_kernel_f32<A> (FP32 velocity-block cell pass of the V-cycle, "
+                                      "32^3 finest level)",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+            "traffic": A_CELL_PASS_F32_DRAM_BYTES, "algorithmic_bytes_per_launch": b_cell,
+            "seconds_per_launch": t_cell,
+            "fp32": {"achieved_tflops": tflops_cell, "peak_tflops": FP32_PEAK_TFLOPS,
+                     "frac": tflops_cell / FP32_PEAK_TFLOPS, "peak_kind": "nominal",
+                     "flops_per_cell": FLOPS_A_CELL_F32},
+            "note": "one thread per cell, 32768 cells: one partial wave, latency-bound"},
         "roofline_fp64_stokes": {"bound": "fp64", "kernel": "velocity_cell_kernel<double,3,STOKES> + gathers "
                                                             "(FP64 Stokes operator, 32^3)",
                                  "seconds_per_application": t_s64, "achieved_tflops": tflops_s64,
@@ -395,6 +411,7 @@ def run_gpu(args):
 
 
 PROFILE_OPS = {"a_cell_pass_fp32": ("TIME_A_CELL_PASS", "FP32"), "a_vmult_fp32": ("TIME_A_VMULT", "FP32"),
+               "stokes_cell_pass_fp64": ("TIME_STOKES_CELL_PASS", "FP64"),
                "stokes_vmult_fp64": ("TIME_STOKES_VMULT", "FP64"), "mass_vmult_fp32": ("TIME_MASS_VMULT", "FP32")}
 
 

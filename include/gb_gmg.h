@@ -228,7 +228,8 @@ enum gb_gmg_timed_operation {
   GB_GMG_TIME_STOKES_PRECONDITIONER = 3, /* stokes_preconditioner (cheap)        */
   GB_GMG_TIME_A_PRECONDITIONER = 4,      /* A_preconditioner (one V-cycle)       */
   GB_GMG_TIME_S_PRECONDITIONER = 5,      /* S_preconditioner (one V-cycle)       */
-  GB_GMG_TIME_A_CELL_PASS = 6            /* A-block cell pass alone (finest)     */
+  GB_GMG_TIME_A_CELL_PASS = 6,           /* A-block cell pass alone (finest)     */
+  GB_GMG_TIME_STOKES_CELL_PASS = 7       /* Stokes cell pass alone (finest)      */
 };
 
 /* Mean device time of one call of `what` in `precision`, over `repeats` calls
