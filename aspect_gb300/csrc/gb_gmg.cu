@@ -51,6 +51,8 @@ struct Handle {
   DevBuf<double> stage_a, stage_b, partial, dots_d;
   double* dots_h = nullptr;
   DevBuf<double> V, Z, wv, xv, rv, bv, tv, t2v, coef_d;
+  DevBuf<double> idrP, idrG, idrU;  // IDR(s): shadow space, G and U blocks (s vectors each)
+  int idr_s_alloc = 0;
   DevBuf<double> hcol_d, arn_d;  // Arnoldi column and scalars (|w|^2, |w| before, 1/|w|) on the device
   DevBuf<int> arn_flag;          // 1: the step needs its second Gram-Schmidt pass
   DevBuf<double> cg_r, cg_z, cg_p, cg_q, cg_x;
@@ -880,6 +882,166 @@ int gmres(Handle& H, double* x, const double* b, double tol, int maxit, int rest
   }
 }
 
+// ---------------------------------------------------------------- IDR(s)
+void to_internal(Handle& H, int lev, const double* d_caller, double* d_internal, bool with_u, bool with_p);
+
+// Shadow space of IDR(s): s vectors in the caller's numbering, entries uniform
+// in [-1, 1) from a SplitMix64 stream per vector (seed + i), orthonormalised by
+// modified Gram-Schmidt in FP64. The oracle builds the same vectors, so both
+// run IDR(s) with the same space.
+uint64_t splitmix64_next(uint64_t& state) {
+  uint64_t z = (state += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+std::vector<double> idr_shadow_space(long n, int s, uint64_t seed) {
+  std::vector<double> P((size_t)s * n);
+  for (int i = 0; i < s; ++i) {
+    uint64_t st = seed + (uint64_t)i;
+    double* p = P.data() + (size_t)i * n;
+    for (long k = 0; k < n; ++k) p[k] = 2.0 * ((double)(splitmix64_next(st) >> 11) * 0x1.0p-53) - 1.0;
+    for (int j = 0; j < i; ++j) {
+      const double* q = P.data() + (size_t)j * n;
+      double d = 0;
+      for (long k = 0; k < n; ++k) d += p[k] * q[k];
+      for (long k = 0; k < n; ++k) p[k] -= d * q[k];
+    }
+    double nn = 0;
+    for (long k = 0; k < n; ++k) nn += p[k] * p[k];
+    nn = std::sqrt(nn);
+    for (long k = 0; k < n; ++k) p[k] /= nn;
+  }
+  return P;
+}
+constexpr uint64_t kIdrSeed = 20261204ull;
+
+// IDR(s) with bi-orthogonalisation and right preconditioning: the published
+// algorithm of van Gijzen and Sonneveld ("Algorithm 913", ACM TOMS 38, 2011),
+// the method behind the reference's "Krylov method for cheap solver steps =
+// IDR(s)" (source/simulator/solver/stokes_matrix_free_local_smoothing.cc:1290-1299,
+// deal.II SolverIDR). One iteration = s inner steps plus one dimension-reduction
+// step, s + 1 preconditioner and operator applications; convergence is checked
+// after every residual update and counted in iterations, as the reference
+// prints them. omega = (t, r) / (t, t). The recursively updated residual is
+// confirmed against the true FP64 residual at the end; if they disagree (FP32
+// V-cycles are not exactly linear) IDR(s) restarts from the true residual.
+int idr(Handle& H, double* x, const double* b, double tol, int maxit, int s, int prec,
+        const gb_gmg_solve_params* P, bool& converged, double& final_res) {
+  const long n = H.n_top();
+  GB_CHECK(s >= 1 && s <= 8, GB_GMG_INVALID_ARGUMENT, "IDR(s) parameter must be in 1..8");
+  if (H.coef_d.n < (size_t)s) H.coef_d.alloc(s);  // (GMRES sizes it restart + 2 when it runs first)
+  if (H.idr_s_alloc != s) {
+    H.idrP.alloc((size_t)s * n);
+    H.idrG.alloc((size_t)s * n);
+    H.idrU.alloc((size_t)s * n);
+    // built in the caller's numbering, staged in the G block, mapped to the internal one
+    const std::vector<double> Ph = idr_shadow_space(n, s, kIdrSeed);
+    GB_CUDA(cudaMemcpyAsync(H.idrG.p, Ph.data(), Ph.size() * sizeof(double), cudaMemcpyHostToDevice, H.st));
+    for (int i = 0; i < s; ++i)
+      to_internal(H, H.n_levels - 1, H.idrG.p + (size_t)i * n, H.idrP.p + (size_t)i * n, true, true);
+    GB_CUDA(cudaStreamSynchronize(H.st));
+    H.idr_s_alloc = s;
+  }
+  const double* Pm = H.idrP.p;
+  double* G = H.idrG.p;
+  double* U = H.idrU.p;
+  double* r = H.rv.p;
+  double* v = H.wv.p;
+  double* t = H.tv.p;
+  double* tmp = H.xv.p;  // not t2v: block_preconditioner uses t2v as scratch
+  double* dd = H.dots_d.p;
+  auto fetch = [&](int k) {  // k doubles of dots_d -> host
+    GB_CUDA(cudaMemcpyAsync(H.dots_h, dd, k * sizeof(double), cudaMemcpyDeviceToHost, H.st));
+    GB_CUDA(cudaStreamSynchronize(H.st));
+    return std::vector<double>(H.dots_h, H.dots_h + k);
+  };
+  auto upload_coef = [&](const std::vector<double>& c) {
+    GB_CUDA(cudaMemcpyAsync(H.coef_d.p, c.data(), c.size() * sizeof(double), cudaMemcpyHostToDevice, H.st));
+  };
+  int it = 0;
+  converged = false;
+  while (true) {
+    stokes64(H, x, t);
+    v_copy<double>(n, b, r, H.st);
+    v_axpby<double>(n, -1.0, t, 1.0, r, H.st);
+    double normr = std::sqrt(dot_host(H, n, r, r));
+    final_res = normr;
+    GB_CHECK(std::isfinite(normr), GB_GMG_NAN_DETECTED, "NaN or Inf in the Stokes residual");
+    if (normr <= tol) { converged = true; return it; }
+    if (it >= maxit) return it;
+    v_zero<double>((size_t)s * n, G, H.st);
+    v_zero<double>((size_t)s * n, U, H.st);
+    std::vector<double> M((size_t)s * s, 0.0);  // M[i*s + k] = (P_i, G_k)
+    for (int i = 0; i < s; ++i) M[(size_t)i * s + i] = 1.0;
+    double om = 1.0;
+    bool inner_conv = false;
+    while (it < maxit && !inner_conv) {
+      ++it;
+      v_multidot(n, r, Pm, n, s, false, dd, H.partial.p, H.st);
+      std::vector<double> f = fetch(s);
+      for (int k = 0; k < s && !inner_conv; ++k) {
+        // c from the lower-triangular system M(k:s, k:s) c = f(k:s)
+        std::vector<double> c(s - k);
+        for (int i = k; i < s; ++i) {
+          double acc = f[i];
+          for (int l = k; l < i; ++l) acc -= M[(size_t)i * s + l] * c[l - k];
+          c[i - k] = acc / M[(size_t)i * s + i];
+        }
+        // v = r - sum c_i G_i, preconditioned; U_k = om v + sum c_i U_i; G_k = K U_k
+        v_copy<double>(n, r, tmp, H.st);
+        std::vector<double> mc(s - k);
+        for (int i = 0; i < s - k; ++i) mc[i] = -c[i];
+        upload_coef(mc);
+        v_multiaxpy(n, s - k, H.coef_d.p, G + (size_t)k * n, n, tmp, H.st);
+        block_preconditioner(H, prec, false, P, tmp, v);
+        v_copy<double>(n, v, tmp, H.st);
+        v_scale<double>(n, om, tmp, H.st);
+        upload_coef(c);
+        v_multiaxpy(n, s - k, H.coef_d.p, U + (size_t)k * n, n, tmp, H.st);
+        double* Uk = U + (size_t)k * n;
+        double* Gk = G + (size_t)k * n;
+        v_copy<double>(n, tmp, Uk, H.st);
+        stokes64(H, Uk, Gk);
+        // bi-orthogonalise G_k against P_0 .. P_{k-1}
+        for (int i = 0; i < k; ++i) {
+          const double alpha = dot_host(H, n, Pm + (size_t)i * n, Gk) / M[(size_t)i * s + i];
+          v_axpby<double>(n, -alpha, G + (size_t)i * n, 1.0, Gk, H.st);
+          v_axpby<double>(n, -alpha, U + (size_t)i * n, 1.0, Uk, H.st);
+        }
+        v_multidot(n, Gk, Pm + (size_t)k * n, n, s - k, false, dd, H.partial.p, H.st);
+        const std::vector<double> mk = fetch(s - k);
+        for (int i = k; i < s; ++i) M[(size_t)i * s + k] = mk[i - k];
+        const double mkk = M[(size_t)k * s + k];
+        GB_CHECK(mkk != 0.0 && std::isfinite(mkk), GB_GMG_BREAKDOWN, "IDR(s) breakdown");
+        const double beta = f[k] / mkk;
+        v_axpby<double>(n, -beta, Gk, 1.0, r, H.st);
+        v_axpby<double>(n, beta, Uk, 1.0, x, H.st);
+        normr = std::sqrt(dot_host(H, n, r, r));
+        final_res = normr;
+        GB_CHECK(std::isfinite(normr), GB_GMG_NAN_DETECTED, "NaN or Inf in the IDR(s) residual");
+        if (normr <= tol) { inner_conv = true; break; }
+        for (int i = k + 1; i < s; ++i) f[i] -= beta * M[(size_t)i * s + k];
+      }
+      if (inner_conv) break;
+      // dimension reduction: v = B r, t = K v, om = (t, r) / (t, t)
+      block_preconditioner(H, prec, false, P, r, v);
+      stokes64(H, v, t);
+      v_multidot(n, t, r, n, 1, true, dd, H.partial.p, H.st);
+      const std::vector<double> tr = fetch(2);
+      GB_CHECK(tr[1] > 0 && std::isfinite(tr[1]), GB_GMG_BREAKDOWN, "IDR(s) breakdown");
+      om = tr[0] / tr[1];
+      v_axpby<double>(n, om, v, 1.0, x, H.st);
+      v_axpby<double>(n, -om, t, 1.0, r, H.st);
+      normr = std::sqrt(dot_host(H, n, r, r));
+      final_res = normr;
+      GB_CHECK(std::isfinite(normr), GB_GMG_NAN_DETECTED, "NaN or Inf in the IDR(s) residual");
+      if (normr <= tol) inner_conv = true;
+    }
+    // loop back: the true residual of the iterate decides
+  }
+}
+
 // ---------------------------------------------------------------- the solve
 void ensure_workspace(Handle& H) {
   const long n = H.n_top();
@@ -1090,7 +1252,9 @@ void solve_internal(Handle& H, const gb_gmg_solve_params* P, gb_gmg_outputs* out
     // is a fixed linear operator. A V-cycle in FP32 is not exactly linear any
     // more, so with FP32 levels the cheap phase is flexible GMRES (FGMRES).
     const bool flexible_cheap = prec == GB_GMG_FP32;
-    if (P->n_cheap_steps > 0)
+    if (P->n_cheap_steps > 0 && P->krylov == GB_GMG_IDR)
+      out->cheap_iterations = idr(H, x, b, tol, P->n_cheap_steps, P->idr_s, prec, P, conv, fr);
+    else if (P->n_cheap_steps > 0)
       out->cheap_iterations =
           gmres(H, x, b, tol, P->n_cheap_steps, P->restart, flexible_cheap, false, prec, false, P, conv, fr);
     if (!conv && P->n_expensive_steps > 0)
@@ -1163,6 +1327,7 @@ void gb_gmg_default_solve_params(gb_gmg_solve_params* p) {
   p->tol_S = 1e-6;
   p->mg_precision = GB_GMG_FP64;
   p->krylov = GB_GMG_GMRES;
+  p->idr_s = 2;
   p->ir_inner_tolerance = 1e-3;
 }
 
@@ -1276,6 +1441,8 @@ int gb_gmg_finalize_setup(gb_gmg* g) {
     gb::ensure_workspace(H);
     GB_CUDA(cudaStreamSynchronize(H.st));
     H.reset_graphs();
+    H.restart_alloc = -1;  // Krylov and IDR(s) blocks are sized by the finest level: rebuilt on next use
+    H.idr_s_alloc = 0;
     H.setup_done = true;
     H.visc_done = false;
     H.prec_done[0] = H.prec_done[1] = false;

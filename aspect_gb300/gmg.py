@@ -24,7 +24,7 @@ LIB_PATH = os.path.join(HERE, "libgb_gmg.so")
 
 OP_STOKES, OP_A, OP_BT, OP_MASS = 0, 1, 2, 3
 FP64, FP32 = 0, 1
-GMRES, GMRES_IR = 0, 1
+GMRES, GMRES_IR, IDR = 0, 1, 2
 VISC_DGQ0, VISC_DGQ1 = 0, 1
 COARSE_CHEBYSHEV, COARSE_DENSE_FP64 = 0, 1
 
@@ -55,7 +55,7 @@ class SolveParams(ctypes.Structure):
                 ("n_cheap_steps", ctypes.c_int), ("n_expensive_steps", ctypes.c_int),
                 ("restart", ctypes.c_int), ("tol_A", ctypes.c_double), ("tol_S", ctypes.c_double),
                 ("mg_precision", ctypes.c_int), ("krylov", ctypes.c_int),
-                ("ir_inner_tolerance", ctypes.c_double)]
+                ("ir_inner_tolerance", ctypes.c_double), ("idr_s", ctypes.c_int)]
 
 
 class Outputs(ctypes.Structure):

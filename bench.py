@@ -9,6 +9,7 @@ preconditioner and an FP32 V-cycle, FP64 outer residual, relative tolerance 1e-8
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
     python bench.py --profile-op a_cell_pass_fp32|stokes_cell_pass_fp64|stokes_vmult_fp64|mass_vmult_fp32|a_vmult_fp32
+    python bench.py --sweep 32,64      (operator timings per size, no solve)
 
 (--profile-op runs one operation of the workload three times between
 cudaProfilerStart/Stop, for `ncu --profile-from-start off` captures.)
@@ -307,6 +308,8 @@ def run_gpu(args):
     log("fp64-mg solve", t64, o64)
     tir, oir, xir = timed_solve(linear_solver_tolerance=TOL, mg_precision=gmg.FP32, krylov=gmg.GMRES_IR)
     log("gmres-ir solve", tir, oir)
+    tidr, oidr, xidr = timed_solve(linear_solver_tolerance=TOL, mg_precision=gmg.FP32, krylov=gmg.IDR, idr_s=2)
+    log("idr(2) solve", tidr, oidr)
     _, _, x32 = timed_solve(**params)
     rel = lambda a, b: float(torch.linalg.norm(a[: f.n_u] - b[: f.n_u]) / torch.linalg.norm(b[: f.n_u]))
 
@@ -402,7 +405,12 @@ def run_gpu(args):
             "gmres_ir": {"solve_s": tir, "iterations": oir["cheap_iterations"],
                          "fp64_stokes_applications": oir["fp64_stokes_applications"],
                          "speedup_vs_fp64_mg": t64 / tir},
-            "velocity_rel_l2_vs_fp64_mg": {"mixed": rel(x32, x64), "gmres_ir": rel(xir, x64)},
+            "idr2_fp32mg": {"solve_s": tidr, "iterations": oidr["cheap_iterations"] + oidr["expensive_iterations"],
+                            "A_preconditioner_applications": oidr["A_preconditioner_applications"],
+                            "fp64_stokes_applications": oidr["fp64_stokes_applications"],
+                            "speedup_vs_fp64_mg": t64 / tidr},
+            "velocity_rel_l2_vs_fp64_mg": {"mixed": rel(x32, x64), "gmres_ir": rel(xir, x64),
+                                           "idr2": rel(xidr, x64)},
             "operator_seconds": ops, "operator_gdofs": gdofs,
             "solve_share_seconds": {"stokes_vmult_fp64": mixed["fp64_stokes_applications"] * t_s64},
         },
@@ -432,6 +440,44 @@ def run_profile_op(name: str):
     print(json.dumps({"profile_op": name, "seconds_per_call": sec, "cells": P.fine.n_cells}), flush=True)
 
 
+def run_sweep(sizes):
+    """Operator timings of the sinker workload at several sizes (no solve): at 32^3
+    every operand is L2-resident, at 64^3 the FP32 A-block vmult's working set
+    (vectors, viscosity, per-cell outputs: ~165 MB) exceeds the 126 MB L2, so
+    its HBM fraction starts to mean something. One JSON line per size."""
+    import torch
+    from aspect_gb300 import gmg, problems
+    torch.cuda.init()
+    peak, peak_kind = peaks()
+    for nc in sizes:
+        P = problems.sinkers_3d(nc)
+        g = gmg.from_problem(P, build=False)
+        f = P.fine
+        n = P.n_dofs
+        eta_words = f.n_cells * (27 if P.projection == 1 else 1)
+        t = {k: g.time_operation(getattr(gmg, w), getattr(gmg, pr), 20)
+             for k, w, pr in [("A_vmult_fp32", "TIME_A_VMULT", "FP32"), ("A_cell_pass_fp32", "TIME_A_CELL_PASS", "FP32"),
+                              ("stokes_vmult_fp64", "TIME_STOKES_VMULT", "FP64"),
+                              ("stokes_cell_pass_fp64", "TIME_STOKES_CELL_PASS", "FP64"),
+                              ("mass_vmult_fp32", "TIME_MASS_VMULT", "FP32")]}
+        b = {"A_vmult_fp32": 4 * (2 * f.n_u + eta_words),
+             "A_cell_pass_fp32": 4 * (f.n_u + eta_words + 81 * f.n_cells),
+             "stokes_vmult_fp64": 8 * (2 * n + eta_words),
+             "stokes_cell_pass_fp64": 8 * (n + eta_words + 89 * f.n_cells),
+             "mass_vmult_fp32": 4 * (2 * f.n_p + eta_words)}
+        line = {"sweep": f"sinkers_{nc}^3", "cells": f.n_cells, "n_u": f.n_u, "n_p": f.n_p, "peak_gbs": peak,
+                "peak_kind": peak_kind, "ops": {}}
+        for k in t:
+            gbs = b[k] / t[k] / 1e9
+            line["ops"][k] = {"seconds": t[k], "algorithmic_bytes": b[k], "gbs": gbs, "hbm_frac": gbs / peak,
+                              "gdofs": (f.n_u if k.startswith("A") else (f.n_p if k.startswith("mass") else n))
+                              / t[k] / 1e9}
+        line["ops"]["stokes_cell_pass_fp64"]["fp64_tflops"] = FLOPS_STOKES_CELL_F64 * f.n_cells / t["stokes_cell_pass_fp64"] / 1e12
+        line["ops"]["A_cell_pass_fp32"]["fp32_tflops"] = FLOPS_A_CELL_F32 * f.n_cells / t["A_cell_pass_fp32"] / 1e12
+        print(json.dumps(line), flush=True)
+        del g
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -439,8 +485,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--profile-op", default=None, choices=sorted(PROFILE_OPS))
+    ap.add_argument("--sweep", default=None, help="comma-separated cells per direction, e.g. 32,64")
     args = ap.parse_args()
-    if args.profile_op:
+    if args.sweep:
+        run_sweep([int(v) for v in args.sweep.split(",")])
+    elif args.profile_op:
         run_profile_op(args.profile_op)
     elif args.impl == "reference":
         run_reference(args)

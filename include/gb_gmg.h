@@ -68,7 +68,10 @@ enum gb_gmg_precision { GB_GMG_FP64 = 0, GB_GMG_FP32 = 1 };
 
 enum gb_gmg_krylov {
   GB_GMG_GMRES = 0,       /* reference: cheap GMRES, FGMRES fallback          */
-  GB_GMG_GMRES_IR = 1     /* FP64 iterative refinement around FP32 GMRES       */
+  GB_GMG_GMRES_IR = 1,    /* FP64 iterative refinement around FP32 GMRES       */
+  GB_GMG_IDR = 2          /* cheap IDR(s), FGMRES fallback ("Krylov method for
+                             cheap solver steps = IDR(s)",
+                             stokes_matrix_free_local_smoothing.cc:1290-1299)  */
 };
 
 enum gb_gmg_projection {
@@ -110,6 +113,7 @@ typedef struct gb_gmg_solve_params {
   int mg_precision;                /* gb_gmg_precision of the V-cycle                 */
   int krylov;                      /* gb_gmg_krylov                                   */
   double ir_inner_tolerance;       /* GMRES_IR: relative tolerance of each inner solve */
+  int idr_s;                       /* IDR(s) parameter (2), source/simulator/parameters.cc:483 */
 } gb_gmg_solve_params;
 
 /* StokesSolver::SolverOutputs plus the counters the reference prints. */

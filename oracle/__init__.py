@@ -171,10 +171,10 @@ class Oracle:
         return out
 
     def solve(self, rhs, x0=None, tol_rel=1e-7, abs_tol=0.0, n_cheap=1000, n_expensive=1000,
-              restart=100, tol_A=1e-2, tol_S=1e-6):
+              restart=100, tol_A=1e-2, tol_S=1e-6, krylov=0, idr_s=2):
         rhs = _d(rhs)
         sol = _d(np.zeros_like(rhs) if x0 is None else x0).copy()
-        params = _d([tol_rel, abs_tol, n_cheap, n_expensive, restart, tol_A, tol_S])
+        params = _d([tol_rel, abs_tol, n_cheap, n_expensive, restart, tol_A, tol_S, krylov, idr_s])
         out = np.zeros(8)
         self._chk(self.L.orc_solve(self.h, _ptr(params, _dp), _ptr(rhs, _dp), _ptr(sol, _dp),
                                    _ptr(out, _dp)))

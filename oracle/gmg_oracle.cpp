@@ -340,6 +340,8 @@ struct Params {
   double tol_A = 1e-2, tol_S = 1e-6;
   int mg_float = 0;             // level operators in float
   int A_symmetric = 1;
+  int krylov = 0;               // cheap phase: 0 GMRES, 2 IDR(s)
+  int idr_s = 2;                // IDR(s) parameter
 };
 
 struct Outputs {
@@ -1042,6 +1044,122 @@ struct Oracle {
     }
   }
 
+  // IDR(s) shadow space: s vectors, entries uniform in [-1, 1) from a SplitMix64
+  // stream per vector (seed + i), orthonormalised by modified Gram-Schmidt.
+  static uint64_t splitmix64_next(uint64_t& state) {
+    uint64_t z = (state += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  }
+  static std::vector<std::vector<double>> idr_shadow_space(int n, int s, uint64_t seed) {
+    std::vector<std::vector<double>> P(s, std::vector<double>(n));
+    for (int i = 0; i < s; ++i) {
+      uint64_t st = seed + (uint64_t)i;
+      std::vector<double>& p = P[i];
+      for (int k = 0; k < n; ++k) p[k] = 2.0 * ((double)(splitmix64_next(st) >> 11) * 0x1.0p-53) - 1.0;
+      for (int j = 0; j < i; ++j) {
+        double d = 0;
+        for (int k = 0; k < n; ++k) d += p[k] * P[j][k];
+        for (int k = 0; k < n; ++k) p[k] -= d * P[j][k];
+      }
+      double nn = 0;
+      for (int k = 0; k < n; ++k) nn += p[k] * p[k];
+      nn = std::sqrt(nn);
+      for (int k = 0; k < n; ++k) p[k] /= nn;
+    }
+    return P;
+  }
+
+  // IDR(s) with bi-orthogonalisation and right preconditioning, restated from
+  // van Gijzen and Sonneveld, "Algorithm 913: An elegant IDR(s) variant that
+  // efficiently exploits biorthogonality properties", ACM TOMS 38 (2011): the
+  // method the reference selects with "Krylov method for cheap solver steps =
+  // IDR(s)" (stokes_matrix_free_local_smoothing.cc:1290-1299; deal.II SolverIDR,
+  // not vendored). Iterations count outer steps (s + 1 preconditioner
+  // applications each); convergence is checked after every residual update;
+  // omega = (t, r) / (t, t). Ends on the true residual, restarting if needed.
+  int idr(double* x, const double* b, double tol, int maxit, const Params& P, bool& converged, double& final_res) {
+    Level& F = fine();
+    const int n = F.n_u + F.n_p, s = P.idr_s;
+    if (s < 1) throw std::runtime_error("IDR(s) parameter must be >= 1");
+    const std::vector<std::vector<double>> Pm = idr_shadow_space(n, s, 20261204ull);
+    std::vector<double> r(n), v(n), t(n), tmp(n);
+    int it = 0;
+    converged = false;
+    while (true) {
+      stokes_vmult(x, t.data());
+      for (int i = 0; i < n; ++i) r[i] = b[i] - t[i];
+      double normr = std::sqrt(dot(r, r));
+      final_res = normr;
+      if (normr <= tol) { converged = true; return it; }
+      if (it >= maxit) return it;
+      std::vector<std::vector<double>> G(s, std::vector<double>(n, 0.0)), U(s, std::vector<double>(n, 0.0));
+      std::vector<double> M((size_t)s * s, 0.0);
+      for (int i = 0; i < s; ++i) M[(size_t)i * s + i] = 1.0;
+      double om = 1.0;
+      bool inner_conv = false;
+      while (it < maxit && !inner_conv) {
+        ++it;
+        std::vector<double> f(s);
+        for (int i = 0; i < s; ++i) f[i] = dot(r, Pm[i]);
+        for (int k = 0; k < s && !inner_conv; ++k) {
+          std::vector<double> c(s - k);
+          for (int i = k; i < s; ++i) {
+            double acc = f[i];
+            for (int l = k; l < i; ++l) acc -= M[(size_t)i * s + l] * c[l - k];
+            c[i - k] = acc / M[(size_t)i * s + i];
+          }
+          for (int q = 0; q < n; ++q) {
+            double a = r[q];
+            for (int i = k; i < s; ++i) a -= c[i - k] * G[i][q];
+            tmp[q] = a;
+          }
+          block_prec(tmp.data(), v.data(), false, P);
+          for (int q = 0; q < n; ++q) {
+            double a = om * v[q];
+            for (int i = k; i < s; ++i) a += c[i - k] * U[i][q];
+            tmp[q] = a;
+          }
+          U[k] = tmp;
+          stokes_vmult(U[k].data(), G[k].data());
+          for (int i = 0; i < k; ++i) {
+            const double alpha = dot(Pm[i], G[k]) / M[(size_t)i * s + i];
+            for (int q = 0; q < n; ++q) {
+              G[k][q] -= alpha * G[i][q];
+              U[k][q] -= alpha * U[i][q];
+            }
+          }
+          for (int i = k; i < s; ++i) M[(size_t)i * s + k] = dot(G[k], Pm[i]);
+          const double mkk = M[(size_t)k * s + k];
+          if (mkk == 0.0 || !std::isfinite(mkk)) throw std::runtime_error("IDR(s) breakdown");
+          const double beta = f[k] / mkk;
+          for (int q = 0; q < n; ++q) {
+            r[q] -= beta * G[k][q];
+            x[q] += beta * U[k][q];
+          }
+          normr = std::sqrt(dot(r, r));
+          final_res = normr;
+          if (normr <= tol) { inner_conv = true; break; }
+          for (int i = k + 1; i < s; ++i) f[i] -= beta * M[(size_t)i * s + k];
+        }
+        if (inner_conv) break;
+        block_prec(r.data(), v.data(), false, P);
+        stokes_vmult(v.data(), t.data());
+        const double tt = dot(t, t);
+        if (!(tt > 0) || !std::isfinite(tt)) throw std::runtime_error("IDR(s) breakdown");
+        om = dot(t, r) / tt;
+        for (int q = 0; q < n; ++q) {
+          x[q] += om * v[q];
+          r[q] -= om * t[q];
+        }
+        normr = std::sqrt(dot(r, r));
+        final_res = normr;
+        if (normr <= tol) inner_conv = true;
+      }
+    }
+  }
+
   // StokesMatrixFreeHandler::solve (scaled pressure unknown p/s in and out)
   void solve(const double* rhs, double* sol, const Params& P, Outputs& out) {
     Level& F = fine();
@@ -1066,7 +1184,9 @@ struct Oracle {
     bool conv = false;
     double fr = 0;
     out.cheap_iterations = out.expensive_iterations = 0;
-    if (P.n_cheap > 0)
+    if (P.n_cheap > 0 && P.krylov == 2)
+      out.cheap_iterations = idr(x.data(), rhs, tol, P.n_cheap, P, conv, fr);
+    else if (P.n_cheap > 0)
       out.cheap_iterations = gmres(x.data(), rhs, tol, P.n_cheap, P.restart, false, false, P, conv, fr);
     if (!conv && P.n_expensive > 0) {
       out.expensive_iterations = gmres(x.data(), rhs, tol, P.n_expensive, P.restart, true, true, P, conv, fr);
@@ -1284,7 +1404,7 @@ int orc_adjoint_gradient(void* p, const double* u, const double* lam, double* gr
   })
 }
 
-// params: [tol_rel, abs_tol, n_cheap, n_expensive, restart, tol_A, tol_S]
+// params: [tol_rel, abs_tol, n_cheap, n_expensive, restart, tol_A, tol_S, krylov, idr_s]
 // outputs: [initial_res, final_res, tolerance, cheap_its, expensive_its, nA, nS, status]
 int orc_solve(void* p, const double* params, const double* rhs, double* sol, double* outputs) {
   Oracle* h = (Oracle*)p;
@@ -1292,6 +1412,7 @@ int orc_solve(void* p, const double* params, const double* rhs, double* sol, dou
     orc::Params P;
     P.tol_rel = params[0]; P.abs_tol = params[1]; P.n_cheap = (int)params[2];
     P.n_expensive = (int)params[3]; P.restart = (int)params[4]; P.tol_A = params[5]; P.tol_S = params[6];
+    P.krylov = (int)params[7]; P.idr_s = (int)params[8];
     orc::Outputs o;
     h->solve(rhs, sol, P, o);
     outputs[0] = o.initial_nonlinear_residual; outputs[1] = o.final_linear_residual;

@@ -87,3 +87,24 @@ def test_solve_is_bit_reproducible():
     x2, o2 = g.solve(P.rhs, linear_solver_tolerance=1e-8, mg_precision=gmg.FP32)
     assert o1["cheap_iterations"] == o2["cheap_iterations"]
     assert np.array_equal(x1, x2)
+
+
+@pytest.mark.parametrize("precision", [gmg.FP64, gmg.FP32])
+def test_idr_matches_oracle(precision):
+    """IDR(2) as the cheap Krylov method: same shadow space as the oracle (built
+    in the caller's numbering), converged on the true FP64 residual; in FP64 the
+    iteration count matches the oracle's within one."""
+    P = problems.sinkers_3d(8)
+    g = gmg.from_problem(P)
+    x, out = g.solve(P.rhs, linear_solver_tolerance=1e-8, mg_precision=precision, krylov=gmg.IDR, idr_s=2)
+    o = Oracle(P.levels)
+    o.set_viscosity(P.eta, P.projection, P.pressure_scaling)
+    o.build_preconditioner(False)
+    xr, info = o.solve(P.rhs, tol_rel=1e-8, krylov=2, idr_s=2)
+    assert out["status"] == 0 and out["expensive_iterations"] == 0 and info["status"] == 0
+    r = P.rhs - o.vmult(0, len(P.levels) - 1, x)
+    assert np.linalg.norm(r) <= 1.01 * out["solver_tolerance"]
+    f = P.fine
+    assert rel_err(x[: f.n_u], xr[: f.n_u]) < 1e-5
+    if precision == gmg.FP64:
+        assert abs(out["cheap_iterations"] - info["cheap_iterations"]) <= 1
