@@ -1501,6 +1501,65 @@ int gb_gmg_build_preconditioner(gb_gmg* g) {
   })
 }
 
+// correct_stokes_rhs (stokes_matrix_free_local_smoothing.cc:618-754): rhs -= K u0 with
+// plain reads of u0 (read_dof_values_plain: the constrained entries carry the
+// inhomogeneities), contributions distributed through the constraints and
+// nothing added to constrained rows. The cell pass is the FP64 Stokes cell pass
+// over a table of raw internal DoF indices (no constraint codes); the gather is
+// the level's own with the "constrained rows are zero" epilogue.
+int gb_gmg_correct_stokes_rhs(gb_gmg* g, const double* u0, double* rhs) {
+  if (!g || !u0 || !rhs) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
+    const int top = H.n_levels - 1;
+    gb::Level& F = H.levels[top];
+    const long nu = F.n_u, n = F.n_u + F.n_p;
+    const int nv = F.dim == 3 ? 27 : 9, npc = F.dim == 3 ? 8 : 4, ncu = F.dim * nv;
+    if (!F.cdu_raw_d.p) {
+      std::vector<int> ru((size_t)F.n_cells * ncu), rp((size_t)F.n_cells * npc);
+      for (long ic = 0; ic < F.n_cells; ++ic) {
+        const long cc = F.cell_of_internal.empty() ? ic : F.cell_of_internal[ic];
+        for (int k = 0; k < ncu; ++k) {
+          const int gdof = F.cdu[(size_t)cc * ncu + k];
+          ru[(size_t)ic * ncu + k] = F.perm_u.empty() ? gdof : F.perm_u[gdof];
+        }
+        for (int k = 0; k < npc; ++k) {
+          const int gdof = F.cdp[(size_t)cc * npc + k];
+          rp[(size_t)ic * npc + k] = F.perm_p.empty() ? gdof : F.perm_p[gdof];
+        }
+      }
+      F.cdu_raw_d.upload(ru);
+      F.cdp_raw_d.upload(rp);
+    }
+    double* a = H.stage_a.p;
+    double* b = H.stage_b.p;
+    double* y = H.tv.p;
+    GB_CUDA(cudaMemcpyAsync(a, u0, n * sizeof(double), cudaMemcpyHostToDevice, H.st));
+    gb::to_internal(H, top, a, b, true, true);
+    gb::LevelDev<double>& D = F.f64;
+    const gb::LevelView<double> v = F.view<double>(H.s, H.compressible);
+    gb::LevelView<double> plain = v;
+    plain.structured = 0;
+    plain.cdu = F.cdu_raw_d.p;
+    plain.cdp = F.cdp_raw_d.p;
+    gb::launch_cell_pass<double>(plain, gb::OPK_STOKES, b, b + nu, D.Eu.p, D.Ep.p, H.st);
+    ++H.cell_launches;
+    for (int block = 0; block < 2; ++block) {
+      gb::GatherArgs<double> ga{};
+      ga.E = block == 0 ? D.Eu.p : D.Ep.p;
+      ga.x = block == 0 ? b : b + nu;
+      ga.y = block == 0 ? y : y + nu;
+      gb::gather<double>(H, F, v, block, gb::EPI_BT, ga, gb::OPK_STOKES);
+    }
+    gb::to_caller(H, top, y, a, true, true);
+    std::vector<double> corr(n);
+    GB_CUDA(cudaMemcpyAsync(corr.data(), a, n * sizeof(double), cudaMemcpyDeviceToHost, H.st));
+    GB_CUDA(cudaStreamSynchronize(H.st));
+    for (long i = 0; i < n; ++i) rhs[i] -= corr[i];
+  })
+}
+
 int gb_gmg_vmult(gb_gmg* g, int op, int level, int precision, const double* src, double* dst) {
   if (!g) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {

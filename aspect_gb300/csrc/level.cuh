@@ -87,6 +87,7 @@ struct Level {
   // device data
   DevBuf<int> cdu_d, cdp_d, lptr_d, lcol_d, plptr_d, plcol_d;
   DevBuf<int> perm_u_d, perm_p_d, cons_u_d, cons_p_d;
+  DevBuf<int> cdu_raw_d, cdp_raw_d;  // internal cells x internal DoFs, no constraint codes (plain reads)
   DevBuf<int> probe_ptr, probe_g, probe_eptr, probe_li;
   DevBuf<int> pprobe_ptr, pprobe_g, pprobe_eptr, pprobe_li;
   DevBuf<int> Pu_ptr, Pu_col, PuT_ptr, PuT_col, Pp_ptr, Pp_col, PpT_ptr, PpT_col;

@@ -187,6 +187,17 @@ int gb_gmg_build_preconditioner(gb_gmg* h);
  * Constrained rows act as the identity (MatrixFreeOperators::Base::vmult). */
 int gb_gmg_vmult(gb_gmg* h, int op, int level, int precision, const double* src, double* dst);
 
+/* StokesMatrixFreeHandler::correct_stokes_rhs
+   (source/simulator/solver/stokes_matrix_free_local_smoothing.cc:618-754): rhs -= K u0
+   on the finest level, where u0 (caller numbering, velocity then pressure) holds the
+   inhomogeneous constraint values at constrained DoFs (what AffineConstraints::
+   distribute gives on a zero vector) and zeros elsewhere. K is applied with plain
+   reads of u0, contributions are distributed through the constraints, and
+   constrained rows of rhs are left unchanged. Host arrays of n_u + n_p doubles.
+   The solve then runs with homogeneous constraints; the caller adds u0 (distributes
+   the constraints) afterwards, as the reference does. */
+int gb_gmg_correct_stokes_rhs(gb_gmg* h, const double* u0, double* rhs);
+
 /* Same, on device arrays of the finest level in the caller's numbering. */
 int gb_gmg_vmult_device(gb_gmg* h, int op, int precision, const double* d_src, double* d_dst);
 
