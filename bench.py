@@ -127,6 +127,22 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+def job_throughput(seconds_local: float, units_per_rank: float, device=None) -> tuple[float, float]:
+    """Whole-job figures of N replicas: the timed seconds are the maximum over
+    ranks (an all_reduce MAX when a process group is up, on `device`: a CUDA
+    device under NCCL, the CPU under gloo) and the throughput is the units all
+    ranks processed divided by that time. Returns (seconds, units per second)."""
+    import torch
+    import torch.distributed as dist
+    world = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    t = float(seconds_local)
+    if world > 1:
+        tt = torch.tensor([t], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    return t, world * units_per_rank / t
+
+
 def build_problem():
     from aspect_gb300 import problems
     return problems.sinkers_3d(N_CELLS_1D)
@@ -262,13 +278,9 @@ def run_gpu(args):
         wall = time.perf_counter() - wall0
     torch.cuda.profiler.stop()
     launches = g.kernel_launches() - launches0
-    t_sum = sum(step_s)
     log("timed solves", step_s)
-    if world > 1:
-        tt = torch.tensor([t_sum], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_sum = float(tt.item())
-    value = world * args.steps * n / t_sum / 1e6
+    t_sum, value = job_throughput(sum(step_s), args.steps * n, dev)
+    value /= 1e6
     mixed = outs[-1]
 
     # --- end to end through the host-array ABI (pinned host buffers)
