@@ -10,6 +10,7 @@ preconditioner and an FP32 V-cycle, FP64 outer residual, relative tolerance 1e-8
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
     python bench.py --profile-op a_cell_pass_fp32|stokes_cell_pass_fp64|stokes_vmult_fp64|mass_vmult_fp32|a_vmult_fp32
     python bench.py --sweep 32,64      (operator timings per size, no solve)
+    python bench.py --configs solcx64,sphere16,adjoint32,shell3   (FP64-MG vs FP32-MG per workload)
 
 (--profile-op runs one operation of the workload three times between
 cudaProfilerStart/Stop, for `ncu --profile-from-start off` captures.)
@@ -455,7 +456,7 @@ def run_profile_op(name: str):
 def run_sweep(sizes):
     """Operator timings of the sinker workload at several sizes (no solve): at 32^3
     every operand is L2-resident, at 64^3 the FP32 A-block vmult's working set
-    (vectors, viscosity, per-cell outputs: ~165 MB) exceeds the 126 MB L2, so
+    (vectors, viscosity, per-cell outputs: ~165 MB) exceeds the 129 MB L2, so
     its HBM fraction starts to mean something. One JSON line per size."""
     import torch
     from aspect_gb300 import gmg, problems
@@ -490,6 +491,82 @@ def run_sweep(sizes):
         del g
 
 
+def _solve_pair(P, options=None, project=None):
+    """FP64-MG and FP32-MG solves of one workload (each timed after a warm-up solve)."""
+    from aspect_gb300 import gmg
+    t0 = time.perf_counter()
+    g = gmg.from_problem(P, options)
+    setup = time.perf_counter() - t0
+    res = {}
+    for key, prec in (("fp64_mg", gmg.FP64), ("fp32_mg", gmg.FP32)):
+        g.solve(P.rhs, linear_solver_tolerance=TOL, mg_precision=prec)  # warm
+        x, o = g.solve(P.rhs, linear_solver_tolerance=TOL, mg_precision=prec)
+        res[key] = {"solve_s": o["solve_seconds"], "iterations": o["cheap_iterations"] + o["expensive_iterations"],
+                    "status": o["status"], "x": x}
+    f = P.fine
+    u64, u32 = res["fp64_mg"]["x"][: f.n_u], res["fp32_mg"]["x"][: f.n_u]
+    if project is not None:
+        u64, u32 = project(u64), project(u32)
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    line = {"workload": P.name, "cells": f.n_cells, "n_u": f.n_u, "n_p": f.n_p, "setup_s": setup,
+            "delta_iterations": res["fp32_mg"]["iterations"] - res["fp64_mg"]["iterations"],
+            "speedup_fp32_mg": res["fp64_mg"]["solve_s"] / res["fp32_mg"]["solve_s"],
+            "velocity_rel_l2_fp32_vs_fp64": rel(u32, u64),
+            "pressure_rel_l2_fp32_vs_fp64": rel(res["fp32_mg"]["x"][f.n_u:], res["fp64_mg"]["x"][f.n_u:])}
+    for key in ("fp64_mg", "fp32_mg"):
+        line[key] = {k: v for k, v in res[key].items() if k != "x"}
+    return line
+
+
+def _config_line(name):
+    import torch
+    from aspect_gb300 import adjoint, gmg, problems, shell
+    if name == "solcx64":
+        return _solve_pair(problems.solcx(6, density_sign=1.0))
+    if name == "sphere16":
+        return _solve_pair(problems.adaptive_sphere(4, 2))
+    if name == "shell3":
+        P = problems.spherical_shell(3)
+        q, _ = np.linalg.qr(shell.rotation_modes(P.fine).T)
+        return _solve_pair(P, {"coarse_solver": gmg.COARSE_DENSE_FP64}, lambda u: u - q @ (q.T @ u))
+    if name == "adjoint32":
+        def factory(base):
+            g = gmg.StokesMatrixFreeGPU(3, len(base.levels))
+            g.setup_dofs(base.levels)
+            return g
+        ap, ev = adjoint.make_problem(32, factory, tol=1e-8)
+        ev.gradient(ap.lneta)  # warm
+        t0 = time.perf_counter()
+        J, _, _, _ = ev.gradient(ap.lneta)
+        torch.cuda.synchronize()
+        return {"workload": "adjoint_gradient_32^3", "cells": len(ap.lneta), "J": J,
+                "seconds_forward_adjoint_backward": time.perf_counter() - t0,
+                "note": "viscosity tables and preconditioner rebuilt for the evaluation point, then forward "
+                        "and adjoint FP32-MG/FP64 solves to 1e-8 and the backward kernel; host wall time"}
+    raise ValueError(f"unknown workload {name}")
+
+
+def run_configs(names):
+    """FP64-MG against FP32-MG (FP64 FGMRES) solves to 1e-8 on the other
+    workloads: 2D 64^2 SolCx-like (eta jump 1e6), 3D 16^3 + 2 adaptive levels
+    around a sphere, the spherical shell at refinement 3 (FP64 dense coarse
+    solve), and the adjoint gradient on 32^3 (forward + adjoint solve + backward
+    kernel). One JSON line per workload, written as each finishes. Velocity
+    differences on the shell are taken after removing the rigid rotations (its
+    null space under free slip)."""
+    import torch
+    torch.cuda.init()
+    for name in names:
+        try:
+            line = _config_line(name)
+        except Exception as e:  # report it and go on with the next workload
+            line = {"workload": name, "error": f"{type(e).__name__}: {e}"}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -498,8 +575,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--profile-op", default=None, choices=sorted(PROFILE_OPS))
     ap.add_argument("--sweep", default=None, help="comma-separated cells per direction, e.g. 32,64")
+    ap.add_argument("--configs", default=None, help="comma-separated: solcx64,sphere16,adjoint32,shell3")
     args = ap.parse_args()
-    if args.sweep:
+    if args.configs:
+        run_configs(args.configs.split(","))
+    elif args.sweep:
         run_sweep([int(v) for v in args.sweep.split(",")])
     elif args.profile_op:
         run_profile_op(args.profile_op)
