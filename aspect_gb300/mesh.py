@@ -152,14 +152,15 @@ def _lex(idx: tuple, shape: tuple) -> int:
 
 
 def box_level(dim: int, ncells: tuple, extent: tuple, origin: tuple | None = None,
-              free_slip: bool = True) -> LevelMesh:
+              free_slip: bool = True, no_slip: bool = False) -> LevelMesh:
     """Uniform axis-aligned box with lexicographic cells, component-blocked
     Q2 velocity numbering and lexicographic Q1 pressure numbering.
 
     ``free_slip``: no-normal-flux on every face (the normal component is a
     Dirichlet-zero line), as ``Tangential velocity boundary indicators`` gives
     on a box (VectorTools::compute_no_normal_flux_constraints on axis-aligned
-    faces)."""
+    faces). ``no_slip``: every component is zero on every face, as ``Zero
+    velocity boundary indicators`` on all faces gives."""
     origin = origin or (0.0,) * dim
     ncells = tuple(ncells)
     h = tuple(extent[d] / ncells[d] for d in range(dim))
@@ -196,7 +197,14 @@ def box_level(dim: int, ncells: tuple, extent: tuple, origin: tuple | None = Non
     pts_p = np.array([origin[d] + pidx[:, d] * h[d] for d in range(dim)]).T
 
     lines = {}
-    if free_slip:
+    if no_slip:
+        on_bnd = np.zeros(n_nodes, bool)
+        for d in range(dim):
+            on_bnd |= (nidx[:, d] == 0) | (nidx[:, d] == nn[d] - 1)
+        for c in range(dim):
+            for nd in np.nonzero(on_bnd)[0]:
+                lines[int(nd + c * n_nodes)] = ([], 0.0)
+    elif free_slip:
         for c in range(dim):
             on_face = (nidx[:, c] == 0) | (nidx[:, c] == nn[c] - 1)
             for nd in np.nonzero(on_face)[0]:
@@ -212,14 +220,14 @@ def box_level(dim: int, ncells: tuple, extent: tuple, origin: tuple | None = Non
 
 
 def box_hierarchy(dim: int, n_fine: int, extent=None, n_coarse: int = 1,
-                  free_slip: bool = True) -> list[LevelMesh]:
+                  free_slip: bool = True, no_slip: bool = False) -> list[LevelMesh]:
     """Global-coarsening hierarchy of uniform boxes: level l has n_coarse*2**l
     cells per direction, up to n_fine on the finest level."""
     extent = tuple(extent or (1.0,) * dim)
     levels = []
     n = n_coarse
     while n <= n_fine:
-        levels.append(box_level(dim, (n,) * dim, extent, free_slip=free_slip))
+        levels.append(box_level(dim, (n,) * dim, extent, free_slip=free_slip, no_slip=no_slip))
         n *= 2
     assert levels and n // 2 == n_fine, "n_fine must be n_coarse * 2**k"
     for l in range(1, len(levels)):

@@ -104,8 +104,13 @@ def pressure_scaling(level: LevelMesh, eta_mid: np.ndarray, length_scale: float)
     return float(np.exp(np.sum(np.log(eta_mid) * vol) / np.sum(vol)) / length_scale)
 
 
-def harmonic_average(eta_q: np.ndarray, jxw: np.ndarray) -> np.ndarray:
-    return np.sum(jxw, 1) / np.sum(jxw / eta_q, 1)
+def harmonic_average(eta_q: np.ndarray) -> np.ndarray:
+    """Cellwise harmonic average over the quadrature points, unweighted as
+    MaterialAveraging computes it (source/material_model/interface.cc:576-595:
+    N / sum 1/eta_q, zero if any value is zero)."""
+    with np.errstate(divide="ignore"):
+        avg = eta_q.shape[1] / np.sum(1.0 / eta_q, 1)
+    return np.where(np.any(eta_q == 0.0, 1), 0.0, avg)
 
 
 def normalize_pressure_surface(level: LevelMesh, p: np.ndarray, top: float = 1.0) -> float:
@@ -180,7 +185,7 @@ def solcx(n_refinements: int, eta_B: float = 1e6, density_sign: float = -1.0,
     fine = levels[-1]
     xq, jxw = q_points_real(fine)
     eta_q = np.where(xq[..., 0] < 0.5, 1.0, eta_B)
-    eta = harmonic_average(eta_q, jxw)
+    eta = harmonic_average(eta_q)
     rho = density_sign * np.sin(np.pi * xq[..., 1]) * np.cos(np.pi * xq[..., 0])
     force = np.zeros(xq.shape)
     force[..., 1] = -rho
@@ -188,6 +193,36 @@ def solcx(n_refinements: int, eta_B: float = 1e6, density_sign: float = -1.0,
     mid = fine.map_points(np.full((1, 2), 0.5))[:, 0, :]
     s = pressure_scaling(fine, np.where(mid[:, 0] < 0.5, 1.0, eta_B), 0.01 * 1.0)
     return StokesProblem(name or f"solcx_{n}x{n}", levels, eta, 0, s, rhs, 1)
+
+
+def nsinker(n_refinements: int, centres: np.ndarray, dynamic_viscosity_ratio: float = 1e4,
+            sinker_density: float = 10.0, delta: float = 200.0, omega: float = 0.1) -> StokesProblem:
+    """The reference's NSinker benchmark material on the unit cube
+    (benchmarks/nsinker/nsinker.cc:61-76 evaluate, :280-313 inside_outside_factor;
+    parameters of benchmarks/nsinker/nsinker_gmg.prm): with chi the product over
+    the sinkers of 1 - exp(-delta max(0, |x - c| - omega/2)^2),
+    eta = (sqrt(r) - 1/sqrt(r)) (1 - chi) + 1/sqrt(r) for the viscosity ratio r and
+    rho = sinker_density (1 - chi), per quadrature point; eta harmonically averaged
+    per cell ("harmonic average only viscosity"), rho not averaged; gravity -z of
+    magnitude 1; zero velocity on all six faces; pressure scaling 1 (the benchmark
+    overrides it, nsinker.cc:320-331). The sinker centres are data of the
+    benchmark, passed in by the caller."""
+    n = 2 ** n_refinements
+    levels = box_hierarchy(3, n, no_slip=True)
+    fine = levels[-1]
+    xq, jxw = q_points_real(fine)
+    chi = np.ones(xq.shape[:-1])
+    for c in np.asarray(centres, float):
+        dist = np.linalg.norm(xq - c, axis=-1)
+        chi *= 1.0 - np.exp(-delta * np.maximum(0.0, dist - omega / 2.0) ** 2)
+    sr = math.sqrt(dynamic_viscosity_ratio)
+    eta_q = (sr - 1.0 / sr) * (1.0 - chi) + 1.0 / sr
+    rho = sinker_density * (1.0 - chi)
+    force = np.zeros(xq.shape)
+    force[..., 2] = -rho
+    rhs = assemble_rhs(fine, force)
+    return StokesProblem(f"nsinker_{n}^3", levels, harmonic_average(eta_q), 0, 1.0, rhs, 2,
+                         extra=dict(eta_q=eta_q))
 
 
 def sinker_centres(seed: int, n: int = 8) -> np.ndarray:
@@ -226,7 +261,7 @@ def sinkers_3d(n: int = 32, seed: int = BASE_SEED + 2, projection: int = 1,
     centres = sinker_centres(seed)
     xq, jxw = q_points_real(fine)
     eta_q = sinker_viscosity(xq, centres)
-    eta = eta_q if projection == 1 else harmonic_average(eta_q, jxw)
+    eta = eta_q if projection == 1 else harmonic_average(eta_q)
     rho = sinker_density(xq, centres)
     force = np.zeros(xq.shape)
     force[..., 2] = -rho

@@ -103,3 +103,28 @@ def test_oracle_transfer_is_exact_embedding(dim):
     lhs = b @ o.transfer(len(levels) - 1, 0, False, a)
     rhs = a @ o.transfer(len(levels) - 1, 0, True, b)
     assert abs(lhs - rhs) < 1e-12 * abs(lhs)
+
+
+@pytest.mark.parametrize("key,krylov", [("gmres", 0), ("idr2", 2)])
+def test_nsinker_matches_reference_outputs(key, krylov):
+    """The reference's NSinker benchmark on its 4^3 test mesh (3D, zero velocity on
+    all faces, 4 sinkers, viscosity ratio 1e4, harmonic averaging of viscosity
+    only, pressure scaling 1, tolerance 1e-6): the oracle prints the viscosity
+    range, DoF counts, iteration counts and Schur-preconditioner applications of
+    tests/nsinker_gmg_gc/screen-output (GMRES: 21, 22) and
+    tests/nsinker_gmg_idr/screen-output (IDR(2): 9, 25)."""
+    G = json.load(open(os.path.join(GOLDEN, "nsinker_golden.json")))
+    ref = G[key]
+    P = problems.nsinker(2, G["centres"], G["dynamic_viscosity_ratio"], G["sinker_density"], G["delta"],
+                         G["omega"])
+    f = P.fine
+    assert (f.n_u, f.n_p) == (ref["n_u"], ref["n_p"])
+    np.testing.assert_allclose([P.eta.min(), P.eta.max()], ref["viscosity_range"], rtol=5e-6)
+    o = Oracle(P.levels)
+    o.set_viscosity(P.eta, P.projection, P.pressure_scaling)
+    o.build_preconditioner(False)
+    _, info = o.solve(P.rhs, tol_rel=G["linear_solver_tolerance"], n_cheap=G["n_cheap_steps"], n_expensive=0,
+                      restart=G["restart"], krylov=krylov, idr_s=2)
+    assert info["status"] == 0
+    assert info["cheap_iterations"] == ref["cheap_iterations"]
+    assert info["S_preconditioner_applications"] == ref["schur_applications"]
