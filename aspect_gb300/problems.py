@@ -196,7 +196,8 @@ def solcx(n_refinements: int, eta_B: float = 1e6, density_sign: float = -1.0,
 
 
 def nsinker(n_refinements: int, centres: np.ndarray, dynamic_viscosity_ratio: float = 1e4,
-            sinker_density: float = 10.0, delta: float = 200.0, omega: float = 0.1) -> StokesProblem:
+            sinker_density: float = 10.0, delta: float = 200.0, omega: float = 0.1,
+            averaging: str = "harmonic") -> StokesProblem:
     """The reference's NSinker benchmark material on the unit cube
     (benchmarks/nsinker/nsinker.cc:61-76 evaluate, :280-313 inside_outside_factor;
     parameters of benchmarks/nsinker/nsinker_gmg.prm): with chi the product over
@@ -206,7 +207,10 @@ def nsinker(n_refinements: int, centres: np.ndarray, dynamic_viscosity_ratio: fl
     per cell ("harmonic average only viscosity"), rho not averaged; gravity -z of
     magnitude 1; zero velocity on all six faces; pressure scaling 1 (the benchmark
     overrides it, nsinker.cc:320-331). The sinker centres are data of the
-    benchmark, passed in by the caller."""
+    benchmark, passed in by the caller. averaging = "none": the viscosity stays
+    per quadrature point on the finest level and the level tables are the
+    cellwise (DGQ0) projection, as the reference does without averaging
+    (matrix_free_operators.cc:137-330, stokes_matrix_free_local_smoothing.cc:104-116)."""
     n = 2 ** n_refinements
     levels = box_hierarchy(3, n, no_slip=True)
     fine = levels[-1]
@@ -221,8 +225,8 @@ def nsinker(n_refinements: int, centres: np.ndarray, dynamic_viscosity_ratio: fl
     force = np.zeros(xq.shape)
     force[..., 2] = -rho
     rhs = assemble_rhs(fine, force)
-    return StokesProblem(f"nsinker_{n}^3", levels, harmonic_average(eta_q), 0, 1.0, rhs, 2,
-                         extra=dict(eta_q=eta_q))
+    eta = eta_q if averaging == "none" else harmonic_average(eta_q)
+    return StokesProblem(f"nsinker_{n}^3", levels, eta, 0, 1.0, rhs, 2, extra=dict(eta_q=eta_q))
 
 
 def sinker_centres(seed: int, n: int = 8) -> np.ndarray:

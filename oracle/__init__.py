@@ -102,11 +102,16 @@ class Oracle:
     def fine(self):
         return self.levels[-1]
 
-    def set_viscosity(self, eta, projection: int, pressure_scaling: float, compressible: int = 0):
+    def set_viscosity(self, eta, projection: int, pressure_scaling: float, compressible: int = 0,
+                      mg_finest_projected: bool = False):
+        """mg_finest_projected (per-point eta, projection 0): the multigrid levels,
+        the finest included, use the cellwise projection while the outer operators
+        keep the per-point values, as the reference does without averaging."""
         eta = _d(eta)
         n_per_cell = eta.size // self.fine.n_cells
         self._chk(self.L.orc_set_viscosity(self.h, _ptr(eta, _dp), n_per_cell, projection,
-                                           ctypes.c_double(pressure_scaling), compressible))
+                                           ctypes.c_double(pressure_scaling), compressible,
+                                           int(mg_finest_projected)))
 
     def level_viscosity(self, level: int) -> np.ndarray:
         m = self.levels[level]

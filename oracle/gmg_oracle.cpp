@@ -554,8 +554,32 @@ struct Oracle {
   // -------- viscosity on levels (stokes_matrix_free_local_smoothing.cc:174-294)
   // Input: raw material-model values on the finest level, per cell (1 value,
   // already averaged: DGQ0) or per quadrature point (projection = 1: DGQ1).
-  void set_viscosity(const double* eta_in, int n_per_cell, int proj, double s_in, int comp) {
+  // mg_finest_projected (per-point input with DGQ0 only): the multigrid levels,
+  // the finest included, take the DGQ0 projection while the outer operators keep
+  // the per-point values -- what the reference does without averaging
+  // (stokes_matrix_free_local_smoothing.cc:211-294 fills level_cell_data for every
+  // level from the projected vector; matrix_free_operators.cc:137-330 keeps the raw
+  // values in active_cell_data for the outer operators).
+  std::vector<double> active_eta;
+  int active_eta_n = 0;
+  struct ActiveTable {  // swaps the outer-operator table into the finest level for one call
+    Oracle& o;
+    bool on;
+    explicit ActiveTable(Oracle& o_) : o(o_), on(!o_.active_eta.empty()) { swap(); }
+    ~ActiveTable() { swap(); }
+    void swap() {
+      if (!on) return;
+      Level& F = o.levels.back();
+      std::swap(F.eta, o.active_eta);
+      std::swap(F.eta_n, o.active_eta_n);
+    }
+  };
+
+  void set_viscosity(const double* eta_in, int n_per_cell, int proj, double s_in, int comp,
+                     bool mg_finest_projected = false) {
     s = s_in; compressible = comp; projection = proj;
+    active_eta.clear();
+    active_eta_n = 0;
     const int nq = fe.nq, nc_v = dim == 3 ? 8 : 4;
     const int nlev = (int)levels.size();
     // DG coefficient fields per level: DGQ0 -> 1 value, DGQ1 -> vertex values
@@ -583,9 +607,13 @@ struct Oracle {
         dg[l - 1].resize(levels[l - 1].n_cells);
         for (size_t c = 0; c < sum.size(); ++c) dg[l - 1][c] = sum[c] / cnt[c];
       }
+      if (mg_finest_projected && n_per_cell == nq) {
+        active_eta.assign(eta_in, eta_in + (size_t)Fl.n_cells * nq);
+        active_eta_n = nq;
+      }
       for (int l = 0; l < nlev; ++l) {
         Level& L = levels[l];
-        bool active_per_q = (l == nlev - 1 && n_per_cell == nq);
+        bool active_per_q = (l == nlev - 1 && n_per_cell == nq && !mg_finest_projected);
         L.eta_n = active_per_q ? nq : 1;
         L.eta.assign((size_t)L.n_cells * L.eta_n, 0);
         for (int c = 0; c < L.n_cells; ++c) {
@@ -872,16 +900,20 @@ struct Oracle {
 
   // -------- outer (FP64) operators on the finest level
   void stokes_vmult(const double* x, double* y) {
+    ActiveTable at(*this);
     Level& F = fine();
     apply<double>((int)levels.size() - 1, OP_STOKES, x, x + F.n_u, y, y + F.n_u, F.eta.data());
   }
   void a_vmult(const double* x, double* y) {
+    ActiveTable at(*this);
     apply<double>((int)levels.size() - 1, OP_A, x, nullptr, y, nullptr, fine().eta.data());
   }
   void mass_vmult(const double* x, double* y) {
+    ActiveTable at(*this);
     apply<double>((int)levels.size() - 1, OP_MASS, nullptr, x, nullptr, y, fine().eta.data());
   }
   void bt_vmult(const double* xp, double* yu) {
+    ActiveTable at(*this);
     apply<double>((int)levels.size() - 1, OP_BT, nullptr, xp, yu, nullptr, fine().eta.data());
   }
 
@@ -1278,9 +1310,10 @@ int orc_finalize(void* p) {
     for (int l = 1; l < (int)h->levels.size(); ++l) h->build_transfer(l);
   })
 }
-int orc_set_viscosity(void* p, const double* eta, int n_per_cell, int projection, double s, int compressible) {
+int orc_set_viscosity(void* p, const double* eta, int n_per_cell, int projection, double s, int compressible,
+                      int mg_finest_projected) {
   Oracle* h = (Oracle*)p;
-  GUARD(h->set_viscosity(eta, n_per_cell, projection, s, compressible))
+  GUARD(h->set_viscosity(eta, n_per_cell, projection, s, compressible, mg_finest_projected != 0))
 }
 int orc_get_level_viscosity(void* p, int lev, double* out, int* n_per_cell) {
   Oracle* h = (Oracle*)p;

@@ -6,9 +6,9 @@ It reads the NSinker benchmark's input data from the reference -- the number of
 sinkers and the viscosity ratio of benchmarks/nsinker/nsinker_gmg.prm, the
 sinker density default, delta, omega and the first n_sinkers sinker centres of
 benchmarks/nsinker/nsinker.cc -- and the solver outputs the reference committed
-for two of its tests on the 4^3 mesh: tests/nsinker_gmg_gc/screen-output (the
-first solve, GMRES, before the adaptive step) and
-tests/nsinker_gmg_idr/screen-output (IDR(2)).
+for three of its tests on the 4^3 mesh: tests/nsinker_gmg_gc/screen-output (the
+first solve, GMRES, before the adaptive step), tests/nsinker_gmg_idr/screen-output
+(IDR(2)) and tests/nsinker_gmg_no_avg/screen-output (GMRES, no averaging).
 """
 import json
 import os
@@ -38,7 +38,7 @@ def main():
                   linear_solver_tolerance=float(prm_value(prm, "Linear solver tolerance")),
                   n_cheap_steps=int(prm_value(prm, "Number of cheap Stokes solver steps")),
                   restart=int(prm_value(prm, "GMRES solver restart length")))
-    for test, key in (("nsinker_gmg_gc", "gmres"), ("nsinker_gmg_idr", "idr2")):
+    for test, key in (("nsinker_gmg_gc", "gmres"), ("nsinker_gmg_idr", "idr2"), ("nsinker_gmg_no_avg", "no_avg")):
         txt = open(os.path.join(REF, "tests", test, "screen-output")).read()
         its = re.search(r"Stokes solver \((GMRES|IDR\(\d+\))\): (\d+)\+(\d+) iterations", txt)
         schur = re.search(r"Schur complement preconditioner: (\d+)\+(\d+) iterations", txt)
