@@ -1443,6 +1443,10 @@ int gb_gmg_finalize_setup(gb_gmg* g) {
     H.reset_graphs();
     H.restart_alloc = -1;  // Krylov and IDR(s) blocks are sized by the finest level: rebuilt on next use
     H.idr_s_alloc = 0;
+    for (auto& L : H.levels) {  // raw cell-DoF tables of correct_stokes_rhs follow the new numbering
+      L.cdu_raw_d.release();
+      L.cdp_raw_d.release();
+    }
     H.setup_done = true;
     H.visc_done = false;
     H.prec_done[0] = H.prec_done[1] = false;
