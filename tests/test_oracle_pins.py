@@ -38,6 +38,30 @@ def test_solcx_matches_reference_regression(nref):
     np.testing.assert_allclose(errs, golden["errors"], rtol=2e-6)
 
 
+def test_solcx_without_averaging_matches_reference_regression():
+    """sol_cx_4_gmg_no_avg: no material averaging (per-point viscosity for the
+    outer operators, the cellwise projection on every multigrid level, as the
+    reference arranges it): the same 15 iterations and error norms as with
+    averaging, since the viscosity jump lies on cell faces."""
+    golden = json.load(open(os.path.join(GOLDEN, "solcx_golden.json")))["16_no_avg"]
+    exact = np.load(os.path.join(GOLDEN, "solcx_exact.npz"))
+    P = problems.solcx(4)
+    f = P.fine
+    xq, _ = problems.q_points_real(f)
+    eta_q = np.where(xq[..., 0] < 0.5, 1.0, 1e6)
+    o = Oracle(P.levels)
+    o.set_viscosity(eta_q, 0, P.pressure_scaling, mg_finest_projected=True)
+    o.build_preconditioner(False)
+    x, info = o.solve(P.rhs, tol_rel=1e-7)
+    assert info["status"] == 0 and info["cheap_iterations"] == golden["cheap_iterations"]
+    u = x[: f.n_u].copy()
+    p = x[f.n_u:] * P.pressure_scaling
+    f.constraints_u.distribute(u)
+    problems.normalize_pressure_surface(f, p)
+    errs = problems.error_norms(f, u, p, exact["u_16"], exact["p_16"])
+    np.testing.assert_allclose(errs, golden["errors"], rtol=2e-6)
+
+
 def _small_problem(dim, n, per_q, seed=3):
     levels = mesh.box_hierarchy(dim, n)
     f = levels[-1]
