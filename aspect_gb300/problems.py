@@ -175,11 +175,14 @@ def error_norms(level: LevelMesh, u, p, exact_u_q, exact_p_q, n1d: int = 4):
 
 # --------------------------------------------------------------------- problems
 def solcx(n_refinements: int, eta_B: float = 1e6, density_sign: float = -1.0,
-          name: str | None = None) -> StokesProblem:
+          name: str | None = None, average_density: bool = False) -> StokesProblem:
     """SolCx (benchmarks/solcx/solcx.h:2953-2975): eta = 1 for x < 1/2 and eta_B
     otherwise, rho = density_sign * sin(pi y) cos(pi x), g = (0, -1), free slip on
     all walls, harmonic averaging (constant per cell here). density_sign = -1 is
-    the reference benchmark; +1 is the variant of the 64x64 workload."""
+    the reference benchmark; +1 is the variant of the 64x64 workload.
+    average_density: the density is harmonically averaged per cell too (the
+    reference's "harmonic average" as opposed to "harmonic average only
+    viscosity")."""
     n = 2 ** n_refinements
     levels = box_hierarchy(2, n)
     fine = levels[-1]
@@ -187,6 +190,8 @@ def solcx(n_refinements: int, eta_B: float = 1e6, density_sign: float = -1.0,
     eta_q = np.where(xq[..., 0] < 0.5, 1.0, eta_B)
     eta = harmonic_average(eta_q)
     rho = density_sign * np.sin(np.pi * xq[..., 1]) * np.cos(np.pi * xq[..., 0])
+    if average_density:
+        rho = np.repeat(harmonic_average(rho)[:, None], rho.shape[1], 1)
     force = np.zeros(xq.shape)
     force[..., 1] = -rho
     rhs = assemble_rhs(fine, force)

@@ -6,7 +6,8 @@ It builds the reference's own SolCx analytic solution (oracle/ref_build.sh ->
 oracle/_ref/libsolcx.so), evaluates it at the QGauss(4) points of the 4x4 and
 16x16 meshes the reference tests use, and records the numbers printed in the
 reference's committed outputs tests/sol_cx_{2,4}_gmg/screen-output and
-tests/sol_cx_4_gmg_no_avg/screen-output (no material averaging).
+tests/sol_cx_4_gmg_no_avg/screen-output (no material averaging) and
+tests/no_cheap_gmg/screen-output (expensive solver only, density averaged too).
 """
 import ctypes
 import json
@@ -51,7 +52,8 @@ def main():
         out[f"p_{n}"] = p.reshape(f.n_cells, -1)
     np.savez_compressed(os.path.join(HERE, "solcx_exact.npz"), **out)
     golden = {}
-    for test, n in (("sol_cx_2_gmg", 4), ("sol_cx_4_gmg", 16), ("sol_cx_4_gmg_no_avg", "16_no_avg")):
+    for test, n in (("sol_cx_2_gmg", 4), ("sol_cx_4_gmg", 16), ("sol_cx_4_gmg_no_avg", "16_no_avg"),
+                    ("no_cheap_gmg", "16_no_cheap")):
         txt = open(os.path.join(REF, "tests", test, "screen-output")).read()
         its = re.search(r"Solving Stokes system \(GMG\)\.\.\. (\d+)\+(\d+) iterations", txt)
         errs = re.search(r"Errors u_L1, p_L1, u_L2, p_L2: ([^\n]+)", txt).group(1)

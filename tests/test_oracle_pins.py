@@ -62,6 +62,31 @@ def test_solcx_without_averaging_matches_reference_regression():
     np.testing.assert_allclose(errs, golden["errors"], rtol=2e-6)
 
 
+def test_expensive_solver_matches_reference_regression():
+    """no_cheap_gmg: SolCx 16x16 with no cheap steps (FGMRES with the expensive
+    block preconditioner: CG on the velocity block to 1e-2 and on the Schur
+    approximation to 1e-6, V-cycles as their preconditioners) and "harmonic
+    average" of density as well as viscosity: 0+12 iterations and the four
+    error norms the reference prints."""
+    golden = json.load(open(os.path.join(GOLDEN, "solcx_golden.json")))["16_no_cheap"]
+    exact = np.load(os.path.join(GOLDEN, "solcx_exact.npz"))
+    P = problems.solcx(4, average_density=True)
+    f = P.fine
+    o = Oracle(P.levels)
+    o.set_viscosity(P.eta, P.projection, P.pressure_scaling)
+    o.build_preconditioner(False)
+    x, info = o.solve(P.rhs, tol_rel=1e-7, n_cheap=0)
+    assert info["status"] == 0
+    assert (info["cheap_iterations"], info["expensive_iterations"]) == (golden["cheap_iterations"],
+                                                                        golden["expensive_iterations"])
+    u = x[: f.n_u].copy()
+    p = x[f.n_u:] * P.pressure_scaling
+    f.constraints_u.distribute(u)
+    problems.normalize_pressure_surface(f, p)
+    errs = problems.error_norms(f, u, p, exact["u_16"], exact["p_16"])
+    np.testing.assert_allclose(errs, golden["errors"], rtol=2e-6)
+
+
 def _small_problem(dim, n, per_q, seed=3):
     levels = mesh.box_hierarchy(dim, n)
     f = levels[-1]
