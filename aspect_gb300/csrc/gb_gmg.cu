@@ -43,6 +43,7 @@ struct Handle {
   std::string err;
   double s = 1.0;
   int compressible = 0, projection = 0;
+  int visc_n_per_cell = 0;  // n_per_cell of the last successful set_viscosity
   double eta_min = 0, eta_max = 0;
   bool setup_done = false, visc_done = false;
   bool prec_done[2] = {false, false};  // per precision (0 fp64, 1 fp32)
@@ -1464,7 +1465,9 @@ int gb_gmg_set_viscosity(gb_gmg* g, const double* eta, int n_per_cell, int proje
     H.s = s;
     H.compressible = compressible;
     H.projection = projection;
+    H.visc_done = false;
     gb::compute_level_viscosity(H.levels, eta, n_per_cell, projection, H.eta_min, H.eta_max);
+    H.visc_n_per_cell = n_per_cell;
     for (auto& L : H.levels) gb::upload_viscosity(L, s);
     H.reset_graphs();
     H.visc_done = true;
@@ -1477,14 +1480,31 @@ int gb_gmg_update_viscosity(gb_gmg* g, const double* eta, int n_per_cell) {
   ABI_TRY(g, {
     Handle& H = g->h;
     GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
-    const int nq = H.dim == 3 ? 27 : 9;
-    GB_CHECK(n_per_cell == 1 || n_per_cell == nq, 1, "n_per_cell must be 1 or 3^dim");
-    double mn, mx;
-    gb::compute_level_viscosity(H.levels, eta, n_per_cell, H.projection, mn, mx);
+    GB_CHECK(eta, 1, "null viscosity");
+    // The device tables, the level views built from Level::eta_n and the captured
+    // V-cycles all assume the layout of the last set_viscosity: a different one
+    // is rejected before anything changes.
+    GB_CHECK(n_per_cell == H.visc_n_per_cell, 1, "viscosity layout differs from the last set_viscosity");
+    std::vector<std::vector<double>> saved_eta;
+    std::vector<int> saved_n;
     for (auto& L : H.levels) {
-      GB_CHECK(L.eta.size() == L.f64.eta.n, 1, "viscosity layout differs from the last set_viscosity");
-      gb::upload_viscosity(L, H.s);  // same sizes: device addresses (and captured graphs) stay valid
+      saved_eta.push_back(L.eta);
+      saved_n.push_back(L.eta_n);
     }
+    double mn, mx;
+    try {
+      gb::compute_level_viscosity(H.levels, eta, n_per_cell, H.projection, mn, mx);
+      for (auto& L : H.levels)
+        GB_CHECK(L.eta.size() == L.f64.eta.n, 1, "viscosity layout differs from the last set_viscosity");
+    } catch (...) {
+      for (size_t l = 0; l < H.levels.size(); ++l) {
+        H.levels[l].eta = std::move(saved_eta[l]);
+        H.levels[l].eta_n = saved_n[l];
+      }
+      throw;
+    }
+    // same sizes on every level: device addresses (and captured graphs) stay valid
+    for (auto& L : H.levels) gb::upload_viscosity(L, H.s);
     H.eta_min = mn;
     H.eta_max = mx;
   })

@@ -16,7 +16,11 @@
  *    across the ABI. gb_gmg_last_error() gives the message of the last error.
  *  - The caller owns every host array; the library copies what it needs into
  *    GB300 device memory (HBM). The handle owns all device memory. Set-up calls
- *    allocate; apply/solve calls do not.
+ *    allocate; operator, transfer and V-cycle calls do not. A solve allocates
+ *    only the first time it meets a Krylov size it has not held since the last
+ *    gb_gmg_finalize_setup (restart length for GMRES/FGMRES, s for IDR(s)):
+ *    (restart + 1) + restart FP64 vectors of the finest level, about 1.4 GB at
+ *    32^3 with restart 100; later solves of the same size reuse them.
  *  - One host thread per handle. Each handle drives one GPU (the current CUDA
  *    device when gb_gmg_create is called).
  *  - Levels are numbered 0 (coarsest) .. n_levels-1 (finest = active mesh).
@@ -259,9 +263,8 @@ int64_t gb_gmg_kernel_launches(const gb_gmg* h);
 
 /* Allocation-free FP32 A-block apply (no counterpart in the reference; ASPECT
  * always owns its operator scratch). For callers that cannot call cudaMalloc
- * when they need the operator: code recording its own CUDA graph, code under a
- * device-memory budget owned by another allocator, or code that must not block
- * on the driver's allocator. dst = A src on a uniform lattice box level in the
+ * when they need the operator: code under a device-memory budget owned by
+ * another allocator, or code that must not block on the driver's allocator. dst = A src on a uniform lattice box level in the
  * lattice numbering (velocity components blocked, Q2 nodes lexicographic, x
  * fastest; constrained rows act as the identity), with the per-cell scratch in
  * a static device array of GB_GMG_NOALLOC_MAX_CELLS cells (1.33 MB, held by
@@ -273,8 +276,9 @@ int64_t gb_gmg_kernel_launches(const gb_gmg* h);
  * host; stream (a cudaStream_t) may be NULL. Larger levels return
  * GB_GMG_EXCEEDS_STATIC_SCRATCH. Calls share the one array: calls whose kernels
  * overlap on the GPU race and must be serialised by the caller. The first call
- * on a device looks up the array's address; make it before any stream capture.
- * The result is written asynchronously on `stream`. */
+ * on a device looks up the array's address and keeps it; make it before any
+ * stream capture. After cudaDeviceReset the kept address is stale: reload the
+ * library first. The result is written asynchronously on `stream`. */
 #define GB_GMG_NOALLOC_MAX_CELLS 4096
 int gb_gmg_ablock_apply_lattice_noalloc(int dim, const int32_t* n_cells_dir, const double* cell_size,
                                         uint32_t zero_faces, int eta_per_cell, const float* d_eta,

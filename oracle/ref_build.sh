@@ -5,8 +5,9 @@
 # build time into oracle/_ref/ (git-ignored); nothing of it enters the repo.
 # Used only to generate the golden fixtures under tests/golden/.
 set -e
-REF=${ASPECT_REFERENCE:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+# the reference tree: $ASPECT_REFERENCE, else a directory "reference" beside the repository
+REF=${ASPECT_REFERENCE:-$(cd "$HERE/../.." && pwd)/reference}
 OUT="$HERE/_ref"
 SRC="$REF/benchmarks/solcx/solcx.h"
 [ -f "$SRC" ] || { echo "reference not present: $SRC" >&2; exit 2; }

@@ -15,7 +15,9 @@ import os
 import re
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("ASPECT_REFERENCE", "/root/reference")
+ROOT = os.path.dirname(os.path.dirname(HERE))
+# the reference tree: $ASPECT_REFERENCE, else a directory "reference" beside the repository
+REF = os.environ.get("ASPECT_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 
 
 def prm_value(txt, key):

@@ -23,7 +23,8 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 from aspect_gb300 import fe, problems  # noqa: E402
 
-REF = os.environ.get("ASPECT_REFERENCE", "/root/reference")
+# the reference tree: $ASPECT_REFERENCE, else a directory "reference" beside the repository
+REF = os.environ.get("ASPECT_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 
 
 def main():

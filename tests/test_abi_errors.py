@@ -69,6 +69,10 @@ def test_noalloc_entry_point_checks_before_touching_the_device(L):
     assert f(3, nc, neg, 0, 1, dummy, dummy, dummy, None) == INVALID         # non-positive size
     big = (ctypes.c_int32 * 3)(17, 16, 16)                                   # 4352 > 4096 cells
     assert f(3, big, h, 0, 27, dummy, dummy, dummy, None) == EXCEEDS
+    huge = (ctypes.c_int32 * 3)(2 ** 31 - 1, 2 ** 31 - 1, 2)                 # product beyond 64 bits
+    assert f(3, huge, h, 0, 1, dummy, dummy, dummy, None) == EXCEEDS
+    wrap = (ctypes.c_int32 * 3)(2 ** 16, 2 ** 16, 2 ** 16)                   # 2^48 cells
+    assert f(3, wrap, h, 0, 1, dummy, dummy, dummy, None) == EXCEEDS
 
 
 def test_no_gpu_means_no_solver():

@@ -1,9 +1,9 @@
 """The allocation-free A-block entry point against the handle-based one.
 
 gb_gmg_ablock_apply_lattice_noalloc serves callers that cannot call cudaMalloc
-when they need the operator (code recording its own CUDA graph, code under a
-device-memory budget owned by another allocator); its per-cell scratch is a
-static device array shared by all calls. Checked here through the C ABI against
+when they need the operator (code under a device-memory budget owned by another
+allocator, code that must not block on the driver's allocator); its per-cell
+scratch is a static device array shared by all calls. Checked here through the C ABI against
 gb_gmg_vmult (FP32 A block) on the same lattice levels, on two calls in a row so
 that a call cannot lean on what the previous one left in the shared array.
 This file is collected last on purpose.
