@@ -41,7 +41,6 @@ METRIC = "Stokes solve time & operator GDoF/s: FP32-MG vs FP64-MG at 1e-8 FP64 r
 WORKLOAD = "sinkers_32^3_Q2Q1_eta1e6_q1proj_fgmres_fp32mg_tol1e-8"
 TOL = 1e-8
 N_CELLS_1D = 32
-CPU_SAMPLE_ITERATIONS = 12
 # Arithmetic per cell of the two cell kernels, counted from their source (an FMA
 # counts 2): the FP32 lattice A-block cell pass (3 x 270 interpolation, 27 x 141
 # per point, 3 x 270 transposed interpolation) and the FP64 Stokes cell pass
@@ -163,64 +162,65 @@ def algorithmic_bytes(P, op: str, word: int) -> int:
     return 2 * n * word + eta_words * word
 
 
-def cpu_baseline(P, n_threads: int, iterations_to_converge: int):
-    """FP64-MG oracle on the host cores: CPU_SAMPLE_ITERATIONS GMRES iterations of
-    the same solve, scaled to the converged iteration count."""
+def cpu_solves(P, n_threads: int, mg_float: bool, n_solves: int):
+    """Full converged solves of the workload on the host cores with the CPU
+    restatement of the reference algorithm (oracle, fast mode: sum-factorised
+    cell operators as in the reference's deal.II code, OpenMP over colour-ordered
+    cells). Returns (seconds of each solve, outputs of the last)."""
+    import oracle
     from oracle import Oracle
+    oracle.set_fast(True)
     o = Oracle(P.levels, n_threads=n_threads)
     o.set_viscosity(P.eta, P.projection, P.pressure_scaling)
-    o.build_preconditioner(False)
-    o.estimate_eigenvalues()
-    t = time.perf_counter()
-    _, info = o.solve(P.rhs, tol_rel=TOL, n_cheap=CPU_SAMPLE_ITERATIONS, n_expensive=0)
-    dt = time.perf_counter() - t
-    its = max(info["cheap_iterations"], 1)
-    est = dt / its * iterations_to_converge
-    return {"seconds_sample": dt, "iterations_sample": its, "seconds_per_solve_est": est,
-            "dofs_per_s": P.n_dofs / est}
+    o.build_preconditioner(mg_float)
+    times, info = [], None
+    for _ in range(n_solves):
+        t = time.perf_counter()
+        _, info = o.solve(P.rhs, tol_rel=TOL)
+        times.append(time.perf_counter() - t)
+        if info["status"] != 0:
+            raise RuntimeError(f"CPU solve did not converge: {info}")
+    return times, info
+
+
+def cpu_baseline(P, n_threads: int):
+    """One full FP64-MG and one full FP32-MG solve on the host cores."""
+    t64, i64 = cpu_solves(P, n_threads, False, 1)
+    t32, i32 = cpu_solves(P, n_threads, True, 1)
+    return {"fp64_mg": {"seconds": t64[0], "iterations": i64["cheap_iterations"] + i64["expensive_iterations"],
+                        "mdofs": P.n_dofs / t64[0] / 1e6},
+            "fp32_mg": {"seconds": t32[0], "iterations": i32["cheap_iterations"] + i32["expensive_iterations"],
+                        "mdofs": P.n_dofs / t32[0] / 1e6}}
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's FP64-MG solve
+    (GMGNumberType = double), all host cores, one full solve to 1e-8 per step;
+    after the timed steps one FP32-MG solve (GMGNumberType = float)."""
     world, rank, _ = dist_init()
     if world > 1 and rank != 0:
         return
     P = build_problem()
     threads = os.cpu_count() or 1
-    # the FP64-MG reference needs this many iterations on the workload (same
-    # algorithm as the GPU FP64-MG path; measured there and in the oracle)
-    its_full = int(os.environ.get("GB_FP64_ITERATIONS", "0")) or None
-    vals, times = [], []
-    from oracle import Oracle
-    o = Oracle(P.levels, n_threads=threads)
-    o.set_viscosity(P.eta, P.projection, P.pressure_scaling)
-    o.build_preconditioner(False)
-    o.estimate_eigenvalues()
-    for step in range(args.warmup + args.steps):
-        t = time.perf_counter()
-        _, info = o.solve(P.rhs, tol_rel=TOL, n_cheap=CPU_SAMPLE_ITERATIONS, n_expensive=0)
-        dt = time.perf_counter() - t
-        if step >= args.warmup:
-            per_it = dt / max(info["cheap_iterations"], 1)
-            times.append(per_it)
-    per_it = statistics.median(times)
-    its = its_full or REFERENCE_FP64_ITERATIONS
-    sec = per_it * its
-    value = P.n_dofs / sec / 1e6
+    times, info = cpu_solves(P, threads, False, args.warmup + args.steps)
+    timed = times[args.warmup:]
+    its = info["cheap_iterations"] + info["expensive_iterations"]
+    value = len(timed) * P.n_dofs / sum(timed) / 1e6
+    t32, i32 = cpu_solves(P, threads, True, 1)
+    sample = (f"full FP64-MG solves of the same 32^3 workload to 1e-8 ({its} GMRES iterations each), one per step; "
+              f"CPU restatement of the reference algorithm, sum-factorised cell operators, OpenMP over "
+              f"colour-ordered cells")
     line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "MDoF/s", "n_gpus": 0,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD.replace("fp32mg", "fp64mg"), "n_dofs": P.n_dofs},
-            "cpu_baseline": {"value": value, "unit": "MDoF/s", "cores": threads, "kind": "port",
-                             "sample": f"{CPU_SAMPLE_ITERATIONS} GMRES iterations per step of the same 32^3 "
-                                       f"FP64-MG solve (CPU oracle, OpenMP over colour-ordered cells), "
-                                       f"seconds per iteration x {its} iterations to 1e-8"},
-            "e2e": {"value": value, "unit": "MDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(timed) / len(timed) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD.replace("fgmres_fp32mg", "gmres_fp64mg"), "n_dofs": P.n_dofs,
+                       "iterations": its},
+            "cpu_baseline": {"value": value, "unit": "MDoF/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "MDoF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "detail": {"seconds_per_solve": timed,
+                       "fp32_mg": {"seconds": t32[0], "iterations": i32["cheap_iterations"] + i32["expensive_iterations"],
+                                   "mdofs": P.n_dofs / t32[0] / 1e6}}}
     print(json.dumps(line), flush=True)
-
-
-# iterations of the FP64-MG solve of this workload to 1e-8 (measured on the GPU
-# path, which runs the same algorithm as the oracle; used to scale CPU samples)
-REFERENCE_FP64_ITERATIONS = 56
 
 
 def run_gpu(args):
@@ -367,7 +367,7 @@ def run_gpu(args):
     its_mixed = mixed["cheap_iterations"] + mixed["expensive_iterations"]
     its64 = o64["cheap_iterations"] + o64["expensive_iterations"]
     log("operators", ops)
-    cpu = cpu_baseline(P, os.cpu_count() or 1, its64)
+    cpu = cpu_baseline(P, os.cpu_count() or 1)
     log("cpu baseline", cpu)
     line = {
         "metric": METRIC, "value": value, "unit": "MDoF/s", "n_gpus": world, "steps": args.steps,
@@ -404,9 +404,14 @@ def run_gpu(args):
                                  "seconds_per_application": t_s64, "achieved_tflops": tflops_s64,
                                  "peak_tflops": FP64_PEAK_TFLOPS, "frac": tflops_s64 / FP64_PEAK_TFLOPS,
                                  "peak_kind": "nominal", "flops_per_cell": FLOPS_STOKES_CELL_F64},
-        "cpu_baseline": {"value": cpu["dofs_per_s"] / 1e6, "unit": "MDoF/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"{cpu['iterations_sample']} GMRES iterations of the same 32^3 solve, FP64-MG "
-                                   f"CPU oracle ({cpu['seconds_sample']:.1f} s), scaled to {its64} iterations"},
+        "cpu_baseline": {"value": cpu["fp64_mg"]["mdofs"], "unit": "MDoF/s", "cores": os.cpu_count(),
+                         "kind": "port",
+                         "sample": f"one full FP64-MG solve of the same 32^3 workload to 1e-8 "
+                                   f"({cpu['fp64_mg']['iterations']} iterations, {cpu['fp64_mg']['seconds']:.2f} s), "
+                                   f"CPU restatement of the reference algorithm (sum-factorised cell operators); "
+                                   f"FP32-MG: {cpu['fp32_mg']['seconds']:.2f} s, {cpu['fp32_mg']['iterations']} "
+                                   f"iterations",
+                         "fp32_mg": cpu["fp32_mg"]},
         "clocks": clocks,
         "detail": {
             "setup_seconds": setup_s, "wall_seconds_timed": wall,

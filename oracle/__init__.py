@@ -44,10 +44,18 @@ def lib():
                      "orc_finalize", "orc_set_viscosity", "orc_get_level_viscosity",
                      "orc_build_preconditioner", "orc_vmult", "orc_get_diagonal", "orc_transfer",
                      "orc_estimate_eigenvalues", "orc_get_eigenvalues", "orc_set_eigenvalues",
-                     "orc_vcycle", "orc_block_preconditioner", "orc_solve", "orc_adjoint_gradient"]:
+                     "orc_vcycle", "orc_block_preconditioner", "orc_solve", "orc_adjoint_gradient",
+                     "orc_set_fast"]:
             getattr(L, name).restype = ctypes.c_int
         _lib = L
     return _lib
+
+
+def set_fast(on: bool) -> None:
+    """Process-wide switch of the oracle library: True selects the sum-factorised
+    cell operators and parallel reductions used to time the CPU baseline; False
+    (the default) the plain quadrature loops the parity tests check against."""
+    lib().orc_set_fast(int(bool(on)))
 
 
 def _d(a):

@@ -187,6 +187,10 @@ struct Level {
   // transfers from the coarser level (CSR rows = this level's dofs)
   std::vector<int> Pu_ptr, Pu_col, Pp_ptr, Pp_col;
   std::vector<double> Pu_val, Pp_val;
+  // their transposes, built on first use in fast mode
+  std::vector<int> PuT_ptr, PuT_col, PpT_ptr, PpT_col;
+  std::vector<double> PuT_val, PpT_val;
+  bool PT_built = false;
   // smoother data
   std::vector<double> diagA_inv, diagM_inv;
   double eigA[2] = {0, 0}, eigM[2] = {0, 0};  // (min, max) estimates
@@ -332,6 +336,197 @@ static void cell_apply(const Level& L, const FE& fe, int c, int op, double s, in
   }
 }
 
+// ---------------------------------------------------------------- sum-factorised cell kernel
+// The same cell operator as cell_apply, evaluated by sum factorisation the way
+// the reference's CPU code does (deal.II FEEvaluation: tensor-product sweeps
+// of the 1D basis values and derivatives at the Gauss points, then the
+// quadrature-point physics, then the transposed sweeps). It serves the CPU
+// baseline timing ("fast" mode); the checker keeps the plain quadrature loops
+// above, and tests compare the two.
+struct Basis1D {
+  double S[3][3], D[3][3];  // phi_n(g_q), phi_n'(g_q) of the Q2 basis at the 3 Gauss points
+};
+static Basis1D make_basis1d() {
+  Basis1D b;
+  const double g[3] = {0.5 - 0.5 * std::sqrt(0.6), 0.5, 0.5 + 0.5 * std::sqrt(0.6)};
+  const double q2n[3] = {0.0, 0.5, 1.0};
+  for (int q = 0; q < 3; ++q) lagrange1d(q2n, 3, g[q], b.S[q], b.D[q]);
+  return b;
+}
+static const Basis1D& basis1d() {
+  static const Basis1D b = make_basis1d();
+  return b;
+}
+
+// out[.. q_dir ..] = sum_n M[q][n] in[.. n_dir ..] (or M^T), 3 points per direction
+template <class T, int dim, int dir, bool transpose>
+static inline void sf_sweep(const double (&M)[3][3], const T* in, T* out) {
+  constexpr int st = dir == 0 ? 1 : dir == 1 ? 3 : 9;
+  constexpr int N = dim == 3 ? 27 : 9;
+  for (int b = 0; b < N; ++b) {
+    if ((b / st) % 3 != 0) continue;
+    const T a0 = in[b], a1 = in[b + st], a2 = in[b + 2 * st];
+    for (int q = 0; q < 3; ++q) {
+      const T m0 = (T)(transpose ? M[0][q] : M[q][0]);
+      const T m1 = (T)(transpose ? M[1][q] : M[q][1]);
+      const T m2 = (T)(transpose ? M[2][q] : M[q][2]);
+      out[b + q * st] = m0 * a0 + m1 * a1 + m2 * a2;
+    }
+  }
+}
+
+// reference gradient g[dir][q] of one nodal field u
+template <class T, int dim>
+static inline void sf_grad(const Basis1D& B, const T* u, T (*g)[27]) {
+  if (dim == 2) {
+    T t[9];
+    sf_sweep<T, 2, 1, false>(B.S, u, t);
+    sf_sweep<T, 2, 0, false>(B.D, t, g[0]);
+    sf_sweep<T, 2, 1, false>(B.D, u, t);
+    sf_sweep<T, 2, 0, false>(B.S, t, g[1]);
+  } else {
+    T t1[27], t2[27];
+    sf_sweep<T, 3, 2, false>(B.S, u, t1);
+    sf_sweep<T, 3, 1, false>(B.S, t1, t2);
+    sf_sweep<T, 3, 0, false>(B.D, t2, g[0]);
+    sf_sweep<T, 3, 1, false>(B.D, t1, t2);
+    sf_sweep<T, 3, 0, false>(B.S, t2, g[1]);
+    sf_sweep<T, 3, 2, false>(B.D, u, t1);
+    sf_sweep<T, 3, 1, false>(B.S, t1, t2);
+    sf_sweep<T, 3, 0, false>(B.S, t2, g[2]);
+  }
+}
+
+// y += sum_dir (gradient in direction dir)^T r[dir]
+template <class T, int dim>
+static inline void sf_grad_t(const Basis1D& B, T (*r)[27], T* y) {
+  if (dim == 2) {
+    T a[9], b[9];
+    sf_sweep<T, 2, 0, true>(B.D, r[0], a);
+    sf_sweep<T, 2, 1, true>(B.S, a, b);
+    for (int n = 0; n < 9; ++n) y[n] += b[n];
+    sf_sweep<T, 2, 0, true>(B.S, r[1], a);
+    sf_sweep<T, 2, 1, true>(B.D, a, b);
+    for (int n = 0; n < 9; ++n) y[n] += b[n];
+  } else {
+    T a[27], b[27], s1[27];
+    sf_sweep<T, 3, 0, true>(B.D, r[0], a);
+    sf_sweep<T, 3, 1, true>(B.S, a, s1);
+    sf_sweep<T, 3, 0, true>(B.S, r[1], a);
+    sf_sweep<T, 3, 1, true>(B.D, a, b);
+    for (int n = 0; n < 27; ++n) s1[n] += b[n];
+    sf_sweep<T, 3, 2, true>(B.S, s1, a);
+    for (int n = 0; n < 27; ++n) y[n] += a[n];
+    sf_sweep<T, 3, 0, true>(B.S, r[2], a);
+    sf_sweep<T, 3, 1, true>(B.S, a, b);
+    sf_sweep<T, 3, 2, true>(B.D, b, a);
+    for (int n = 0; n < 27; ++n) y[n] += a[n];
+  }
+}
+
+template <class T, int dim>
+static void cell_apply_sf(const Level& L, const FE& fe, int c, int op, double s, int compressible,
+                          const T* eta_tab, const T* xu, const T* xp, T* yu, T* yp) {
+  constexpr int d = dim, nq = dim == 3 ? 27 : 9, nv = nq, np = dim == 3 ? 8 : 4;
+  const Basis1D& B = basis1d();
+  const bool use_u = (op == OP_STOKES || op == OP_A), use_p = (op == OP_STOKES || op == OP_BT);
+  const bool cart = L.geom_kind == 0;
+  T gref[3][3][27];  // [component][reference direction][q]
+  if (use_u)
+    for (int cc = 0; cc < d; ++cc) sf_grad<T, dim>(B, xu + cc * nv, gref[cc]);
+  T rref[3][3][27];
+  T fp[27];
+  for (int q = 0; q < nq; ++q) {
+    const double* iJ = &L.invJ[((size_t)c * nq + q) * d * d];
+    const T jxw = (T)L.JxW[(size_t)c * nq + q];
+    const T eta = eta_tab[(size_t)c * L.eta_n + (L.eta_n == 1 ? 0 : q)];
+    T G[3][3] = {{0}};
+    if (use_u && cart) {  // box cells: diagonal inverse Jacobian
+      for (int cc = 0; cc < d; ++cc)
+        for (int e = 0; e < d; ++e) G[cc][e] = gref[cc][e][q] * (T)iJ[e * d + e];
+    } else if (use_u) {
+      for (int cc = 0; cc < d; ++cc)
+        for (int e = 0; e < d; ++e) {
+          T t = 0;
+          for (int a = 0; a < d; ++a) t += gref[cc][a][q] * (T)iJ[a * d + e];
+          G[cc][e] = t;
+        }
+    }
+    T pq = 0;
+    if (use_p)
+      for (int n = 0; n < np; ++n) pq += xp[n] * (T)fe.pval[q * np + n];
+    T F[3][3] = {{0}};
+    T div = 0;
+    for (int e = 0; e < d; ++e) div += G[e][e];
+    if (use_u) {
+      const T eta2 = (T)2 * eta;
+      for (int a = 0; a < d; ++a)
+        for (int b = 0; b < d; ++b) F[a][b] = eta2 * (T)0.5 * (G[a][b] + G[b][a]);
+      if (compressible)
+        for (int a = 0; a < d; ++a) F[a][a] -= eta2 / (T)3 * div;
+    }
+    if (use_p)
+      for (int a = 0; a < d; ++a) F[a][a] -= (T)s * pq;
+    for (int cc = 0; cc < d; ++cc)
+      for (int a = 0; a < d; ++a) {
+        if (cart) {
+          rref[cc][a][q] = F[cc][a] * (T)iJ[a * d + a] * jxw;
+          continue;
+        }
+        T t = 0;
+        for (int e = 0; e < d; ++e) t += F[cc][e] * (T)iJ[a * d + e];
+        rref[cc][a][q] = t * jxw;
+      }
+    if (op == OP_STOKES) fp[q] = -(T)s * div * jxw;
+  }
+  for (int cc = 0; cc < d; ++cc) sf_grad_t<T, dim>(B, rref[cc], yu + cc * nv);
+  if (op == OP_STOKES)
+    for (int n = 0; n < np; ++n) {
+      T t = 0;
+      for (int q = 0; q < nq; ++q) t += (T)fe.pval[q * np + n] * fp[q];
+      yp[n] += t;
+    }
+}
+
+// "fast" mode (CPU baseline timing only): sum-factorised cell operators and
+// deterministic parallel reductions (fixed chunks summed in order).
+static bool g_fast = false;
+
+template <class T>
+static void cell_apply_any(const Level& L, const FE& fe, int c, int op, double s, int compressible,
+                           const T* eta_tab, const T* xu, const T* xp, T* yu, T* yp) {
+  if (g_fast && op != OP_MASS) {
+    if (L.dim == 3) cell_apply_sf<T, 3>(L, fe, c, op, s, compressible, eta_tab, xu, xp, yu, yp);
+    else cell_apply_sf<T, 2>(L, fe, c, op, s, compressible, eta_tab, xu, xp, yu, yp);
+    return;
+  }
+  cell_apply<T>(L, fe, c, op, s, compressible, eta_tab, xu, xp, yu, yp);
+}
+
+// sum a[i] b[i]: serial in the checker; in fast mode 256 fixed chunks summed
+// in parallel and then in chunk order, so the result does not depend on the
+// number of threads
+static double dot_n(const double* a, const double* b, long n) {
+  if (!g_fast || n < 65536) {
+    double s_ = 0;
+    for (long i = 0; i < n; ++i) s_ += a[i] * b[i];
+    return s_;
+  }
+  constexpr int K = 256;
+  double part[K];
+  const long chunk = (n + K - 1) / K;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < K; ++k) {
+    double s_ = 0;
+    const long e = std::min(n, (k + 1) * chunk);
+    for (long i = k * chunk; i < e; ++i) s_ += a[i] * b[i];
+    part[k] = s_;
+  }
+  double s_ = 0;
+  for (int k = 0; k < K; ++k) s_ += part[k];
+  return s_;
+}
+
 // ---------------------------------------------------------------- solver state
 struct Params {
   double tol_rel = 1e-7;        // Linear solver tolerance
@@ -395,7 +590,7 @@ struct Oracle {
             for (int m = 0; m < e.n; ++m) v += (T)e.w[m] * src_p[e.g[m]];
             xp[i] = v;
           }
-        cell_apply<T>(L, fe, c, op, s, compressible, eta_tab, xu, xp, yu, yp);
+        cell_apply_any<T>(L, fe, c, op, s, compressible, eta_tab, xu, xp, yu, yp);
         if (wu)
           for (int i = 0; i < nu; ++i) {
             Expansion e = expand(L.cu, L.cdu[(size_t)c * nu + i]);
@@ -448,7 +643,7 @@ struct Oracle {
         for (int j = 0; j < nl; ++j) {
           double xu[81] = {0}, xp[8] = {0}, yu[81] = {0}, yp[8] = {0};
           if (block == 0) xu[j] = 1.0; else xp[j] = 1.0;
-          cell_apply<double>(L, fe, c, block == 0 ? OP_A : OP_MASS, s, compressible, L.eta.data(), xu, xp, yu, yp);
+          cell_apply_any<double>(L, fe, c, block == 0 ? OP_A : OP_MASS, s, compressible, L.eta.data(), xu, xp, yu, yp);
           for (int i = 0; i < nl; ++i) K[(size_t)i * nl + j] = block == 0 ? yu[i] : yp[i];
         }
         for (int g : gs) {
@@ -543,12 +738,52 @@ struct Oracle {
   template <class T>
   void restrict_add(int lev, int block, const T* fine_v, T* coarse) {
     Level& F = levels[lev];
+    if (g_fast) {  // rows of P^T in parallel (fast mode builds the transpose once)
+      build_transfer_transpose(lev);
+      const auto& ptr = block == 0 ? F.PuT_ptr : F.PpT_ptr;
+      const auto& col = block == 0 ? F.PuT_col : F.PpT_col;
+      const auto& val = block == 0 ? F.PuT_val : F.PpT_val;
+      const int n = (int)ptr.size() - 1;
+#pragma omp parallel for schedule(static)
+      for (int r = 0; r < n; ++r) {
+        T t = 0;
+        for (int k = ptr[r]; k < ptr[r + 1]; ++k) t += (T)val[k] * fine_v[col[k]];
+        coarse[r] += t;
+      }
+      return;
+    }
     const auto& ptr = block == 0 ? F.Pu_ptr : F.Pp_ptr;
     const auto& col = block == 0 ? F.Pu_col : F.Pp_col;
     const auto& val = block == 0 ? F.Pu_val : F.Pp_val;
     int n = (int)ptr.size() - 1;
     for (int r = 0; r < n; ++r)
       for (int k = ptr[r]; k < ptr[r + 1]; ++k) coarse[col[k]] += (T)val[k] * fine_v[r];
+  }
+  void build_transfer_transpose(int lev) {
+    Level& F = levels[lev];
+    if (F.PT_built) return;
+    for (int block = 0; block < 2; ++block) {
+      const auto& ptr = block == 0 ? F.Pu_ptr : F.Pp_ptr;
+      const auto& col = block == 0 ? F.Pu_col : F.Pp_col;
+      const auto& val = block == 0 ? F.Pu_val : F.Pp_val;
+      const int nc = block == 0 ? levels[lev - 1].n_u : levels[lev - 1].n_p;
+      auto& tp = block == 0 ? F.PuT_ptr : F.PpT_ptr;
+      auto& tc = block == 0 ? F.PuT_col : F.PpT_col;
+      auto& tv = block == 0 ? F.PuT_val : F.PpT_val;
+      tp.assign(nc + 1, 0);
+      for (int c : col) tp[c + 1]++;
+      for (int r = 0; r < nc; ++r) tp[r + 1] += tp[r];
+      tc.assign(col.size(), 0);
+      tv.assign(col.size(), 0.0);
+      std::vector<int> fill(tp.begin(), tp.end() - 1);
+      const int nf = (int)ptr.size() - 1;
+      for (int r = 0; r < nf; ++r)
+        for (int k = ptr[r]; k < ptr[r + 1]; ++k) {
+          tc[fill[col[k]]] = r;
+          tv[fill[col[k]]++] = val[k];
+        }
+    }
+    F.PT_built = true;
   }
 
   // -------- viscosity on levels (stokes_matrix_free_local_smoothing.cc:174-294)
@@ -810,10 +1045,12 @@ struct Oracle {
     std::vector<T> d(n), t(n);
     int k0;
     if (zero_start) {
+#pragma omp parallel for schedule(static) if (g_fast && n > 16384)
       for (int i = 0; i < n; ++i) { d[i] = (T)(1.0 / theta) * dinv[i] * b[i]; x[i] = d[i]; }
       k0 = 1;
     } else {
       level_op<T>(lev, block, x, t.data());
+#pragma omp parallel for schedule(static) if (g_fast && n > 16384)
       for (int i = 0; i < n; ++i) { d[i] = (T)(1.0 / theta) * dinv[i] * (b[i] - t[i]); x[i] += d[i]; }
       k0 = 1;
     }
@@ -823,6 +1060,7 @@ struct Oracle {
       double rhokp = 1.0 / (2.0 * sigma - rhok);
       double f1 = rhokp * rhok, f2 = 2.0 * rhokp / delta;
       rhok = rhokp;
+#pragma omp parallel for schedule(static) if (g_fast && n > 16384)
       for (int i = 0; i < n; ++i) {
         d[i] = (T)f1 * d[i] + (T)f2 * dinv[i] * (b[i] - t[i]);
         x[i] += d[i];
@@ -918,15 +1156,9 @@ struct Oracle {
   }
 
   static double dot(const std::vector<double>& a, const std::vector<double>& b) {
-    double s_ = 0;
-    for (size_t i = 0; i < a.size(); ++i) s_ += a[i] * b[i];
-    return s_;
+    return dot_n(a.data(), b.data(), (long)a.size());
   }
-  static double dotp(const double* a, const double* b, int n) {
-    double s_ = 0;
-    for (int i = 0; i < n; ++i) s_ += a[i] * b[i];
-    return s_;
-  }
+  static double dotp(const double* a, const double* b, int n) { return dot_n(a, b, n); }
 
   // preconditioned CG (expensive inner solves), returns iterations
   template <class Mat, class Prec>
@@ -1020,8 +1252,12 @@ struct Oracle {
         for (int pass = 0; pass < 2; ++pass) {
           std::vector<double> hh(j + 1);
           for (int i = 0; i <= j; ++i) hh[i] = dot(w, V[i]);
-          for (int i = 0; i <= j; ++i)
-            for (int k = 0; k < n; ++k) w[k] -= hh[i] * V[i][k];
+#pragma omp parallel for schedule(static) if (g_fast)
+          for (int k = 0; k < n; ++k) {
+            double t = w[k];
+            for (int i = 0; i <= j; ++i) t -= hh[i] * V[i][k];
+            w[k] = t;
+          }
           for (int i = 0; i <= j; ++i) h[i] += hh[i];
           double nw = std::sqrt(dot(w, w));
           if (pass == 0 && nw > 0.7 * norm_before) break;
@@ -1055,12 +1291,19 @@ struct Oracle {
         y[i] = t / H[i][i];
       }
       if (flexible) {
-        for (int i = 0; i < m; ++i)
-          for (int k = 0; k < n; ++k) x[k] += y[i] * Z[i][k];
+#pragma omp parallel for schedule(static) if (g_fast)
+        for (int k = 0; k < n; ++k) {
+          double t = x[k];
+          for (int i = 0; i < m; ++i) t += y[i] * Z[i][k];
+          x[k] = t;
+        }
       } else {
-        std::fill(tmp.begin(), tmp.end(), 0.0);
-        for (int i = 0; i < m; ++i)
-          for (int k = 0; k < n; ++k) tmp[k] += y[i] * V[i][k];
+#pragma omp parallel for schedule(static) if (g_fast)
+        for (int k = 0; k < n; ++k) {
+          double t = 0.0;
+          for (int i = 0; i < m; ++i) t += y[i] * V[i][k];
+          tmp[k] = t;
+        }
         std::vector<double> z(n);
         block_prec(tmp.data(), z.data(), expensive, P);
         for (int k = 0; k < n; ++k) x[k] += z[k];
@@ -1260,6 +1503,12 @@ void* orc_create(int dim, int n_levels) {
 }
 void orc_destroy(void* p) { delete (Oracle*)p; }
 const char* orc_last_error(void* p) { return ((Oracle*)p)->err.c_str(); }
+// 1: sum-factorised cell operators and parallel reductions (CPU baseline timing);
+// 0 (default): the checker's plain quadrature loops and serial reductions
+int orc_set_fast(int on) {
+  orc::g_fast = on != 0;
+  return 0;
+}
 int orc_set_num_threads(int n) {
 #ifdef _OPENMP
   if (n > 0) omp_set_num_threads(n);

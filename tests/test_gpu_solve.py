@@ -45,8 +45,11 @@ def test_solcx_64_matches_oracle(precision):
     xr, info = o.solve(P.rhs, tol_rel=1e-8)
     f = P.fine
     assert out["status"] == 0 and info["status"] == 0
-    # both solutions satisfy the same 1e-8 residual; they agree to the conditioning
-    assert rel_err(x[: f.n_u], xr[: f.n_u]) < 1e-5
+    # FP64: the same algorithm to rounding (1e-8); FP32 V-cycle: both satisfy the
+    # same 1e-8 FP64 residual and agree to the conditioning
+    tol = 1e-8 if precision == gmg.FP64 else 1e-6
+    assert rel_err(x[: f.n_u], xr[: f.n_u]) < tol
+    assert rel_err(x[f.n_u:], xr[f.n_u:]) < tol
     if precision == gmg.FP64:
         assert abs(out["cheap_iterations"] - info["cheap_iterations"]) <= 1
     # true residual of the GPU solution, measured by the oracle in FP64
@@ -66,7 +69,8 @@ def test_sinkers_mixed_precision(krylov):
     r = P.rhs - o.vmult(0, len(P.levels) - 1, x32)
     assert np.linalg.norm(r) <= 1.01 * o32["solver_tolerance"]
     f = P.fine
-    assert rel_err(x32[: f.n_u], x64[: f.n_u]) < 1e-5
+    assert rel_err(x32[: f.n_u], x64[: f.n_u]) < 1e-6
+    assert rel_err(x32[f.n_u:], x64[f.n_u:]) < 1e-6
 
 
 def test_no_convergence_is_reported():
@@ -105,6 +109,8 @@ def test_idr_matches_oracle(precision):
     r = P.rhs - o.vmult(0, len(P.levels) - 1, x)
     assert np.linalg.norm(r) <= 1.01 * out["solver_tolerance"]
     f = P.fine
-    assert rel_err(x[: f.n_u], xr[: f.n_u]) < 1e-5
+    tol = 1e-8 if precision == gmg.FP64 else 1e-6
+    assert rel_err(x[: f.n_u], xr[: f.n_u]) < tol
+    assert rel_err(x[f.n_u:], xr[f.n_u:]) < tol
     if precision == gmg.FP64:
         assert abs(out["cheap_iterations"] - info["cheap_iterations"]) <= 1
