@@ -17,7 +17,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgb_gmg.so")
-SOURCES = ["kernels_f32.cu", "kernels_f64.cu", "adjoint.cu", "vec.cu", "level_setup.cu", "gb_gmg.cu", "noalloc.cu", "mass_bottom.cu"]
+SOURCES = ["kernels_f32.cu", "kernels_f64.cu", "adjoint.cu", "vec.cu", "level_setup.cu", "gb_gmg.cu", "noalloc.cu", "mass_bottom.cu", "ablock_fused.cu"]
+# measured FP64/FP32 FMA peaks for the benchmark's rooflines (not part of the solver)
+PROBE_LIB = os.path.join(HERE, "libgb_probe.so")
+PROBE_SOURCES = ["peak_probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 
@@ -36,7 +39,8 @@ def _deps_mtime() -> float:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps_mtime():
+    if (not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps_mtime() and os.path.exists(PROBE_LIB)
+            and os.path.getmtime(PROBE_LIB) >= _deps_mtime()):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     nv = nvcc()
@@ -51,14 +55,17 @@ def build(force: bool = False, verbose: bool = False) -> str:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(compile_one, SOURCES))
-    tmp = LIB + ".tmp"
-    cmd = [nv, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lcusolver", "-lcublas"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
+    all_sources = SOURCES + PROBE_SOURCES
+    with cf.ThreadPoolExecutor(max_workers=min(len(all_sources), os.cpu_count() or 4)) as ex:
+        objs = dict(zip(all_sources, ex.map(compile_one, all_sources)))
+    for lib, srcs, libs in ((LIB, SOURCES, ["-lcudart", "-lcusolver", "-lcublas"]),
+                            (PROBE_LIB, PROBE_SOURCES, ["-lcudart"])):
+        tmp = lib + ".tmp"
+        cmd = [nv, *ARCH, "-shared", "-o", tmp, *[objs[x] for x in srcs], *libs]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, lib)
     return LIB
 
 

@@ -96,13 +96,17 @@ __device__ __forceinline__ void interpolate(T* x) {
   if constexpr (dim == 3) sweep_S<T, dim, 2, transpose>(x);
 }
 
-// derivative along `dir` at Gauss point q of a collocated field
+// derivative along `dir` at Gauss point q of a collocated field. The middle
+// point's middle coefficient is zero; its term is left out at compile time (the
+// compiler may not drop a multiplication by 0.0 itself), which changes no
+// result for finite inputs.
 template <typename T, int dim, int q, int dir>
 __device__ __forceinline__ T colloc_d(const T* x) {
   constexpr int st = fe::pow3(dir);
   constexpr int qd = (q / st) % 3;
   constexpr int b = q - qd * st;
-  return T(fe::Dv(qd, 0)) * x[b] + T(fe::Dv(qd, 1)) * x[b + st] + T(fe::Dv(qd, 2)) * x[b + 2 * st];
+  if constexpr (qd == 1) return T(fe::Dv(1, 0)) * x[b] + T(fe::Dv(1, 2)) * x[b + 2 * st];
+  else return T(fe::Dv(qd, 0)) * x[b] + T(fe::Dv(qd, 1)) * x[b + st] + T(fe::Dv(qd, 2)) * x[b + 2 * st];
 }
 template <typename T, int dim, int q, int dir>
 __device__ __forceinline__ void colloc_dT(T* x, T r) {
@@ -110,7 +114,7 @@ __device__ __forceinline__ void colloc_dT(T* x, T r) {
   constexpr int qd = (q / st) % 3;
   constexpr int b = q - qd * st;
   x[b] += T(fe::Dv(qd, 0)) * r;
-  x[b + st] += T(fe::Dv(qd, 1)) * r;
+  if constexpr (qd != 1) x[b + st] += T(fe::Dv(qd, 1)) * r;
   x[b + 2 * st] += T(fe::Dv(qd, 2)) * r;
 }
 
@@ -504,18 +508,15 @@ __device__ __forceinline__ void mass_cell_op(const LevelView<T>& L, int cell, co
 // point. The per-cell contributions are written slot-major (E[slot][cell]), so
 // the stores of a warp are coalesced.
 template <int op, bool eta_per_q>
-__global__ void __launch_bounds__(128) lattice_cell_kernel_f32(LevelView<float> L, const float* __restrict__ src_u,
-                                                                const float* __restrict__ src_p,
-                                                                float* __restrict__ Eu, float* __restrict__ Ep) {
-  pdl_wait();
+__device__ __forceinline__ void lattice_cell_f32(const LevelView<float>& L, const float* __restrict__ src_u,
+                                                 const float* __restrict__ src_p, int cell, float (&V)[3][27],
+                                                 float (&YP)[8]) {
   constexpr bool need_u = (op == OPK_STOKES || op == OPK_A);
   constexpr bool need_p = (op == OPK_STOKES || op == OPK_BT);
   using T = float;
-  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-  if (cell >= L.n_cells) return;
   StructuredCell<T, 3> sc;
   structured_cell_lex<T, 3>(L, cell, sc);
-  T U[3][27], V[3][27], P[8], YP[8];
+  T U[3][27], P[8];
   if constexpr (need_u) {
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -530,9 +531,9 @@ __global__ void __launch_bounds__(128) lattice_cell_kernel_f32(LevelView<float> 
   if constexpr (need_p) {
 #pragma unroll
     for (int n = 0; n < 8; ++n) P[n] = src_p[sc.pnode0 + structured_pnode_offset<3>(L.Np, n)];
-#pragma unroll
-    for (int n = 0; n < 8; ++n) YP[n] = T(0);
   }
+#pragma unroll
+  for (int n = 0; n < 8; ++n) YP[n] = T(0);
 #pragma unroll
   for (int c = 0; c < 3; ++c)
 #pragma unroll
@@ -597,14 +598,208 @@ __global__ void __launch_bounds__(128) lattice_cell_kernel_f32(LevelView<float> 
     }
   });
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    interpolate<T, 3, true>(V[c]);
+  for (int c = 0; c < 3; ++c) interpolate<T, 3, true>(V[c]);
+}
+
+template <int op, bool eta_per_q>
+__global__ void __launch_bounds__(128) lattice_cell_kernel_f32(LevelView<float> L, const float* __restrict__ src_u,
+                                                                const float* __restrict__ src_p,
+                                                                float* __restrict__ Eu, float* __restrict__ Ep) {
+  pdl_wait();
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= L.n_cells) return;
+  float V[3][27], YP[8];
+  lattice_cell_f32<op, eta_per_q>(L, src_u, src_p, cell, V, YP);
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
 #pragma unroll
     for (int n = 0; n < 27; ++n) Eu[(size_t)(c * 27 + n) * L.n_cells + cell] = V[c][n];
-  }
   if constexpr (op == OPK_STOKES) {
 #pragma unroll
     for (int n = 0; n < 8; ++n) Ep[(size_t)n * L.n_cells + cell] = YP[n];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 cell pass of isotropic 3D lattice levels (cubic cells, h the same in
+// every direction: the box workloads). GB300 issues about two FP64 FMAs per SM
+// and clock, 1/64 of its FP32 rate, so this kernel is written to spend as few
+// FP64 instructions as possible; shuffles, selects and integer work are almost
+// free next to them.
+//  * One velocity component per thread, three threads per cell, as in
+//    velocity_cell_kernel; the symmetric gradient's off-diagonal entries come
+//    from the sibling threads by warp shuffles.
+//  * The geometry is folded into two per-point constants (IsoCoef): with
+//    g = ih gr (gr the reference gradient), the reference-direction fluxes are
+//      R_cc = 2 K_q eta gr_cc - M_q p,  R_ce = K_q eta (gr_ce + gr_ec),
+//    K_q = ih^2 |det J| w_q, M_q = s ih |det J| w_q.
+//  * The Q1 pressure work is done once per cell, not once per component: thread
+//    c interpolates the pressure to the nine Gauss points of plane z = c (sum
+//    factorisation, 38 operations) and the other threads read them by shuffle;
+//    the divergence at each point is summed by shuffles, kept by the thread of
+//    that point's plane, and integrated back plane by plane (transposed sum
+//    factorisation), the three partial results then summed by shuffles.
+// Output layout and summation into nodes are those of velocity_cell_kernel
+// (cell-major contributions), so the gathers are shared.
+template <typename T>
+struct IsoCoef {
+  T K[27];  // ih^2 |det J| w_q
+  T M[27];  // s ih |det J| w_q
+};
+
+template <int op, bool eta_per_q>
+__global__ void __launch_bounds__(128) lattice_iso_kernel_f64(LevelView<double> L, IsoCoef<double> C,
+                                                               const double* __restrict__ src_u,
+                                                               const double* __restrict__ src_p,
+                                                               double* __restrict__ Eu, double* __restrict__ Ep) {
+  pdl_wait();
+  using T = double;
+  constexpr bool need_u = (op == OPK_STOKES || op == OPK_A);
+  constexpr bool need_p = (op == OPK_STOKES || op == OPK_BT);
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int grp = lane / 3;
+  int comp = lane - 3 * grp;
+  bool active = grp < 10;
+  if (!active) { grp = 9; comp = 0; }  // lanes 30, 31 shadow lane 27 and write nothing
+  const int lb = 3 * grp;
+  const int l1 = lb + (comp + 1) % 3, l2 = lb + (comp + 2) % 3;
+  const int k1 = (comp + 1) % 3, k2 = (comp + 2) % 3;
+  const int idx = warp * 10 + grp;
+  active = active && idx < L.n_cells;
+  const int cell = active ? idx : 0;
+  StructuredCell<T, 3> sc;
+  structured_cell_lex<T, 3>(L, cell, sc);
+
+  T U[27], V[27];
+  if constexpr (need_u) {
+#pragma unroll
+    for (int n = 0; n < 27; ++n) {
+      T v = T(0);
+      if (active && !structured_zero<T, 3>(L, sc, comp, n))
+        v = src_u[comp * L.n_nodes + sc.node0 + structured_node_offset<3>(L.Nn, n)];
+      U[n] = v;
+    }
+    interpolate<T, 3, false>(U);
+  }
+#pragma unroll
+  for (int n = 0; n < 27; ++n) V[n] = T(0);
+
+  // scaled pressure at the nine points of plane z = comp: spl[qy*3+qx] = M_q p(q)
+  T spl[9];
+  if constexpr (need_p) {
+    T P[8];
+#pragma unroll
+    for (int n = 0; n < 8; ++n) P[n] = active ? src_p[sc.pnode0 + structured_pnode_offset<3>(L.Np, n)] : T(0);
+    const T z0 = sel3(T(fe::P1v(0, 0)), T(fe::P1v(1, 0)), T(fe::P1v(2, 0)), comp);
+    const T z1 = sel3(T(fe::P1v(0, 1)), T(fe::P1v(1, 1)), T(fe::P1v(2, 1)), comp);
+    T a[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = z0 * P[i] + z1 * P[i + 4];
+    T b[6];
+#pragma unroll
+    for (int y = 0; y < 2; ++y)
+#pragma unroll
+      for (int qx = 0; qx < 3; ++qx) b[y * 3 + qx] = T(fe::P1v(qx, 0)) * a[2 * y] + T(fe::P1v(qx, 1)) * a[2 * y + 1];
+#pragma unroll
+    for (int qy = 0; qy < 3; ++qy)
+#pragma unroll
+      for (int qx = 0; qx < 3; ++qx) {
+        const int j = qy * 3 + qx;
+        const T m = sel3(C.M[j], C.M[9 + j], C.M[18 + j], comp);
+        spl[j] = m * (T(fe::P1v(qy, 0)) * b[qx] + T(fe::P1v(qy, 1)) * b[3 + qx]);
+      }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 9; ++j) spl[j] = T(0);
+  }
+
+  const T* __restrict__ eq = eta_per_q ? L.eta + (size_t)cell * 27 : L.eta;
+  const T eta_cell = eta_per_q ? T(1) : L.eta[cell];
+  T dq[9];  // reference divergence at the points of plane z = comp
+#pragma unroll
+  for (int j = 0; j < 9; ++j) dq[j] = T(0);
+  const bool compressible = L.compressible != 0;
+
+  static_for<27>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    constexpr int qz = q / 9, j = q % 9;
+    T pq = T(0);
+    if constexpr (need_p) pq = __shfl_sync(full, spl[j], lb + qz);
+    T R0, R1, R2;
+    if constexpr (need_u) {
+      const T g0 = colloc_d<T, 3, q, 0>(U);
+      const T g1 = colloc_d<T, 3, q, 1>(U);
+      const T g2 = colloc_d<T, 3, q, 2>(U);
+      const T gcc = sel3(g0, g1, g2, comp);
+      const T gk1 = sel3(g0, g1, g2, k1);
+      const T gk2 = sel3(g0, g1, g2, k2);
+      const T r1 = __shfl_sync(full, gk2, l1);  // d_comp u_k1
+      const T r2 = __shfl_sync(full, gk1, l2);  // d_comp u_k2
+      const T eta = eta_per_q ? eq[q] : eta_cell;
+      const T a = eta * C.K[q];
+      T Rc;
+      if constexpr (op == OPK_STOKES) Rc = T(2) * (a * gcc) - pq;
+      else Rc = T(2) * (a * gcc);
+      if (op == OPK_STOKES || compressible) {
+        const T tot = gcc + __shfl_sync(full, gcc, l1) + __shfl_sync(full, gcc, l2);
+        if (compressible) Rc -= T(2.0 / 3.0) * (a * tot);
+        if (op == OPK_STOKES) dq[j] = comp == qz ? tot : dq[j];
+      }
+      const T Rk1 = a * (gk1 + r1);
+      const T Rk2 = a * (gk2 + r2);
+      R0 = sel3(Rc, Rk2, Rk1, comp);
+      R1 = sel3(Rk1, Rc, Rk2, comp);
+      R2 = sel3(Rk2, Rk1, Rc, comp);
+    } else {
+      R0 = comp == 0 ? -pq : T(0);
+      R1 = comp == 1 ? -pq : T(0);
+      R2 = comp == 2 ? -pq : T(0);
+    }
+    colloc_dT<T, 3, q, 0>(V, R0);
+    colloc_dT<T, 3, q, 1>(V, R1);
+    colloc_dT<T, 3, q, 2>(V, R2);
+  });
+  interpolate<T, 3, true>(V);
+  if (active) {
+    T* e = Eu + ((size_t)cell * 3 + comp) * 27;
+#pragma unroll
+    for (int n = 0; n < 27; ++n) e[n] = V[n];
+  }
+  if constexpr (op == OPK_STOKES) {
+    // pressure test -s JxW div, plane z = comp: f = -M_q dq, then back to the 8 nodes
+    T f[9];
+#pragma unroll
+    for (int jj = 0; jj < 9; ++jj) f[jj] = -sel3(C.M[jj], C.M[9 + jj], C.M[18 + jj], comp) * dq[jj];
+    T b[6];  // [ny][qx]
+#pragma unroll
+    for (int ny = 0; ny < 2; ++ny)
+#pragma unroll
+      for (int qx = 0; qx < 3; ++qx)
+        b[ny * 3 + qx] = T(fe::P1v(0, ny)) * f[qx] + T(fe::P1v(1, ny)) * f[3 + qx] + T(fe::P1v(2, ny)) * f[6 + qx];
+    T a[4];  // [ny][nx]
+#pragma unroll
+    for (int ny = 0; ny < 2; ++ny)
+#pragma unroll
+      for (int nx = 0; nx < 2; ++nx)
+        a[ny * 2 + nx] = T(fe::P1v(0, nx)) * b[ny * 3] + T(fe::P1v(1, nx)) * b[ny * 3 + 1] +
+                         T(fe::P1v(2, nx)) * b[ny * 3 + 2];
+    const T z0 = sel3(T(fe::P1v(0, 0)), T(fe::P1v(1, 0)), T(fe::P1v(2, 0)), comp);
+    const T z1 = sel3(T(fe::P1v(0, 1)), T(fe::P1v(1, 1)), T(fe::P1v(2, 1)), comp);
+    T YP[8];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      YP[i] = z0 * a[i];
+      YP[i + 4] = z1 * a[i];
+    }
+#pragma unroll
+    for (int n = 0; n < 8; ++n) YP[n] += __shfl_sync(full, YP[n], l1) + __shfl_sync(full, YP[n], l2);
+    if (active) {
+#pragma unroll
+      for (int n = 0; n < 8; ++n)
+        if (n % 3 == comp) Ep[(size_t)cell * 8 + n] = YP[n];
+    }
   }
 }
 
@@ -1118,6 +1313,91 @@ __global__ void __launch_bounds__(128) velocity_diag_kernel(LevelView<T> L, int 
     // all probes of structured levels have one owner thread (component pc)
     const bool owner = L.structured ? (k / nv == comp) : (comp == 0);
     if (probe_ok && owner && target >= 0) diag[target] += tot;
+  }
+}
+
+// A-block diagonal of lattice levels, directly: for the local DoF (component c,
+// node n), 2 eta eps(phi):eps(phi) = eta (|grad phi_n|^2 + kappa (d_c phi_n)^2)
+// with kappa = 1 (kappa = 1/3 with the compressible term), so
+//   K_cell[(c,n),(c,n)] = |det J| sum_e ih_e^2 A_e(n) + kappa |det J| ih_c^2 A_c(n),
+//   A_e(n) = sum_q w_q eta_q (d phi_n / d xi_e (q))^2,
+// 27 x 27 FMAs per direction with compile-time coefficients instead of 81
+// applications of the cell operator. Thread `comp` of a cell accumulates
+// A_comp(n) for all n; the three threads exchange them by shuffles and thread
+// comp writes the diagonal of its component. Constrained local DoFs get 0 (the
+// caller sets constrained rows). Output layout as the operator's cell pass
+// (slot-major E[slot][cell] or cell-major E[cell][slot]), so the level's gather
+// sums it into nodes.
+__host__ __device__ constexpr double q2_deriv_at_gauss(int q, int n) {
+  // phi_0' = 4x - 3, phi_1' = 4 - 8x, phi_2' = 4x - 1 at x = 1/2 + (q - 1) sqrt(15)/10
+  return n == 0 ? 4.0 * (0.5 + (q - 1) * fe::SQ15 / 10) - 3.0
+       : n == 1 ? 4.0 - 8.0 * (0.5 + (q - 1) * fe::SQ15 / 10)
+                : 4.0 * (0.5 + (q - 1) * fe::SQ15 / 10) - 1.0;
+}
+template <int dim, int e, int n, int q>
+__host__ __device__ constexpr double diag_weight() {
+  double g = 1.0;
+  for (int d = 0; d < dim; ++d) {
+    const int qd = (q / fe::pow3(d)) % 3, nd = (n / fe::pow3(d)) % 3;
+    g *= d == e ? q2_deriv_at_gauss(qd, nd) : fe::Sv(qd, nd);
+  }
+  return g * g * qweight<dim, q>();
+}
+
+template <typename T, int dim>
+__global__ void __launch_bounds__(128) lattice_diag_kernel(LevelView<T> L, T* __restrict__ Eu, int slot_major) {
+  pdl_wait();
+  constexpr int nv = Shape<dim>::nv, cpw = Shape<dim>::cpw;
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int grp = lane / dim;
+  int comp = lane - grp * dim;
+  bool active = grp < cpw;
+  if (!active) { grp = cpw - 1; comp = 0; }
+  const int lb = grp * dim;
+  const int idx = warp * cpw + grp;
+  active = active && idx < L.n_cells;
+  const int cell = active ? idx : 0;
+  StructuredCell<T, dim> sc;
+  structured_cell_lex<T, dim>(L, cell, sc);
+  const bool per_q = L.eta_n != 1;
+  const T eta_cell = per_q ? T(0) : L.eta[cell];
+  const T* __restrict__ eq = per_q ? L.eta + (size_t)cell * nv : L.eta;
+  T acc[nv];
+#pragma unroll
+  for (int n = 0; n < nv; ++n) acc[n] = T(0);
+  static_for<nv>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    const T eta = per_q ? eq[q] : eta_cell;
+    static_for<nv>([&](auto nc) {
+      constexpr int n = decltype(nc)::value;
+      T w;
+      if constexpr (dim == 3)
+        w = sel3(T(diag_weight<3, 0, n, q>()), T(diag_weight<3, 1, n, q>()), T(diag_weight<3, 2, n, q>()), comp);
+      else
+        w = comp == 0 ? T(diag_weight<2, 0, n, q>()) : T(diag_weight<2, 1, n, q>());
+      acc[n] += eta * w;
+    });
+  });
+  const T kappa = L.compressible ? T(1.0 / 3.0) : T(1);
+  T ih2[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) ih2[d] = d < dim ? L.inv_h[d] * L.inv_h[d] : T(0);
+  const T own = (T(1) + kappa) * (dim == 3 ? sel3(ih2[0], ih2[1], ih2[2], comp) : (comp == 0 ? ih2[0] : ih2[1]));
+  const T w1 = dim == 3 ? sel3(ih2[1], ih2[2], ih2[0], comp) : (comp == 0 ? ih2[1] : ih2[0]);
+  const T w2 = dim == 3 ? sel3(ih2[2], ih2[0], ih2[1], comp) : T(0);
+#pragma unroll
+  for (int n = 0; n < nv; ++n) {
+    const T a1 = __shfl_sync(full, acc[n], lb + (comp + 1) % dim);
+    T v = own * acc[n] + w1 * a1;
+    if constexpr (dim == 3) v += w2 * __shfl_sync(full, acc[n], lb + (comp + 2) % dim);
+    v *= L.det;
+    if (active) {
+      const int slot = comp * nv + n;
+      Eu[slot_major ? (size_t)slot * L.n_cells + cell : (size_t)cell * dim * nv + slot] =
+          structured_zero<T, dim>(L, sc, comp, n) ? T(0) : v;
+    }
   }
 }
 

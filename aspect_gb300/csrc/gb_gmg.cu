@@ -44,6 +44,7 @@ struct Handle {
   double s = 1.0;
   int compressible = 0, projection = 0;
   int visc_n_per_cell = 0;  // n_per_cell of the last successful set_viscosity
+  int n_sm = 1;             // streaming multiprocessors of the handle's GPU
   double eta_min = 0, eta_max = 0;
   bool setup_done = false, visc_done = false;
   bool prec_done[2] = {false, false};  // per precision (0 fp64, 1 fp32)
@@ -160,12 +161,36 @@ void mass_lattice(Handle& H, Level& L, const LevelView<T>& v, int epi, GatherArg
   ++H.cell_launches;
 }
 
+// FP32 A-block application of a large lattice level through the fused kernel
+// (one cell-and-gather pass plus the face pass); false when the level does not use it
 template <typename T>
-void apply_op(Handle& H, int lev, int op, const T* su, const T* sp, T* du, T* dp) {
+bool fused_a(Handle& H, Level& L, int epi, const GatherArgs<T>& a) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (L.fused_tz > 0) {
+      launch_fused_a(L.view<float>(H.s, H.compressible), epi, a, L.f32.Fa.p, L.fused_tz, H.st);
+      H.cell_launches += 2;
+      return true;
+    }
+  }
+  return false;
+}
+
+// outer = true: an operator of the outer solver (FGMRES product, expensive inner
+// solves, rhs correction); it takes the level's per-point table where the level
+// keeps one for them (no averaging), the multigrid operators the level table.
+template <typename T>
+void apply_op(Handle& H, int lev, int op, const T* su, const T* sp, T* du, T* dp, bool outer = false) {
   Level& L = H.levels[lev];
   LevelDev<T>& D = L.dev<T>();
-  const LevelView<T> v = L.view<T>(H.s, H.compressible);
-  if (op == OPK_MASS && L.structured) {
+  const bool own_table = outer && L.eta_active_n > 0;
+  const LevelView<T> v = own_table ? L.view_outer<T>(H.s, H.compressible) : L.view<T>(H.s, H.compressible);
+  if (op == OPK_A && !own_table) {
+    GatherArgs<T> a{};
+    a.x = const_cast<T*>(su);
+    a.y = du;
+    if (fused_a<T>(H, L, EPI_STORE, a)) return;
+  }
+  if (op == OPK_MASS && L.structured && !own_table) {  // per-cell matrices of the level table
     GatherArgs<T> a{};
     a.x = const_cast<T*>(sp);
     a.y = dp;
@@ -201,6 +226,16 @@ template <typename T>
 void level_op_cheb(Handle& H, int lev, int block, T* x, const T* b, const T* dinv, T* d, double f1, double f2) {
   Level& L = H.levels[lev];
   LevelDev<T>& D = L.dev<T>();
+  if (block == 0) {
+    GatherArgs<T> a{};
+    a.x = x;
+    a.b = b;
+    a.dinv = dinv;
+    a.d = d;
+    a.f1 = (T)f1;
+    a.f2 = (T)f2;
+    if (fused_a<T>(H, L, EPI_CHEB, a)) return;
+  }
   const LevelView<T> v = L.view<T>(H.s, H.compressible);
   launch_cell_pass<T>(v, block == 0 ? OPK_A : OPK_MASS, x, x, D.Eu.p, D.Ep.p, H.st);
   ++H.cell_launches;
@@ -220,6 +255,13 @@ template <typename T>
 void level_op_resid(Handle& H, int lev, int block, const T* x, const T* b, T* y) {
   Level& L = H.levels[lev];
   LevelDev<T>& D = L.dev<T>();
+  if (block == 0) {
+    GatherArgs<T> a{};
+    a.x = const_cast<T*>(x);
+    a.b = b;
+    a.y = y;
+    if (fused_a<T>(H, L, EPI_RESID, a)) return;
+  }
   const LevelView<T> v = L.view<T>(H.s, H.compressible);
   if (block == 1 && L.structured) {
     GatherArgs<T> a{};
@@ -251,13 +293,28 @@ void compute_diagonals(Handle& H, int lev) {
   D.dinvM.zero(H.st);
   ProbesView<T> pu{L.probe_ptr.p, L.probe_g.p, L.probe_eptr.p, L.probe_li.p, D.probe_w.p};
   ProbesView<T> pp{L.pprobe_ptr.p, L.pprobe_g.p, L.pprobe_eptr.p, L.pprobe_li.p, D.pprobe_w.p};
+  // lattice levels: the velocity diagonal directly per cell (lattice_diag_kernel),
+  // summed into nodes by the level's own gather (constrained rows are set below)
+  const bool direct = L.structured && v.geom == GEOM_CART;
+  if (direct) {
+    launch_lattice_diag<T>(v, D.Eu.p, cell_pass_slot_major<T>(v, OPK_A), H.st);
+    ++H.cell_launches;
+    GatherArgs<T> a{};
+    a.E = D.Eu.p;
+    a.x = D.dinvA.p;
+    a.y = D.dinvA.p;
+    gather<T>(H, L, v, 0, EPI_STORE, a, OPK_A);
+  }
   for (int k = 0; k < L.n_colours; ++k) {
     const int cnt = L.colour_count[k];
     if (!cnt) continue;
     const int begin = L.structured ? 0 : L.colour_begin[k];
-    launch_velocity_diag<T>(v, k, begin, cnt, pu, D.dinvA.p, H.st);
+    if (!direct) {
+      launch_velocity_diag<T>(v, k, begin, cnt, pu, D.dinvA.p, H.st);
+      ++H.cell_launches;
+    }
     launch_mass_diag<T>(v, k, begin, cnt, pp, D.dinvM.p, H.st);
-    H.cell_launches += 2;
+    ++H.cell_launches;
   }
   GB_CUDA(cudaStreamSynchronize(H.st));
   for (int block = 0; block < 2; ++block) {
@@ -647,7 +704,7 @@ void vcycle(Handle& H, int block, int prec, const double* src, double* dst) {
 // ---------------------------------------------------------------- FP64 active-level operators
 void stokes64(Handle& H, const double* x, double* y) {
   Level& F = H.top();
-  apply_op<double>(H, H.n_levels - 1, OPK_STOKES, x, x + F.n_u, y, y + F.n_u);
+  apply_op<double>(H, H.n_levels - 1, OPK_STOKES, x, x + F.n_u, y, y + F.n_u, true);
   ++H.n_stokes64;
 }
 // Stokes operator with FP32 arithmetic on FP64 vectors (inner solves of GMRES_IR)
@@ -655,7 +712,7 @@ void stokes32(Handle& H, const double* x, double* y) {
   Level& F = H.top();
   const long n = F.n_u + F.n_p;
   v_cast<double, float>(n, x, H.f32_a.p, H.st);
-  apply_op<float>(H, H.n_levels - 1, OPK_STOKES, H.f32_a.p, H.f32_a.p + F.n_u, H.f32_b.p, H.f32_b.p + F.n_u);
+  apply_op<float>(H, H.n_levels - 1, OPK_STOKES, H.f32_a.p, H.f32_a.p + F.n_u, H.f32_b.p, H.f32_b.p + F.n_u, true);
   v_cast<float, double>(n, H.f32_b.p, y, H.st);
 }
 
@@ -702,8 +759,8 @@ int cg_solve(Handle& H, int block, int prec, long n, double* x, const double* b,
   double* p = H.cg_p.p;
   double* q = H.cg_q.p;
   auto op = [&](const double* a, double* y) {
-    if (block == 0) apply_op<double>(H, top, OPK_A, a, nullptr, y, nullptr);
-    else apply_op<double>(H, top, OPK_MASS, nullptr, a, nullptr, y);
+    if (block == 0) apply_op<double>(H, top, OPK_A, a, nullptr, y, nullptr, true);
+    else apply_op<double>(H, top, OPK_MASS, nullptr, a, nullptr, y, true);
   };
   auto pre = [&](const double* a, double* y) { vcycle_exec(H, block, prec, a, y); };
   GB_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), H.st));
@@ -1316,6 +1373,7 @@ void gb_gmg_default_options(gb_gmg_options* o) {
   o->schur_smoothing_steps = 4;
   o->force_indexed_layout = 0;
   o->coarse_solver = GB_GMG_COARSE_CHEBYSHEV;
+  o->fused_a_min_cells = 65536;
 }
 
 void gb_gmg_default_solve_params(gb_gmg_solve_params* p) {
@@ -1343,7 +1401,10 @@ int gb_gmg_create(const gb_gmg_options* opt, int dim, int degree_v, int n_levels
   g->h.n_levels = n_levels;
   g->h.levels.resize(n_levels);
   for (auto& L : g->h.levels) L.dim = dim;
-  if (cudaStreamCreateWithFlags(&g->h.st, cudaStreamNonBlocking) != cudaSuccess) {
+  int dev = 0;
+  if (cudaStreamCreateWithFlags(&g->h.st, cudaStreamNonBlocking) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&g->h.n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    if (g->h.st) cudaStreamDestroy(g->h.st);
     delete g;
     return GB_GMG_CUDA_ERROR;
   }
@@ -1371,7 +1432,7 @@ int gb_gmg_set_level_mesh(gb_gmg* g, int level, int64_t n_cells, const int32_t* 
     GB_CHECK(level >= 0 && level < H.n_levels, 1, "level out of range");
     GB_CHECK(n_cells > 0 && n_u > 0 && n_p > 0 && cdu && cdp && geom, 1, "empty mesh or null array");
     GB_CHECK(n_u < (1LL << 31) && n_p < (1LL << 31), 1, "more than 2^31 DoFs per block");
-    GB_CHECK(geometry_kind == 0 || geometry_kind == 1, 1, "unknown geometry kind");
+    GB_CHECK(geometry_kind >= 0 && geometry_kind <= 2, 1, "unknown geometry kind");
     gb::Level& L = H.levels[level];
     const int nv = H.dim == 3 ? 27 : 9, np = H.dim == 3 ? 8 : 4;
     L.n_cells = n_cells;
@@ -1382,7 +1443,9 @@ int gb_gmg_set_level_mesh(gb_gmg* g, int level, int64_t n_cells, const int32_t* 
     for (int v : L.cdu) GB_CHECK(v >= 0 && v < n_u, 1, "velocity DoF index out of range");
     for (int v : L.cdp) GB_CHECK(v >= 0 && v < n_p, 1, "pressure DoF index out of range");
     L.geom_kind = geometry_kind;
-    const size_t ng = geometry_kind == 0 ? (size_t)n_cells * 2 * H.dim : (size_t)n_cells * nv * H.dim;
+    const size_t ng = geometry_kind == 0   ? (size_t)n_cells * 2 * H.dim
+                      : geometry_kind == 1 ? (size_t)n_cells * nv * H.dim
+                                           : (size_t)n_cells * nv * (H.dim * H.dim + 1);
     L.geom.assign(geom, geom + ng);
     L.cu.init(n_u);
     L.cp.init(n_p);
@@ -1439,6 +1502,18 @@ int gb_gmg_finalize_setup(gb_gmg* g) {
     for (auto& L : H.levels) GB_CHECK(L.n_cells > 0, 2, "a level has no mesh");
     for (auto& L : H.levels) gb::setup_level(L, H.opt.force_indexed_layout != 0);
     for (int l = 1; l < H.n_levels; ++l) gb::setup_transfer(H.levels[l], H.levels[l - 1]);
+    for (auto& L : H.levels) {  // FP32 A-block applications of large lattice levels: fused kernel
+      L.fused_tz = 0;
+      L.f32.Fa.release();
+      const long min_cells = H.opt.fused_a_min_cells > 0 ? H.opt.fused_a_min_cells : -1;
+      if (min_cells < 0) continue;
+      const gb::LevelView<float> v = L.view<float>(H.s, 0);
+      const int tz = gb::fused_a_tile_layers(v, H.n_sm, min_cells);
+      if (tz > 0 && gb::fused_a_prepare()) {
+        L.f32.Fa.alloc(gb::fused_a_face_floats(v, tz));
+        L.fused_tz = tz;
+      }
+    }
     gb::ensure_workspace(H);
     GB_CUDA(cudaStreamSynchronize(H.st));
     H.reset_graphs();
@@ -1562,7 +1637,7 @@ int gb_gmg_correct_stokes_rhs(gb_gmg* g, const double* u0, double* rhs) {
     GB_CUDA(cudaMemcpyAsync(a, u0, n * sizeof(double), cudaMemcpyHostToDevice, H.st));
     gb::to_internal(H, top, a, b, true, true);
     gb::LevelDev<double>& D = F.f64;
-    const gb::LevelView<double> v = F.view<double>(H.s, H.compressible);
+    const gb::LevelView<double> v = F.view_outer<double>(H.s, H.compressible);
     gb::LevelView<double> plain = v;
     plain.structured = 0;
     plain.cdu = F.cdu_raw_d.p;
@@ -1635,7 +1710,7 @@ int gb_gmg_vmult_device(gb_gmg* g, int op, int precision, const double* d_src, d
     gb::Level& L = H.levels[top];
     gb::to_internal(H, top, d_src, H.stage_a.p, true, true);
     if (precision == GB_GMG_FP64) {
-      gb::apply_op<double>(H, top, 0, H.stage_a.p, H.stage_a.p + L.n_u, H.stage_b.p, H.stage_b.p + L.n_u);
+      gb::apply_op<double>(H, top, 0, H.stage_a.p, H.stage_a.p + L.n_u, H.stage_b.p, H.stage_b.p + L.n_u, true);
     } else {
       gb::stokes32(H, H.stage_a.p, H.stage_b.p);
     }
@@ -1833,7 +1908,7 @@ int gb_gmg_adjoint_gradient(gb_gmg* g, const double* u, const double* lambda, do
     gb::to_internal(H, top, H.stage_a.p, H.wv.p, true, false);
     double* gcell = H.tv.p;  // n_cells <= n_u
     GB_CUDA(cudaMemsetAsync(gcell, 0, F.n_cells * sizeof(double), H.st));
-    const gb::LevelView<double> v = F.view<double>(H.s, H.compressible);
+    const gb::LevelView<double> v = F.view_outer<double>(H.s, H.compressible);
     for (int k = 0; k < F.n_colours; ++k) {
       const int cnt = F.colour_count[k];
       if (!cnt) continue;

@@ -87,6 +87,30 @@ void launch_cell_pass<GB_T>(const LevelView<GB_T>& L, int op, const GB_T* su, co
       return;
     }
   }
+#else
+  // FP64 velocity-test operators of isotropic 3D lattice levels (cubic cells)
+  if (op != OPK_MASS && L.dim == 3 && L.structured && L.geom == GEOM_CART && L.inv_h[0] == L.inv_h[1] &&
+      L.inv_h[1] == L.inv_h[2]) {
+    IsoCoef<double> C;
+    const double ih = L.inv_h[0];
+    for (int q = 0; q < 27; ++q) {
+      const double w = fe::Wv(q % 3) * fe::Wv((q / 3) % 3) * fe::Wv(q / 9);
+      C.K[q] = ih * ih * L.det * w;
+      C.M[q] = L.s * ih * L.det * w;
+    }
+    const int g = cell_grid<3>(L.n_cells);
+    const bool pq = L.eta_n != 1;
+#define GB_ISO(OP)                                                                                   \
+  {                                                                                                  \
+    if (pq) lattice_iso_kernel_f64<OP, true><<<g, kCellThreads, 0, s>>>(L, C, su, sp, Eu, Ep);       \
+    else lattice_iso_kernel_f64<OP, false><<<g, kCellThreads, 0, s>>>(L, C, su, sp, Eu, Ep);         \
+  }
+    if (op == OPK_STOKES) GB_ISO(OPK_STOKES)
+    else if (op == OPK_A) GB_ISO(OPK_A)
+    else GB_ISO(OPK_BT)
+#undef GB_ISO
+    return;
+  }
 #endif
   if (L.dim == 3) cell_pass_dim<3>(L, op, su, sp, Eu, Ep, s);
   else cell_pass_dim<2>(L, op, su, sp, Eu, Ep, s);
@@ -124,6 +148,13 @@ void launch_velocity_diag<GB_T>(const LevelView<GB_T>& L, int colour, int begin,
     velocity_diag_kernel<GB_T, 3><<<cell_grid<3>(count), kCellThreads, 0, s>>>(L, colour, begin, count, pr.ptr, pr.g, pr.eptr, pr.li, pr.w, diag);
   else
     velocity_diag_kernel<GB_T, 2><<<cell_grid<2>(count), kCellThreads, 0, s>>>(L, colour, begin, count, pr.ptr, pr.g, pr.eptr, pr.li, pr.w, diag);
+}
+
+template <>
+void launch_lattice_diag<GB_T>(const LevelView<GB_T>& L, GB_T* Eu, bool slot_major, cudaStream_t s) {
+  if (L.n_cells <= 0) return;
+  if (L.dim == 3) lattice_diag_kernel<GB_T, 3><<<cell_grid<3>(L.n_cells), kCellThreads, 0, s>>>(L, Eu, slot_major);
+  else lattice_diag_kernel<GB_T, 2><<<cell_grid<2>(L.n_cells), kCellThreads, 0, s>>>(L, Eu, slot_major);
 }
 
 template <>

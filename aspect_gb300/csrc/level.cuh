@@ -56,6 +56,8 @@ struct LevelDev {
   DevBuf<T> gu_w, gp_w;  // gather weights (general levels)
   DevBuf<T> Eu, Ep;      // per-cell contributions of pass 1
   DevBuf<T> Mp;          // lattice levels: per-cell pressure mass matrices [cell][np][np]
+  DevBuf<T> Fa;          // fused A-block operator (FP32): per-tile partial sums of face nodes
+  DevBuf<T> eta_active;  // finest level without averaging: per-point table of the outer operators
   // V-cycle work vectors (A block: n_u, Schur block: n_p)
   DevBuf<T> solA, defA, tA, dA, solM, defM, tM, dM;
   double eigA[2] = {0, 0}, eigM[2] = {0, 0};
@@ -81,6 +83,7 @@ struct Level {
   std::vector<int> perm_u, perm_p;        // caller DoF -> internal DoF
   std::vector<int> internal_of_cell;      // caller cell -> internal cell
   std::vector<int> cell_of_internal;      // internal cell -> caller cell
+  int fused_tz = 0;  // > 0: FP32 A-block applications use the fused kernel, tiles of this many layers
   int n_colours = 0;
   std::vector<int> colour_begin, colour_count;
   std::vector<int> cons_u, cons_p;        // internal constrained DoFs
@@ -100,11 +103,25 @@ struct Level {
   // viscosity table, internal cell order
   std::vector<double> eta;
   int eta_n = 1;
+  // without averaging (GB_GMG_VISC_NONE), finest level only: the per-point table
+  // of the outer operators, caller cell order (eta_active_n = 0: none)
+  std::vector<double> eta_active;
+  int eta_active_n = 0;
 
   template <typename T>
   LevelDev<T>& dev();
   template <typename T>
   LevelView<T> view(double s, int compressible);
+  // the view of the outer operators: the per-point table where the level keeps one
+  template <typename T>
+  LevelView<T> view_outer(double s, int compressible) {
+    LevelView<T> v = view<T>(s, compressible);
+    if (eta_active_n > 0) {
+      v.eta = dev<T>().eta_active.p;
+      v.eta_n = eta_active_n;
+    }
+    return v;
+  }
   template <typename T>
   GatherCsr<T> csr(int block) {
     LevelDev<T>& D = dev<T>();

@@ -326,6 +326,20 @@ void setup_general(Level& L) {
     }
     L.f64.gbox.upload(gb);
     L.f32.gbox.upload(std::vector<float>(gb.begin(), gb.end()));
+  } else if (L.geom_kind == 2) {
+    // the caller's per-point inverse Jacobians and |det J|, in internal cell order
+    const int stride = d * d + 1;
+    std::vector<double> gt((size_t)L.n_cells * nq * stride);
+    for (long c = 0; c < L.n_cells; ++c) {
+      const long ic = L.internal_of_cell[c];
+      for (int q = 0; q < nq; ++q) {
+        const double* src = &L.geom[((size_t)c * nq + q) * stride];
+        GB_CHECK(src[d * d] > 0 && std::isfinite(src[d * d]), 1, "|det J| of a geometry table entry must be positive");
+        std::copy(src, src + stride, &gt[((size_t)ic * nq + q) * stride]);
+      }
+    }
+    L.f64.gtab.upload(gt);
+    L.f32.gtab.upload(std::vector<float>(gt.begin(), gt.end()));
   } else {
     const double g3[3] = {0.5 - std::sqrt(15.0) / 10, 0.5, 0.5 + std::sqrt(15.0) / 10};
     const double q2n[3] = {0.0, 0.5, 1.0};
@@ -578,6 +592,7 @@ void compute_level_viscosity(std::vector<Level>& levels, const double* eta_in, i
       for (int e = 0; e < d; ++e) det *= Fl.geom[c * 2 * d + d + e];
       return w * det;
     }
+    if (Fl.geom_kind == 2) return w * Fl.geom[((size_t)c * nq + q) * (d * d + 1) + d * d];
     // Q2 geometry: recompute |det J| at the point
     const double q2n[3] = {0.0, 0.5, 1.0};
     double v1[3][3], d1[3][3];
@@ -599,7 +614,18 @@ void compute_level_viscosity(std::vector<Level>& levels, const double* eta_in, i
     return w * std::fabs(det);
   };
   std::vector<std::vector<double>> dg(nlev);
-  if (projection == 0) {
+  for (auto& L : levels) {
+    L.eta_active.clear();
+    L.eta_active_n = 0;
+  }
+  if (projection == 2) {
+    // no averaging: the outer operators keep the per-point values, every level's
+    // table (the finest included) is the cellwise projection below
+    GB_CHECK(n_per_cell == nq, 1, "no averaging needs one value per quadrature point");
+    Fl.eta_active.assign(eta_in, eta_in + (size_t)Fl.n_cells * nq);
+    Fl.eta_active_n = nq;
+  }
+  if (projection == 0 || projection == 2) {
     dg[nlev - 1].assign(Fl.n_cells, 0.0);
     for (long c = 0; c < Fl.n_cells; ++c) {
       if (n_per_cell == 1) {
@@ -626,7 +652,7 @@ void compute_level_viscosity(std::vector<Level>& levels, const double* eta_in, i
     }
     for (int l = 0; l < nlev; ++l) {
       Level& L = levels[l];
-      const bool per_q = (l == nlev - 1 && n_per_cell == nq);
+      const bool per_q = (l == nlev - 1 && n_per_cell == nq && projection == 0);
       L.eta_n = per_q ? nq : 1;
       L.eta.assign((size_t)L.n_cells * L.eta_n, 0);
       for (long c = 0; c < L.n_cells; ++c) {
@@ -637,6 +663,7 @@ void compute_level_viscosity(std::vector<Level>& levels, const double* eta_in, i
       }
     }
   } else {
+    GB_CHECK(projection == 1, 1, "unknown viscosity projection");
     GB_CHECK(n_per_cell == nq, 1, "projection to Q1 needs one value per quadrature point");
     dg[nlev - 1].assign((size_t)Fl.n_cells * ncv, 0.0);
     for (long c = 0; c < Fl.n_cells; ++c) {
@@ -695,6 +722,18 @@ void upload_viscosity(Level& L, double s) {
   }
   L.f64.eta.upload(e);
   L.f32.eta.upload(std::vector<float>(e.begin(), e.end()));
+  if (L.eta_active_n > 0) {
+    std::vector<double> ea((size_t)L.n_cells * L.eta_active_n);
+    for (long c = 0; c < L.n_cells; ++c) {
+      const long ic = L.internal_of_cell[c];
+      for (int k = 0; k < L.eta_active_n; ++k) ea[ic * L.eta_active_n + k] = L.eta_active[c * L.eta_active_n + k];
+    }
+    L.f64.eta_active.upload(ea);
+    L.f32.eta_active.upload(std::vector<float>(ea.begin(), ea.end()));
+  } else {
+    L.f64.eta_active.release();
+    L.f32.eta_active.release();
+  }
   if (!L.structured) return;
   // per-cell local pressure mass matrices of a lattice level:
   // M[i][j] = sum_q s^2 / eta_q * |det J| w_q psi_i(q) psi_j(q)
@@ -780,7 +819,7 @@ size_t Level::device_bytes() const {
          D.pprobe_w.bytes() + D.Pu_val.bytes() + D.PuT_val.bytes() + D.Pp_val.bytes() + D.PpT_val.bytes() +
          D.dinvA.bytes() + D.dinvM.bytes() + D.solA.bytes() + D.defA.bytes() + D.tA.bytes() + D.dA.bytes() +
          D.solM.bytes() + D.defM.bytes() + D.tM.bytes() + D.dM.bytes() + D.gu_w.bytes() + D.gp_w.bytes() +
-         D.Eu.bytes() + D.Ep.bytes() + D.Mp.bytes();
+         D.Eu.bytes() + D.Ep.bytes() + D.Mp.bytes() + D.Fa.bytes() + D.eta_active.bytes();
   };
   add(f32);
   add(f64);

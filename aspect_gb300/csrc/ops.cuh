@@ -28,6 +28,20 @@ void launch_gather(const LevelView<T>& L, int block, int epi, const GatherCsr<T>
 // one-pass pressure mass operator of a lattice level (Mc: per-cell local matrices)
 template <typename T>
 void launch_mass_lattice(const LevelView<T>& L, const T* Mc, int epi, const GatherArgs<T>& a, cudaStream_t s);
+// Fused FP32 A-block operator of large 3D lattice levels (ablock_fused.cu):
+// cell layers per tile for a level (0: the level does not qualify), the face
+// buffer it needs (floats), the one-time kernel attribute set-up (call outside
+// stream capture), and the two launches of one application with epilogue
+// EPI_STORE, EPI_RESID or EPI_CHEB.
+int fused_a_tile_layers(const LevelView<float>& L, int n_sm, long min_cells);
+size_t fused_a_face_floats(const LevelView<float>& L, int tz);
+bool fused_a_prepare();
+void launch_fused_a(const LevelView<float>& L, int epi, const GatherArgs<float>& a, float* F, int tz,
+                    cudaStream_t s);
+// A-block diagonal contributions of a lattice level, one pass over all cells
+// (set-up only; the level's gather sums them)
+template <typename T>
+void launch_lattice_diag(const LevelView<T>& L, T* Eu, bool slot_major, cudaStream_t s);
 // diagonals, colour by colour (set-up only)
 template <typename T>
 void launch_velocity_diag(const LevelView<T>& L, int colour, int begin, int count, const ProbesView<T>& pr,

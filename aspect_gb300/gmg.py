@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(HERE, "libgb_gmg.so")
 OP_STOKES, OP_A, OP_BT, OP_MASS = 0, 1, 2, 3
 FP64, FP32 = 0, 1
 GMRES, GMRES_IR, IDR = 0, 1, 2
-VISC_DGQ0, VISC_DGQ1 = 0, 1
+VISC_DGQ0, VISC_DGQ1, VISC_NONE = 0, 1, 2
 COARSE_CHEBYSHEV, COARSE_DENSE_FP64 = 0, 1
 
 STATUS = {0: "OK", 1: "INVALID_ARGUMENT", 2: "NOT_READY", 3: "CUDA_ERROR", 4: "NO_CONVERGENCE",
@@ -47,7 +47,8 @@ class Options(ctypes.Structure):
                 ("smoothing_range", ctypes.c_double), ("eig_cg_iterations", ctypes.c_int),
                 ("coarse_degree", ctypes.c_int), ("coarse_range", ctypes.c_double),
                 ("coarse_eig_cg_iterations", ctypes.c_int), ("schur_smoothing_steps", ctypes.c_int),
-                ("force_indexed_layout", ctypes.c_int), ("coarse_solver", ctypes.c_int)]
+                ("force_indexed_layout", ctypes.c_int), ("coarse_solver", ctypes.c_int),
+                ("fused_a_min_cells", ctypes.c_int)]
 
 
 class SolveParams(ctypes.Structure):

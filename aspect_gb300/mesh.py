@@ -14,7 +14,9 @@ Conventions (shared with ``include/gb_gmg.h``):
   velocity components blocked (``c * 3**dim + node``);
 * geometry kind 0 (``GEOM_BOX``): per cell ``[x0.., h..]`` (lower corner and
   edge lengths of an axis-aligned box); kind 1 (``GEOM_Q2``): the 3**dim Q2
-  support points of the cell mapping, ``[node][dim]``;
+  support points of the cell mapping, ``[node][dim]``; kind 2 (``GEOM_TABLE``):
+  per QGauss(3) point the inverse Jacobian and ``|det J|`` of the caller's own
+  mapping (``to_table_geometry``; the solver only, not the harness's assembly);
 * a constraint line is ``x[row] = sum_k w_k x[col_k] + inhomogeneity``; a line
   with no entries is a Dirichlet constraint (zero in the homogeneous operators);
 * child index of a fine cell = sum_d bit_d << d, bit_d = which half of the
@@ -28,6 +30,7 @@ import numpy as np
 
 GEOM_BOX = 0
 GEOM_Q2 = 1
+GEOM_TABLE = 2
 
 
 @dataclasses.dataclass
@@ -278,6 +281,21 @@ def to_q2_geometry(level: LevelMesh, distortion=None) -> LevelMesh:
         flat = X.reshape(-1, level.dim)
         X = (flat + distortion(flat)).reshape(X.shape)
     return dataclasses.replace(level, geom_kind=GEOM_Q2, geometry=X.reshape(level.n_cells, -1))
+
+
+def to_table_geometry(level: LevelMesh, jacobians: np.ndarray | None = None) -> LevelMesh:
+    """Same level with GEOM_TABLE cell geometry: per cell and QGauss(3) point the
+    inverse Jacobian (d xi_d / d x_e at [d*dim+e]) and |det J|. ``jacobians``
+    (n_cells, 3**dim, dim, dim) [x-component, xi-direction] are the caller's
+    mapping at the Gauss points; by default the level's own mapping."""
+    from . import fe
+    gp = fe.tensor_points(level.dim, fe.gauss(3)[0])
+    J = level.jacobians(gp) if jacobians is None else np.asarray(jacobians, float)
+    inv = np.linalg.inv(J)
+    det = np.abs(np.linalg.det(J))
+    d = level.dim
+    table = np.concatenate([inv.reshape(level.n_cells, len(gp), d * d), det[..., None]], axis=-1)
+    return dataclasses.replace(level, geom_kind=GEOM_TABLE, geometry=table.reshape(level.n_cells, -1))
 
 
 def smooth_distortion(amplitude: float = 0.03):

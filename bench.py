@@ -41,22 +41,36 @@ METRIC = "Stokes solve time & operator GDoF/s: FP32-MG vs FP64-MG at 1e-8 FP64 r
 WORKLOAD = "sinkers_32^3_Q2Q1_eta1e6_q1proj_fgmres_fp32mg_tol1e-8"
 TOL = 1e-8
 N_CELLS_1D = 32
-# Arithmetic per cell of the two cell kernels, counted from their source (an FMA
-# counts 2): the FP32 lattice A-block cell pass (3 x 270 interpolation, 27 x 141
-# per point, 3 x 270 transposed interpolation) and the FP64 Stokes cell pass
-# (3 threads x (270 + 27 x 86 + 270)).
-FLOPS_A_CELL_F32 = 5427
-FLOPS_STOKES_CELL_F64 = 8586
-# nominal CUDA-core peaks (no measured figure is recorded for them): FP32 =
-# 152 SMs x 128 lanes x 2 x 2.07 GHz; FP64 = GB300's published 1.25 TFLOP/s
-FP32_PEAK_TFLOPS = 80.5
-FP64_PEAK_TFLOPS = 1.25
-# dram__bytes_read.sum + dram__bytes_write.sum of one finest-level launch of each
-# cell pass (ncu --set full of `bench.py --profile-op stokes_cell_pass_fp64` /
-# `a_cell_pass_fp32`, cold cache, summarised in profiles/): the reads of u, p
-# and eta; the per-cell outputs stay in L2
-STOKES_CELL_PASS_F64_DRAM_BYTES = 14206720
-A_CELL_PASS_F32_DRAM_BYTES = 6853888
+# Algorithmic arithmetic per cell (the unit of the FP rooflines), counted by
+# the sum-factorisation formula of the operator, not from any kernel's
+# instructions (an FMA counts 2): A block = 3 components x 6 sweeps x 81 FMA x
+# 2 (evaluate and integrate) x 2 + 27 points x 40 = 6,912; the Stokes operator
+# adds the Q1 pressure by sum factorisation (3 sweeps of 2 -> 3 points each
+# way, 2 x 114 FMA) and about 10 flop per point: 6,912 + 456 + 270 = 7,638.
+ALG_FLOPS_A_CELL = 6912
+ALG_FLOPS_STOKES_CELL = 7638
+# dram__bytes_read.sum + dram__bytes_write.sum of one finest-level launch of the
+# FP64 Stokes cell pass (ncu, cold cache, `bench.py --profile-op
+# stokes_cell_pass_fp64`, profiles/): the reads of u, p and eta and the writes
+# of the per-cell contributions that leave L2
+STOKES_CELL_PASS_F64_DRAM_BYTES = None
+
+
+def measured_fp_peaks():
+    """FP64 and FP32 FMA throughput of this GPU in TFLOP/s, measured live by the
+    FMA-chain probe (aspect_gb300/csrc/peak_probe.cu, libgb_probe.so)."""
+    import ctypes
+    lib = ctypes.CDLL(os.path.join(ROOT, "aspect_gb300", "libgb_probe.so"))
+    out = {}
+    for key, fn in (("fp64", lib.gb_probe_fp64_fma_tflops), ("fp32", lib.gb_probe_fp32_fma_tflops)):
+        v = ctypes.c_double()
+        fn.argtypes = [ctypes.POINTER(ctypes.c_double)]
+        best = 0.0
+        for _ in range(3):
+            if fn(ctypes.byref(v)) == 0:
+                best = max(best, v.value)
+        out[key] = best
+    return out
 
 
 def log(*a):
@@ -237,10 +251,24 @@ def run_gpu(args):
     f = P.fine
     n = P.n_dofs
     log("problem built", n)
+    # set-up in the handler's phases: setup_dofs (once per mesh), assemble (set
+    # the viscosity: once per nonlinear iteration in ASPECT) and
+    # build_preconditioner (diagonals, eigenvalue estimates, captured V-cycles:
+    # also once per nonlinear iteration)
     t0 = time.perf_counter()
-    g = gmg.from_problem(P)
-    setup_s = time.perf_counter() - t0
-    log("setup done", setup_s)
+    g = gmg.StokesMatrixFreeGPU(3, len(P.levels))
+    g.setup_dofs(P.levels)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    g.assemble(P.eta, P.projection, P.pressure_scaling)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    g.build_preconditioner()
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    setup = {"setup_dofs_s": t1 - t0, "assemble_s": t2 - t1, "build_preconditioner_s": t3 - t2}
+    setup_s = t3 - t0
+    log("setup done", setup)
 
     rhs_d = torch.from_numpy(P.rhs).to(dev)
     sol_d = torch.zeros(n, dtype=torch.float64, device=dev)
@@ -345,21 +373,22 @@ def run_gpu(args):
              "A_vmult_fp32": f.n_u / ops["A_vmult_fp32"] / 1e9,
              "A_vmult_fp64": f.n_u / ops["A_vmult_fp64"] / 1e9}
     # --- rooflines, each kernel timed alone on the finest level with CUDA events
-    # on the library's stream: the FP32 lattice cell pass of the velocity block
-    # (every V-cycle level), the FP64 Stokes operator and its cell pass
-    t_cell = g.time_operation(gmg.TIME_A_CELL_PASS, gmg.FP32, 20)
-    eta_words = f.n_cells * (27 if P.projection == 1 else 1)
-    b_cell = 4 * (f.n_u + eta_words + 81 * f.n_cells)  # reads x and eta, writes 81 contributions per cell
+    # on the library's stream, against peaks measured on this GPU: the FP64
+    # Stokes cell pass (the FGMRES matrix-vector product; the largest share of
+    # the solve's launch list) is bound by the FP64 pipe, the FP32 A-block
+    # operator (every V-cycle level) by the FP32 pipe at this arithmetic
+    # intensity (~35 flop per compulsory byte against a ridge near 12)
+    fp = measured_fp_peaks()
+    log("measured FMA peaks (TFLOP/s)", fp)
     peak, peak_kind = peaks()
-    achieved = b_cell / t_cell / 1e9
-    tflops_cell = FLOPS_A_CELL_F32 * f.n_cells / t_cell / 1e12
-    t_s64 = ops["stokes_vmult_fp64"]
-    tflops_s64 = FLOPS_STOKES_CELL_F64 * f.n_cells / t_s64 / 1e12
-    # the dominant kernel of the solve (largest share of the launch list): the FP64
-    # Stokes cell pass of the FGMRES matrix-vector product, timed alone
+    eta_words = f.n_cells * (27 if P.projection == 1 else 1)
     t_sc = g.time_operation(gmg.TIME_STOKES_CELL_PASS, gmg.FP64, 20)
-    b_sc = 8 * (n + eta_words + 89 * f.n_cells)  # reads u, p and eta, writes 81 + 8 contributions per cell
-    tflops_sc = FLOPS_STOKES_CELL_F64 * f.n_cells / t_sc / 1e12
+    t_s64 = ops["stokes_vmult_fp64"]
+    t_a32 = ops["A_vmult_fp32"]
+    flops_sc = ALG_FLOPS_STOKES_CELL * f.n_cells
+    flops_a = ALG_FLOPS_A_CELL * f.n_cells
+    bytes_s64 = 8 * (2 * n + eta_words)      # compulsory: u, p in and out, eta
+    bytes_a32 = 4 * (2 * f.n_u + eta_words)  # compulsory: u in and out, eta
     clocks = clk.summary()
 
     if rank != 0:
@@ -377,33 +406,28 @@ def run_gpu(args):
         "config": {"workload": WORKLOAD, "cells": f.n_cells, "n_u": f.n_u, "n_p": f.n_p, "levels": len(P.levels),
                    "tolerance": TOL, "krylov": "FGMRES(100), FP64", "mg": "FP32 V-cycle, Chebyshev(4)",
                    "l2": "flushed between timed solves (256 MiB write)", "parallelism": f"replicas x{world}"},
-        "e2e": {"value": e2e_value, "unit": "MDoF/s", "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": n * 8},
+        "e2e": {"value": e2e_value, "unit": "MDoF/s", "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": n * 8,
+                "solves": len(e2e_s), "seconds_per_solve": e2e_s},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": "velocity_cell_kernel<double,3,STOKES> (FP64 Stokes cell pass, "
-                                                "32^3 finest level, 3 threads per cell)",
-                     "achieved": b_sc / t_sc / 1e9, "peak": peak, "unit": "GB/s", "frac": b_sc / t_sc / 1e9 / peak,
-                     "peak_kind": peak_kind, "traffic": STOKES_CELL_PASS_F64_DRAM_BYTES,
-                     "algorithmic_bytes_per_launch": b_sc, "seconds_per_launch": t_sc,
-                     "fp64": {"achieved_tflops": tflops_sc, "peak_tflops": FP64_PEAK_TFLOPS,
-                              "frac": tflops_sc / FP64_PEAK_TFLOPS, "peak_kind": "nominal",
-                              "flops_per_cell": FLOPS_STOKES_CELL_F64},
-                     "note": "bound by the FP64 pipe (1/64 of the FP32 rate on GB300), not by HBM: its inputs and "
-                             "outputs are L2-resident within a solve"},
-        "roofline_fp32_a_cell_pass": {
-            "bound": "hbm", "kernel": "lattice_cell_kernel_f32<A> (FP32 velocity-block cell pass of the V-cycle, "
-                                      "32^3 finest level)",
-            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-            "traffic": A_CELL_PASS_F32_DRAM_BYTES, "algorithmic_bytes_per_launch": b_cell,
-            "seconds_per_launch": t_cell,
-            "fp32": {"achieved_tflops": tflops_cell, "peak_tflops": FP32_PEAK_TFLOPS,
-                     "frac": tflops_cell / FP32_PEAK_TFLOPS, "peak_kind": "nominal",
-                     "flops_per_cell": FLOPS_A_CELL_F32},
-            "note": "one thread per cell, 32768 cells: one partial wave, latency-bound"},
-        "roofline_fp64_stokes": {"bound": "fp64", "kernel": "velocity_cell_kernel<double,3,STOKES> + gathers "
-                                                            "(FP64 Stokes operator, 32^3)",
-                                 "seconds_per_application": t_s64, "achieved_tflops": tflops_s64,
-                                 "peak_tflops": FP64_PEAK_TFLOPS, "frac": tflops_s64 / FP64_PEAK_TFLOPS,
-                                 "peak_kind": "nominal", "flops_per_cell": FLOPS_STOKES_CELL_F64},
+        "roofline": {"bound": "fp64", "kernel": "lattice_iso_kernel_f64<STOKES> (FP64 Stokes cell pass, 32^3 "
+                                                 "finest level, 3 threads per cell)",
+                     "achieved": flops_sc / t_sc / 1e12, "peak": fp["fp64"], "unit": "TFLOP/s",
+                     "frac": flops_sc / t_sc / 1e12 / fp["fp64"],
+                     "peak_kind": "measured (FP64 FMA-chain probe, libgb_probe.so, this run)",
+                     "traffic": STOKES_CELL_PASS_F64_DRAM_BYTES, "algorithmic_flops_per_launch": flops_sc,
+                     "flops_per_cell": ALG_FLOPS_STOKES_CELL, "seconds_per_launch": t_sc,
+                     "hbm": {"operator": "FP64 Stokes vmult (cell pass + gathers)", "seconds": t_s64,
+                             "algorithmic_bytes": bytes_s64, "achieved": bytes_s64 / t_s64 / 1e9, "peak": peak,
+                             "unit": "GB/s", "frac": bytes_s64 / t_s64 / 1e9 / peak, "peak_kind": peak_kind}},
+        "roofline_fp32_a_vmult": {
+            "bound": "fp32", "kernel": "FP32 A-block vmult, 32^3 finest level (lattice cell pass + gather)",
+            "achieved": flops_a / t_a32 / 1e12, "peak": fp["fp32"], "unit": "TFLOP/s",
+            "frac": flops_a / t_a32 / 1e12 / fp["fp32"], "peak_kind": "measured (FP32 FMA-chain probe)",
+            "seconds_per_application": t_a32, "flops_per_cell": ALG_FLOPS_A_CELL,
+            "hbm": {"algorithmic_bytes": bytes_a32, "achieved": bytes_a32 / t_a32 / 1e9, "peak": peak,
+                    "unit": "GB/s", "frac": bytes_a32 / t_a32 / 1e9 / peak, "peak_kind": peak_kind},
+            "note": "all operands L2-resident at 32^3; the 64^3 / 128^3 sweep (bench.py --sweep) gives the "
+                    "HBM-resident figures"},
         "cpu_baseline": {"value": cpu["fp64_mg"]["mdofs"], "unit": "MDoF/s", "cores": os.cpu_count(),
                          "kind": "port",
                          "sample": f"one full FP64-MG solve of the same 32^3 workload to 1e-8 "
@@ -414,7 +438,7 @@ def run_gpu(args):
                          "fp32_mg": cpu["fp32_mg"]},
         "clocks": clocks,
         "detail": {
-            "setup_seconds": setup_s, "wall_seconds_timed": wall,
+            "setup_seconds": setup_s, "setup_phases": setup, "wall_seconds_timed": wall,
             "mixed": {"solve_s": t_sum / args.steps, "iterations": its_mixed,
                       "fp64_stokes_applications": mixed["fp64_stokes_applications"],
                       "final_residual": mixed["final_linear_residual"], "tolerance": mixed["solver_tolerance"]},
@@ -459,16 +483,20 @@ def run_profile_op(name: str):
 
 
 def run_sweep(sizes):
-    """Operator timings of the sinker workload at several sizes (no solve): at 32^3
-    every operand is L2-resident, at 64^3 the FP32 A-block vmult's working set
-    (vectors, viscosity, per-cell outputs: ~165 MB) exceeds the 129 MB L2, so
-    its HBM fraction starts to mean something. One JSON line per size."""
+    """Operator timings of the sinker workload at several sizes (no solve). At 32^3
+    every operand is L2-resident; from 64^3 on the FP32 A-block operator's vectors
+    and viscosity exceed the 129 MB L2, so its HBM fraction means something. Bytes
+    are the compulsory ones (vectors in and out, viscosity table); flops the
+    algorithmic sum-factorisation counts. One JSON line per size."""
     import torch
     from aspect_gb300 import gmg, problems
     torch.cuda.init()
     peak, peak_kind = peaks()
+    fp = measured_fp_peaks()
     for nc in sizes:
+        t0 = time.perf_counter()
         P = problems.sinkers_3d(nc)
+        t_problem = time.perf_counter() - t0
         g = gmg.from_problem(P, build=False)
         f = P.fine
         n = P.n_dofs
@@ -479,19 +507,25 @@ def run_sweep(sizes):
                               ("stokes_cell_pass_fp64", "TIME_STOKES_CELL_PASS", "FP64"),
                               ("mass_vmult_fp32", "TIME_MASS_VMULT", "FP32")]}
         b = {"A_vmult_fp32": 4 * (2 * f.n_u + eta_words),
-             "A_cell_pass_fp32": 4 * (f.n_u + eta_words + 81 * f.n_cells),
+             "A_cell_pass_fp32": 4 * (f.n_u + eta_words),
              "stokes_vmult_fp64": 8 * (2 * n + eta_words),
-             "stokes_cell_pass_fp64": 8 * (n + eta_words + 89 * f.n_cells),
+             "stokes_cell_pass_fp64": 8 * (n + eta_words),
              "mass_vmult_fp32": 4 * (2 * f.n_p + eta_words)}
+        fl = {"A_vmult_fp32": ("fp32", ALG_FLOPS_A_CELL), "A_cell_pass_fp32": ("fp32", ALG_FLOPS_A_CELL),
+              "stokes_vmult_fp64": ("fp64", ALG_FLOPS_STOKES_CELL),
+              "stokes_cell_pass_fp64": ("fp64", ALG_FLOPS_STOKES_CELL)}
         line = {"sweep": f"sinkers_{nc}^3", "cells": f.n_cells, "n_u": f.n_u, "n_p": f.n_p, "peak_gbs": peak,
-                "peak_kind": peak_kind, "ops": {}}
+                "peak_kind": peak_kind, "peak_tflops": fp, "host_problem_seconds": t_problem,
+                "fused_a_block": nc % 16 == 0 and f.n_cells >= 65536, "ops": {}}
         for k in t:
             gbs = b[k] / t[k] / 1e9
-            line["ops"][k] = {"seconds": t[k], "algorithmic_bytes": b[k], "gbs": gbs, "hbm_frac": gbs / peak,
-                              "gdofs": (f.n_u if k.startswith("A") else (f.n_p if k.startswith("mass") else n))
-                              / t[k] / 1e9}
-        line["ops"]["stokes_cell_pass_fp64"]["fp64_tflops"] = FLOPS_STOKES_CELL_F64 * f.n_cells / t["stokes_cell_pass_fp64"] / 1e12
-        line["ops"]["A_cell_pass_fp32"]["fp32_tflops"] = FLOPS_A_CELL_F32 * f.n_cells / t["A_cell_pass_fp32"] / 1e12
+            row = {"seconds": t[k], "algorithmic_bytes": b[k], "gbs": gbs, "hbm_frac": gbs / peak,
+                   "gdofs": (f.n_u if k.startswith("A") else (f.n_p if k.startswith("mass") else n)) / t[k] / 1e9}
+            if k in fl:
+                kind, per_cell = fl[k]
+                tf = per_cell * f.n_cells / t[k] / 1e12
+                row.update({f"{kind}_tflops": tf, f"{kind}_frac": tf / fp[kind]})
+            line["ops"][k] = row
         print(json.dumps(line), flush=True)
         del g
 

@@ -57,8 +57,14 @@ enum gb_gmg_status {
 };
 
 enum gb_gmg_geometry {
-  GB_GMG_GEOM_BOX = 0, /* per cell: lower corner x0[dim], edge lengths h[dim] */
-  GB_GMG_GEOM_Q2 = 1   /* per cell: 3^dim Q2 mapping support points [node][dim] */
+  GB_GMG_GEOM_BOX = 0,  /* per cell: lower corner x0[dim], edge lengths h[dim]    */
+  GB_GMG_GEOM_Q2 = 1,   /* per cell: 3^dim Q2 mapping support points [node][dim]  */
+  GB_GMG_GEOM_TABLE = 2 /* per cell and QGauss(3) point (lexicographic): the
+                           inverse Jacobian [d*dim+e] = d xi_d / d x_e, then
+                           |det J|; dim*dim+1 values per point. The caller's own
+                           mapping, e.g. ASPECT's MappingQCache of degree 4 on
+                           curved geometries (source/simulator/core.cc:106-119),
+                           evaluated at the quadrature points                   */
 };
 
 enum gb_gmg_operator {
@@ -80,9 +86,17 @@ enum gb_gmg_krylov {
 
 enum gb_gmg_projection {
   GB_GMG_VISC_DGQ0 = 0, /* one (averaged) value per cell; levels: cell means     */
-  GB_GMG_VISC_DGQ1 = 1  /* values per quadrature point, projected to Q1 per cell
+  GB_GMG_VISC_DGQ1 = 1, /* values per quadrature point, projected to Q1 per cell
                            (project_to_Q1 averaging); levels: Q1 interpolation,
                            clamped to the active-level range                    */
+  GB_GMG_VISC_NONE = 2  /* "Material averaging = none": values per quadrature
+                           point for the outer operators (FGMRES product, the
+                           expensive inner solves, rhs correction, adjoint);
+                           every multigrid level, the finest included, takes the
+                           cellwise (DGQ0) projection, as the reference fills its
+                           level tables (stokes_matrix_free_local_smoothing.cc:
+                           211-294, matrix_free_operators.cc:137-330). gb_gmg_vmult
+                           applies the multigrid tables.                        */
 };
 
 /* Mirrors "Solver parameters/Stokes solver parameters" and "Matrix Free"
@@ -98,6 +112,9 @@ typedef struct gb_gmg_options {
   int schur_smoothing_steps;    /* SmootherRelaxation steps for the Schur block (4)  */
   int force_indexed_layout;     /* 1: never use the lattice fast path (testing)      */
   int coarse_solver;            /* gb_gmg_coarse_solver (Chebyshev as the reference)  */
+  int fused_a_min_cells;        /* FP32 A-block applications of 3D lattice levels with at
+                                   least this many cells (and 16 x 8 | cells in x, y) run
+                                   as one fused cell-and-gather pass (65536; 0: never)  */
 } gb_gmg_options;
 
 enum gb_gmg_coarse_solver {

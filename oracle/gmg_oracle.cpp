@@ -203,6 +203,12 @@ static void compute_geometry(Level& L, const FE& fe) {
   L.JxW.assign((size_t)L.n_cells * nq, 0.0);
   for (int c = 0; c < L.n_cells; ++c) {
     for (int q = 0; q < nq; ++q) {
+      if (L.geom_kind == 2) {  // caller's table: inverse Jacobian, then |det J|
+        const double* t = &L.geom[((size_t)c * nq + q) * (d * d + 1)];
+        for (int a = 0; a < d * d; ++a) L.invJ[((size_t)c * nq + q) * d * d + a] = t[a];
+        L.JxW[(size_t)c * nq + q] = t[d * d] * fe.qw[q];
+        continue;
+      }
       double J[3][3] = {{0}};
       if (L.geom_kind == 0) {
         for (int e = 0; e < d; ++e) J[e][e] = L.geom[(size_t)c * 2 * d + d + e];
@@ -1528,7 +1534,9 @@ int orc_set_level_mesh(void* p, int lev, int n_cells, const int* cdu, const int*
     L.cdu.assign(cdu, cdu + (size_t)n_cells * h->fe.nu);
     L.cdp.assign(cdp, cdp + (size_t)n_cells * h->fe.np);
     L.geom_kind = geom_kind;
-    size_t ng = geom_kind == 0 ? (size_t)n_cells * 2 * h->dim : (size_t)n_cells * h->fe.nv * h->dim;
+    size_t ng = geom_kind == 0   ? (size_t)n_cells * 2 * h->dim
+                : geom_kind == 1 ? (size_t)n_cells * h->fe.nv * h->dim
+                                 : (size_t)n_cells * h->fe.nq * (h->dim * h->dim + 1);
     L.geom.assign(geom, geom + ng);
     L.cu.init(n_u); L.cp.init(n_p);
     orc::compute_geometry(L, h->fe);

@@ -9,6 +9,14 @@ def rel_err(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
+def p_err(a, b):
+    """Relative difference of two pressure vectors with their means removed: with
+    free slip (or no slip) on the whole boundary the pressure is determined only
+    up to a constant, which the caller fixes afterwards by normalisation."""
+    a, b = np.asarray(a), np.asarray(b)
+    return rel_err(a - a.mean(), b - b.mean())
+
+
 def hierarchy(dim, n, geometry="box", permute=False, seed=0):
     levels = mesh.box_hierarchy(dim, n)
     if geometry == "q2":

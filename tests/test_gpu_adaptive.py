@@ -7,7 +7,7 @@ import pytest
 
 from aspect_gb300 import gmg, octree, problems
 from oracle import Oracle
-from tests.gpu_util import rel_err
+from tests.gpu_util import p_err, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -82,8 +82,9 @@ def test_adaptive_sphere_solve(base, nad):
     for x, out in ((x64, o64), (x32, o32)):
         assert np.linalg.norm(P.rhs - o.vmult(0, top, x)) <= 1.01 * out["solver_tolerance"]
     f = P.fine
-    assert rel_err(x32[: f.n_u], x64[: f.n_u]) < 1e-6
+    # both meet the same FP64 residual; they agree to the problem's conditioning
+    assert rel_err(x32[: f.n_u], x64[: f.n_u]) < 1e-5
     o.build_preconditioner(False)
     xr, info = o.solve(P.rhs, tol_rel=1e-8)
     assert abs(info["cheap_iterations"] - o64["cheap_iterations"]) <= 1
-    assert rel_err(x64[: f.n_u], xr[: f.n_u]) < 1e-8 and rel_err(x64[f.n_u:], xr[f.n_u:]) < 1e-8
+    assert rel_err(x64[: f.n_u], xr[: f.n_u]) < 1e-8 and p_err(x64[f.n_u:], xr[f.n_u:]) < 1e-8

@@ -164,3 +164,90 @@ def test_fp32_a_block_on_large_lattice_level(per_q, comp):
         y_ref = o.vmult(1, top, x)
         assert rel_err(g.vmult(1, top, x, gmg.FP32), y_ref) < TOL32 * 10
         assert rel_err(g.vmult(1, top, x, gmg.FP64), y_ref) < TOL64
+
+
+@pytest.mark.parametrize("n,per_q", [(16, True), (32, True), (32, False)])
+def test_fused_ablock_operator(n, per_q):
+    """The fused FP32 A-block operator of large lattice levels (one cell-and-gather
+    pass per tile of 16 x 8 cells and a face pass) against the two-pass operator
+    and the oracle, on every level where it applies; its Chebyshev and residual
+    epilogues through a V-cycle and a mixed solve; bit-reproducibility."""
+    levels = mesh.box_hierarchy(3, n)
+    f = levels[-1]
+    eta = random_eta(f, per_q, seed=n)
+    fused = gmg.StokesMatrixFreeGPU(3, len(levels), {"fused_a_min_cells": 1})
+    plain = gmg.StokesMatrixFreeGPU(3, len(levels), {"fused_a_min_cells": 0})
+    for g in (fused, plain):
+        g.setup_dofs(levels)
+        g.assemble(eta, 0, 1.0)
+        g.build_preconditioner()
+    o = Oracle(levels)
+    o.set_viscosity(eta, 0, 1.0)
+    rng = np.random.default_rng(n)
+    for lev, m in enumerate(levels):
+        x = rng.normal(size=m.n_u)
+        yf = fused.vmult(gmg.OP_A, lev, x, gmg.FP32)
+        assert rel_err(yf, o.vmult(1, lev, x)) < TOL32 * 10, lev
+        assert rel_err(yf, plain.vmult(gmg.OP_A, lev, x, gmg.FP32)) < TOL32, lev
+        assert np.array_equal(yf, fused.vmult(gmg.OP_A, lev, x, gmg.FP32))
+    r = rng.normal(size=f.n_u)
+    assert rel_err(fused.vcycle(0, r, gmg.FP32), plain.vcycle(0, r, gmg.FP32)) < 1e-5
+    rhs = np.concatenate([rng.normal(size=f.n_u), np.zeros(f.n_p)])  # consistent: no pressure load
+    rhs[f.constraints_u.rows] = 0.0
+    xf, of = fused.solve(rhs, linear_solver_tolerance=1e-8, mg_precision=gmg.FP32)
+    xp, op = plain.solve(rhs, linear_solver_tolerance=1e-8, mg_precision=gmg.FP32)
+    assert of["status"] == 0 and abs(of["cheap_iterations"] - op["cheap_iterations"]) <= 1
+    assert np.linalg.norm(rhs - o.vmult(0, len(levels) - 1, xf)) <= 1.01 * of["solver_tolerance"]
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_caller_geometry_table(dim):
+    """GB_GMG_GEOM_TABLE: the caller's inverse Jacobians and |det J| at the
+    quadrature points. (a) Built from the level's own Q2 mapping it gives the
+    GB_GMG_GEOM_Q2 operators to rounding. (b) From a mapping the Q2 support
+    points cannot represent -- the exact Jacobian of a smoothly distorted box,
+    x -> x + d(x) on top of the cell's affine map -- the GPU operators agree with
+    the oracle given the same table."""
+    n = 8 if dim == 2 else 4
+    base = mesh.box_hierarchy(dim, n)
+    dist = mesh.smooth_distortion(0.05)
+    q2 = [mesh.to_q2_geometry(l, dist) for l in base]
+    tab = [mesh.to_table_geometry(l) for l in q2]
+    eta = random_eta(base[-1], True)
+    rng = np.random.default_rng(11)
+
+    def solver(levels):
+        g = gmg.StokesMatrixFreeGPU(dim, len(levels))
+        g.setup_dofs(levels)
+        g.assemble(eta, 0, 1.3, 1)
+        return g
+
+    ga, gb = solver(q2), solver(tab)
+    for lev, m in enumerate(q2):
+        x = rng.normal(size=m.n_u + m.n_p)
+        for op in range(4):
+            src = x if op == 0 else (x[: m.n_u] if op == 1 else x[m.n_u:])
+            assert rel_err(gb.vmult(op, lev, src), ga.vmult(op, lev, src)) < 1e-12, (lev, op)
+    # exact Jacobian of X(xi) = B(xi) + d(B(xi)), B the cell's affine box map
+    from aspect_gb300 import fe
+    gp = fe.tensor_points(dim, fe.gauss(3)[0])
+    exact = []
+    for m in base:
+        xb = m.map_points(gp)
+        JB = m.jacobians(gp)
+        eps = 1e-6
+        grad_d = np.zeros(xb.shape + (dim,))
+        for e in range(dim):
+            dx = np.zeros(dim)
+            dx[e] = eps
+            grad_d[..., e] = (dist((xb + dx).reshape(-1, dim)) - dist((xb - dx).reshape(-1, dim))).reshape(
+                xb.shape) / (2 * eps)
+        exact.append(mesh.to_table_geometry(m, np.einsum("cqij,cqjk->cqik", np.eye(dim) + grad_d, JB)))
+    g = solver(exact)
+    o = Oracle(exact)
+    o.set_viscosity(eta, 0, 1.3, 1)
+    for lev, m in enumerate(exact):
+        x = rng.normal(size=m.n_u + m.n_p)
+        for op in range(4):
+            src = x if op == 0 else (x[: m.n_u] if op == 1 else x[m.n_u:])
+            assert rel_err(g.vmult(op, lev, src), o.vmult(op, lev, src)) < TOL64, (lev, op)

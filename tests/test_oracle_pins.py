@@ -187,9 +187,11 @@ def test_nsinker_without_averaging_follows_reference_semantics():
     needs 172 iterations (174 Schur applications). The oracle with that
     arrangement (mg_finest_projected) lands within two iterations of it (a slow
     solve with two restarts amplifies last-digit differences of the projection).
-    The GPU library instead uses the per-point table on its finest level, the
-    operator itself, which needs far fewer iterations for the same 1e-6
-    residual."""
+    With the per-point table on the finest multigrid level as well (the
+    library's GB_GMG_VISC_DGQ0 with per-point values) the V-cycle's finest level
+    is the operator itself, and far fewer iterations reach the same 1e-6
+    residual; the library's GB_GMG_VISC_NONE gives the reference's arrangement
+    (GPU test in test_gpu_solve_parity.py)."""
     G = json.load(open(os.path.join(GOLDEN, "nsinker_golden.json")))
     ref = G["no_avg"]
     P = problems.nsinker(2, G["centres"], G["dynamic_viscosity_ratio"], G["sinker_density"], G["delta"],
@@ -206,3 +208,22 @@ def test_nsinker_without_averaging_follows_reference_semantics():
         its[flag] = info["cheap_iterations"]
     assert abs(its[True] - ref["cheap_iterations"]) <= 2, its
     assert its[False] < ref["cheap_iterations"] // 2, its
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_oracle_geometry_table_matches_q2_mapping(dim):
+    """GEOM_TABLE (the caller's inverse Jacobians and |det J| per Gauss point)
+    built from a level's Q2 mapping gives the same operators as GEOM_Q2."""
+    base = mesh.box_hierarchy(dim, 4)
+    q2 = [mesh.to_q2_geometry(l, mesh.smooth_distortion(0.05)) for l in base]
+    tab = [mesh.to_table_geometry(l) for l in q2]
+    eta = np.exp(np.random.default_rng(3).uniform(-1, 1, size=(base[-1].n_cells, 3 ** dim)))
+    oa, ob = Oracle(q2), Oracle(tab)
+    oa.set_viscosity(eta, 0, 1.3, 1)
+    ob.set_viscosity(eta, 0, 1.3, 1)
+    top = len(base) - 1
+    m = q2[-1]
+    x = np.random.default_rng(4).normal(size=m.n_u + m.n_p)
+    for op, src in ((0, x), (1, x[: m.n_u]), (2, x[m.n_u:]), (3, x[m.n_u:])):
+        a, b = oa.vmult(op, top, src), ob.vmult(op, top, src)
+        assert np.linalg.norm(a - b) <= 1e-13 * np.linalg.norm(a), op
