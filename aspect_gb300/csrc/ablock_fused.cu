@@ -84,12 +84,9 @@ __global__ void __launch_bounds__(kFT, 2) ablock_fused_f32(LevelView<float> L, G
     __syncthreads();
     const float* cin = carry + cur * 3 * kPlane;
     float* cout = carry + (cur ^ 1) * 3 * kPlane;
-    for (int e = t; e < 9 * kPlane; e += kFT) {
-      const int nz = e / (3 * kPlane);
-      const int r = e - nz * 3 * kPlane;
-      const int comp = r / kPlane;
-      const int p = r - comp * kPlane;
-      const int lx = p % kBX, ly = p / kBX;
+    // one item per node column (lx, ly) of the tile: its 3 planes x 3 components
+    for (int p = t; p < kPlane; p += kFT) {
+      const int ly = p / kBX, lx = p - ly * kBX;
       // cells of the layer around (lx, ly), per direction the lower one (candidate
       // 0) first: an odd node lies inside one cell, an even one between two
       const bool ox = lx & 1, oy = ly & 1;
@@ -97,24 +94,36 @@ __global__ void __launch_bounds__(kFT, 2) ablock_fused_f32(LevelView<float> L, G
       const int cy0 = oy ? ly >> 1 : (ly >> 1) - 1, py0 = oy ? 1 : 2;
       const bool vx0 = ox || lx > 0, vx1 = !ox && lx < kBX - 1;
       const bool vy0 = oy || ly > 0, vy1 = !oy && ly < kBY - 1;
-      const float* Cc = C + (comp * 27 + 9 * nz) * kFT;
-      float v = nz == 0 ? cin[comp * kPlane + p] : 0.0f;
-      if (vy0 && vx0) v += Cc[(px0 + 3 * py0) * kFT + cy0 * kTX + cx0];
-      if (vy0 && vx1) v += Cc[(0 + 3 * py0) * kFT + cy0 * kTX + (lx >> 1)];
-      if (vy1 && vx0) v += Cc[(px0 + 0) * kFT + (ly >> 1) * kTX + cx0];
-      if (vy1 && vx1) v += Cc[0 * kFT + (ly >> 1) * kTX + (lx >> 1)];
-      if (nz == 2 && kl < tz - 1) {  // kept for the next layer
-        cout[comp * kPlane + p] = v;
-        continue;
+      // shared-memory offsets of the (up to) four contributions, slot 0 of each
+      const int o00 = (px0 + 3 * py0) * kFT + cy0 * kTX + cx0;
+      const int o01 = (3 * py0) * kFT + cy0 * kTX + (lx >> 1);
+      const int o10 = px0 * kFT + (ly >> 1) * kTX + cx0;
+      const int o11 = (ly >> 1) * kTX + (lx >> 1);
+      const bool xy_face = lx == 0 || lx == kBX - 1 || ly == 0 || ly == kBY - 1;
+      const long node0 = ((long)(2 * k) * L.Nn[1] + 2 * ty * kTY + ly) * L.Nn[0] + 2 * tx * kTX + lx;
+      const long plane = (long)L.Nn[0] * L.Nn[1];
+#pragma unroll
+      for (int nz = 0; nz < 3; ++nz) {
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+          const float* Cc = C + (comp * 27 + 9 * nz) * kFT;
+          float v = nz == 0 ? cin[comp * kPlane + p] : 0.0f;
+          if (vy0 && vx0) v += Cc[o00];
+          if (vy0 && vx1) v += Cc[o01];
+          if (vy1 && vx0) v += Cc[o10];
+          if (vy1 && vx1) v += Cc[o11];
+          if (nz == 2 && kl < tz - 1) {  // kept for the next layer
+            cout[comp * kPlane + p] = v;
+            continue;
+          }
+          const int lz = 2 * kl + nz;
+          if (xy_face || lz == 0 || lz == 2 * tz) {
+            Ft[(size_t)comp * nb + face_index(lx, ly, lz, tz)] = v;
+            continue;
+          }
+          gather_epilogue<float, epi>(a, (long)comp * L.n_nodes + node0 + nz * plane, v, false);
+        }
       }
-      const int lz = 2 * kl + nz;
-      const bool face = lx == 0 || lx == kBX - 1 || ly == 0 || ly == kBY - 1 || lz == 0 || lz == 2 * tz;
-      if (face) {
-        Ft[(size_t)comp * nb + face_index(lx, ly, lz, tz)] = v;
-        continue;
-      }
-      const long node = ((long)(2 * k + nz) * L.Nn[1] + 2 * ty * kTY + ly) * L.Nn[0] + 2 * tx * kTX + lx;
-      gather_epilogue<float, epi>(a, (long)comp * L.n_nodes + node, v, false);
     }
     cur ^= 1;
     __syncthreads();

@@ -44,6 +44,30 @@ struct Handle {
   double s = 1.0;
   int compressible = 0, projection = 0;
   int visc_n_per_cell = 0;  // n_per_cell of the last successful set_viscosity
+  // Newton / prescribed-dilation terms of the outer Stokes operator (finest level,
+  // internal cell order): flags and tables in both precisions
+  struct Newton {
+    int newton = 0, symmetrize = 0, average = 0, dilation = 0;
+    DevBuf<double> t64[6];
+    DevBuf<float> t32[6];
+    bool on() const { return newton || dilation; }
+    template <typename T>
+    NewtonView<T> view() const {
+      const auto& t = pick(t64, t32, T());
+      return NewtonView<T>{newton, symmetrize, average, dilation, t[0].p, t[1].p, t[2].p, t[3].p, t[4].p, t[5].p};
+    }
+    static const DevBuf<double> (&pick(const DevBuf<double> (&a)[6], const DevBuf<float> (&)[6], double))[6] {
+      return a;
+    }
+    static const DevBuf<float> (&pick(const DevBuf<double> (&)[6], const DevBuf<float> (&b)[6], float))[6] {
+      return b;
+    }
+    void clear() {
+      newton = symmetrize = average = dilation = 0;
+      for (auto& b : t64) b.release();
+      for (auto& b : t32) b.release();
+    }
+  } newton_terms;
   int n_sm = 1;             // streaming multiprocessors of the handle's GPU
   double eta_min = 0, eta_max = 0;
   bool setup_done = false, visc_done = false;
@@ -183,8 +207,24 @@ void apply_op(Handle& H, int lev, int op, const T* su, const T* sp, T* du, T* dp
   Level& L = H.levels[lev];
   LevelDev<T>& D = L.dev<T>();
   const bool own_table = outer && L.eta_active_n > 0;
-  const LevelView<T> v = own_table ? L.view_outer<T>(H.s, H.compressible) : L.view<T>(H.s, H.compressible);
-  if (op == OPK_A && !own_table) {
+  LevelView<T> v = own_table ? L.view_outer<T>(H.s, H.compressible) : L.view<T>(H.s, H.compressible);
+  const bool newton = outer && lev == H.n_levels - 1 && H.newton_terms.on();
+  // a prescribed dilation makes the outer viscous terms deviatoric (not the levels')
+  if (newton && H.newton_terms.dilation) v.compressible = 1;
+  if (newton && op == OPK_STOKES) {
+    launch_newton_stokes<T>(v, H.newton_terms.view<T>(), su, sp, D.Eu.p, D.Ep.p, cell_pass_slot_major<T>(v, op),
+                            H.st);
+    ++H.cell_launches;
+    for (int block = 0; block < 2; ++block) {
+      GatherArgs<T> a{};
+      a.E = block == 0 ? D.Eu.p : D.Ep.p;
+      a.x = const_cast<T*>(block == 0 ? su : sp);
+      a.y = block == 0 ? du : dp;
+      gather<T>(H, L, v, block, EPI_STORE, a, op);
+    }
+    return;
+  }
+  if (op == OPK_A && !own_table && !newton) {
     GatherArgs<T> a{};
     a.x = const_cast<T*>(su);
     a.y = du;
@@ -1263,17 +1303,26 @@ void solve_internal(Handle& H, const gb_gmg_solve_params* P, gb_gmg_outputs* out
   GB_CUDA(cudaEventRecord(e0, H.st));
   // initial residual and tolerance (:977-1041)
   double* t = H.tv.p;
-  stokes64(H, x, t);
-  v_copy<double>(n, b, H.rv.p, H.st);
-  v_axpby<double>(n, -1.0, t, 1.0, H.rv.p, H.st);
-  out->initial_nonlinear_residual = std::sqrt(dot_host(H, n, H.rv.p, H.rv.p));
-  v_copy<double>(n, x, H.wv.p, H.st);
-  GB_CUDA(cudaMemsetAsync(H.wv.p, 0, nu * sizeof(double), H.st));
-  stokes64(H, H.wv.p, t);
-  v_copy<double>(nu, b, H.rv.p, H.st);
-  v_axpby<double>(nu, -1.0, t, 1.0, H.rv.p, H.st);
-  const double ru = std::sqrt(dot_host(H, nu, H.rv.p, H.rv.p));
-  const double rp = std::sqrt(dot_host(H, n - nu, b + nu, b + nu));
+  double ru, rp;
+  if (P->solve_newton_system) {
+    // a Newton update: zero initial guess, residual and tolerance from |rhs| (:959-970, :1026-1040)
+    GB_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), H.st));
+    ru = std::sqrt(dot_host(H, nu, b, b));
+    rp = std::sqrt(dot_host(H, n - nu, b + nu, b + nu));
+    out->initial_nonlinear_residual = std::sqrt(ru * ru + rp * rp);
+  } else {
+    stokes64(H, x, t);
+    v_copy<double>(n, b, H.rv.p, H.st);
+    v_axpby<double>(n, -1.0, t, 1.0, H.rv.p, H.st);
+    out->initial_nonlinear_residual = std::sqrt(dot_host(H, n, H.rv.p, H.rv.p));
+    v_copy<double>(n, x, H.wv.p, H.st);
+    GB_CUDA(cudaMemsetAsync(H.wv.p, 0, nu * sizeof(double), H.st));
+    stokes64(H, H.wv.p, t);
+    v_copy<double>(nu, b, H.rv.p, H.st);
+    v_axpby<double>(nu, -1.0, t, 1.0, H.rv.p, H.st);
+    ru = std::sqrt(dot_host(H, nu, H.rv.p, H.rv.p));
+    rp = std::sqrt(dot_host(H, n - nu, b + nu, b + nu));
+  }
   const double tol = P->absolute_tolerance > 0 ? P->absolute_tolerance
                                                : P->linear_solver_tolerance * std::sqrt(ru * ru + rp * rp);
   out->solver_tolerance = tol;
@@ -1387,6 +1436,7 @@ void gb_gmg_default_solve_params(gb_gmg_solve_params* p) {
   p->mg_precision = GB_GMG_FP64;
   p->krylov = GB_GMG_GMRES;
   p->idr_s = 2;
+  p->solve_newton_system = 0;
   p->ir_inner_tolerance = 1e-3;
 }
 
@@ -1523,6 +1573,7 @@ int gb_gmg_finalize_setup(gb_gmg* g) {
       L.cdu_raw_d.release();
       L.cdp_raw_d.release();
     }
+    H.newton_terms.clear();
     H.setup_done = true;
     H.visc_done = false;
     H.prec_done[0] = H.prec_done[1] = false;
@@ -1582,6 +1633,52 @@ int gb_gmg_update_viscosity(gb_gmg* g, const double* eta, int n_per_cell) {
     for (auto& L : H.levels) gb::upload_viscosity(L, H.s);
     H.eta_min = mn;
     H.eta_max = mx;
+  })
+}
+
+int gb_gmg_set_newton_terms(gb_gmg* g, const gb_gmg_newton_terms* t) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(H.setup_done, GB_GMG_NOT_READY, "finalize_setup has not been called");
+    auto& N = H.newton_terms;
+    if (!t || !(t->enable_newton_derivatives || t->enable_prescribed_dilation)) {
+      N.clear();
+      return GB_GMG_OK;
+    }
+    const bool newton = t->enable_newton_derivatives != 0, dil = t->enable_prescribed_dilation != 0;
+    GB_CHECK(!newton || (t->strain_rate && t->newton_factor_wrt_strain_rate && t->newton_factor_wrt_pressure), 1,
+             "Newton derivatives need the strain-rate and both Newton-factor tables");
+    GB_CHECK(!dil || t->dilation_lhs, 1, "a prescribed dilation needs its lhs table");
+    GB_CHECK(!(newton && dil) || (t->dilation_derivative_wrt_strain_rate && t->dilation_derivative_wrt_pressure), 1,
+             "Newton derivatives with a prescribed dilation need both dilation-derivative tables");
+    gb::Level& F = H.top();
+    const int nq = H.dim == 3 ? 27 : 9, ns = H.dim == 3 ? 6 : 3;
+    const double* src[6] = {t->strain_rate, t->newton_factor_wrt_strain_rate, t->newton_factor_wrt_pressure,
+                            t->dilation_lhs, t->dilation_derivative_wrt_strain_rate,
+                            t->dilation_derivative_wrt_pressure};
+    const int width[6] = {ns, ns, 1, 1, ns, 1};
+    const bool used[6] = {newton, newton, newton, dil, newton && dil, newton && dil};
+    N.clear();
+    for (int k = 0; k < 6; ++k) {
+      if (!used[k]) continue;
+      const size_t per_cell = (size_t)nq * width[k];
+      std::vector<double> h((size_t)F.n_cells * per_cell);
+      for (long c = 0; c < F.n_cells; ++c) {
+        const long ic = F.internal_of_cell[c];
+        for (size_t i = 0; i < per_cell; ++i) {
+          const double v = src[k][(size_t)c * per_cell + i];
+          GB_CHECK(std::isfinite(v), GB_GMG_NAN_DETECTED, "non-finite value in a Newton / dilation table");
+          h[(size_t)ic * per_cell + i] = v;
+        }
+      }
+      N.t64[k].upload(h);
+      N.t32[k].upload(std::vector<float>(h.begin(), h.end()));
+    }
+    N.newton = newton;
+    N.symmetrize = t->symmetrize_newton_system != 0;
+    N.average = t->average_newton_factors != 0;
+    N.dilation = dil;
   })
 }
 
@@ -1679,17 +1776,20 @@ int gb_gmg_vmult(gb_gmg* g, int op, int level, int precision, const double* src,
     else gb::v_permute_scatter<double, double>(L.n_p, L.perm_p_d.p, a, b, H.st);
     const double* su = in_u ? b : nullptr;
     const double* sp = in_p ? (in_u ? b + L.n_u : b) : nullptr;
+    // the Stokes operator of the finest level is the outer one (per-point table
+    // without averaging, Newton / dilation terms); all others the multigrid's
+    const bool outer = op == gb::OPK_STOKES && level == H.n_levels - 1;
     if (precision == GB_GMG_FP64) {
       double* du = out_u ? a : nullptr;
       double* dp = out_p ? (out_u ? a + L.n_u : a) : nullptr;
-      gb::apply_op<double>(H, level, op, su, sp, du, dp);
+      gb::apply_op<double>(H, level, op, su, sp, du, dp, outer);
     } else {
       gb::v_cast<double, float>(nin, b, H.f32_a.p, H.st);
       const float* fu = in_u ? H.f32_a.p : nullptr;
       const float* fp = in_p ? (in_u ? H.f32_a.p + L.n_u : H.f32_a.p) : nullptr;
       float* du = out_u ? H.f32_b.p : nullptr;
       float* dp = out_p ? (out_u ? H.f32_b.p + L.n_u : H.f32_b.p) : nullptr;
-      gb::apply_op<float>(H, level, op, fu, fp, du, dp);
+      gb::apply_op<float>(H, level, op, fu, fp, du, dp, outer);
       gb::v_cast<float, double>(nout, H.f32_b.p, a, H.st);
     }
     if (out_u && out_p) gb::to_caller(H, level, a, b, true, true);

@@ -28,6 +28,24 @@ void launch_gather(const LevelView<T>& L, int block, int epi, const GatherCsr<T>
 // one-pass pressure mass operator of a lattice level (Mc: per-cell local matrices)
 template <typename T>
 void launch_mass_lattice(const LevelView<T>& L, const T* Mc, int epi, const GatherArgs<T>& a, cudaStream_t s);
+// Newton-derivative and prescribed-dilation tables of the outer Stokes operator
+// (newton.cu): per internal cell and quadrature point, symmetric tensors in
+// deal.II's unrolled component order.
+template <typename T>
+struct NewtonView {
+  int newton, symmetrize, average, dilation;
+  const T* E;    // strain_rate_table
+  const T* D;    // newton_factor_wrt_strain_rate_table
+  const T* dp;   // newton_factor_wrt_pressure_table
+  const T* lhs;  // dilation_lhs_term_table
+  const T* DD;   // dilation_derivative_wrt_strain_rate_table
+  const T* dpd;  // dilation_derivative_wrt_pressure_table
+};
+// cell pass of the outer Stokes operator with those terms (the level's gathers follow)
+template <typename T>
+void launch_newton_stokes(const LevelView<T>& L, const NewtonView<T>& N, const T* su, const T* sp, T* Eu, T* Ep,
+                          bool slot_major, cudaStream_t s);
+
 // Fused FP32 A-block operator of large 3D lattice levels (ablock_fused.cu):
 // cell layers per tile for a level (0: the level does not qualify), the face
 // buffer it needs (floats), the one-time kernel attribute set-up (call outside

@@ -56,7 +56,17 @@ class SolveParams(ctypes.Structure):
                 ("n_cheap_steps", ctypes.c_int), ("n_expensive_steps", ctypes.c_int),
                 ("restart", ctypes.c_int), ("tol_A", ctypes.c_double), ("tol_S", ctypes.c_double),
                 ("mg_precision", ctypes.c_int), ("krylov", ctypes.c_int),
-                ("ir_inner_tolerance", ctypes.c_double), ("idr_s", ctypes.c_int)]
+                ("ir_inner_tolerance", ctypes.c_double), ("idr_s", ctypes.c_int),
+                ("solve_newton_system", ctypes.c_int)]
+
+
+class NewtonTerms(ctypes.Structure):
+    _fields_ = [("enable_newton_derivatives", ctypes.c_int), ("symmetrize_newton_system", ctypes.c_int),
+                ("average_newton_factors", ctypes.c_int), ("enable_prescribed_dilation", ctypes.c_int),
+                ("strain_rate", ctypes.c_void_p), ("newton_factor_wrt_strain_rate", ctypes.c_void_p),
+                ("newton_factor_wrt_pressure", ctypes.c_void_p), ("dilation_lhs", ctypes.c_void_p),
+                ("dilation_derivative_wrt_strain_rate", ctypes.c_void_p),
+                ("dilation_derivative_wrt_pressure", ctypes.c_void_p)]
 
 
 class Outputs(ctypes.Structure):
@@ -77,7 +87,7 @@ EXPORTS = ["gb_gmg_default_options", "gb_gmg_default_solve_params", "gb_gmg_crea
            "gb_gmg_set_eigenvalues", "gb_gmg_transfer", "gb_gmg_vcycle", "gb_gmg_block_preconditioner",
            "gb_gmg_solve", "gb_gmg_solve_device", "gb_gmg_adjoint_gradient", "gb_gmg_memory_consumption",
            "gb_gmg_kernel_launches", "gb_gmg_time_operation", "gb_gmg_ablock_apply_lattice_noalloc",
-           "gb_gmg_update_viscosity", "gb_gmg_correct_stokes_rhs"]
+           "gb_gmg_update_viscosity", "gb_gmg_correct_stokes_rhs", "gb_gmg_set_newton_terms"]
 
 TIME_STOKES_VMULT, TIME_A_VMULT, TIME_MASS_VMULT = 0, 1, 2
 TIME_STOKES_PRECONDITIONER, TIME_A_PRECONDITIONER, TIME_S_PRECONDITIONER = 3, 4, 5
@@ -114,6 +124,7 @@ def load_library(path: str = LIB_PATH):
     L.gb_gmg_set_viscosity.argtypes = [vp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int]
     L.gb_gmg_build_preconditioner.argtypes = [vp]
     L.gb_gmg_update_viscosity.argtypes = [vp, dp, ctypes.c_int]
+    L.gb_gmg_set_newton_terms.argtypes = [vp, ctypes.POINTER(NewtonTerms)]
     L.gb_gmg_vmult.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp]
     L.gb_gmg_correct_stokes_rhs.argtypes = [vp, dp, dp]
     L.gb_gmg_vmult_device.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, dp]
@@ -224,6 +235,20 @@ class StokesMatrixFreeGPU:
         """New viscosity for the operators; keeps the last-built preconditioner."""
         eta = _d(eta)
         self._chk(self.L.gb_gmg_update_viscosity(self.h, _p(eta), eta.size // self.levels[-1].n_cells))
+
+    def set_newton_terms(self, newton=False, symmetrize=False, average=False, dilation=False, strain_rate=None,
+                         d_eta_d_strain_rate=None, d_eta_d_pressure=None, dilation_lhs=None,
+                         d_dilation_d_strain_rate=None, d_dilation_d_pressure=None):
+        """OperatorCellData's Newton / prescribed-dilation tables of the outer Stokes
+        operator (per finest cell and quadrature point); all flags False clears them."""
+        if not (newton or dilation):
+            self._chk(self.L.gb_gmg_set_newton_terms(self.h, None))
+            return
+        arrs = [None if a is None else _d(a) for a in (strain_rate, d_eta_d_strain_rate, d_eta_d_pressure,
+                                                          dilation_lhs, d_dilation_d_strain_rate, d_dilation_d_pressure)]
+        t = NewtonTerms(int(newton), int(symmetrize), int(average), int(dilation),
+                        *[None if a is None else a.ctypes.data for a in arrs])
+        self._chk(self.L.gb_gmg_set_newton_terms(self.h, ctypes.byref(t)))
 
     def build_preconditioner(self):
         self._chk(self.L.gb_gmg_build_preconditioner(self.h))

@@ -135,6 +135,11 @@ typedef struct gb_gmg_solve_params {
   int krylov;                      /* gb_gmg_krylov                                   */
   double ir_inner_tolerance;       /* GMRES_IR: relative tolerance of each inner solve */
   int idr_s;                       /* IDR(s) parameter (2), source/simulator/parameters.cc:483 */
+  int solve_newton_system;         /* StokesSolver::Interface::solve's solve_newton_system
+                                      (interface.h:90-94): the solution is a Newton update,
+                                      so the solve starts from zero and the tolerance and
+                                      initial_nonlinear_residual use |rhs| alone
+                                      (stokes_matrix_free_local_smoothing.cc:952-1041)   */
 } gb_gmg_solve_params;
 
 /* StokesSolver::SolverOutputs plus the counters the reference prints. */
@@ -199,6 +204,34 @@ int gb_gmg_set_viscosity(gb_gmg* h, const double* eta, int n_per_cell, int proje
  * e.g. finite-difference checks or nonlinear iterations that reuse a
  * preconditioner; ASPECT itself rebuilds after every assemble(). */
 int gb_gmg_update_viscosity(gb_gmg* h, const double* eta, int n_per_cell);
+
+/* Newton-derivative and prescribed-dilation terms of the outer Stokes operator
+ * (OperatorCellData, include/aspect/simulator/solver/matrix_free_operators.h:92-208;
+ * applied in StokesOperator::local_apply, matrix_free_operators.cc:400-538; the
+ * tables are filled in stokes_matrix_free_local_smoothing.cc:296-612). Per finest
+ * cell (caller order) and QGauss(3) point (lexicographic); symmetric tensors in
+ * deal.II's unrolled order (00, 11, 22, 01, 02, 12 in 3D; 00, 11, 01 in 2D).
+ * Only the outer Stokes operator (the FGMRES product, gb_gmg_vmult of
+ * GB_GMG_OP_STOKES on the finest level) takes the Newton terms; with a
+ * prescribed dilation the outer viscous terms are deviatoric as with
+ * compressibility; the multigrid levels are unchanged, as in the reference
+ * (:311-313). Arrays a flag does not use may be NULL. */
+typedef struct gb_gmg_newton_terms {
+  int enable_newton_derivatives;
+  int symmetrize_newton_system;
+  int average_newton_factors;
+  int enable_prescribed_dilation;
+  const double* strain_rate;                          /* strain_rate_table                 */
+  const double* newton_factor_wrt_strain_rate;        /* newton_factor_wrt_strain_rate_table */
+  const double* newton_factor_wrt_pressure;           /* newton_factor_wrt_pressure_table  */
+  const double* dilation_lhs;                         /* dilation_lhs_term_table           */
+  const double* dilation_derivative_wrt_strain_rate;  /* dilation_derivative_wrt_strain_rate_table */
+  const double* dilation_derivative_wrt_pressure;     /* dilation_derivative_wrt_pressure_table */
+} gb_gmg_newton_terms;
+
+/* Sets (or with NULL clears) the Newton / dilation terms; call after
+ * gb_gmg_set_viscosity, as assemble() does. */
+int gb_gmg_set_newton_terms(gb_gmg* h, const gb_gmg_newton_terms* terms);
 
 /* build_preconditioner (:1856-1867): level diagonals for both blocks and both
  * precisions, eigenvalue estimates (:834-849) and the captured V-cycles. */

@@ -45,7 +45,7 @@ def lib():
                      "orc_build_preconditioner", "orc_vmult", "orc_get_diagonal", "orc_transfer",
                      "orc_estimate_eigenvalues", "orc_get_eigenvalues", "orc_set_eigenvalues",
                      "orc_vcycle", "orc_block_preconditioner", "orc_solve", "orc_adjoint_gradient",
-                     "orc_set_fast"]:
+                     "orc_set_fast", "orc_set_newton"]:
             getattr(L, name).restype = ctypes.c_int
         _lib = L
     return _lib
@@ -176,6 +176,14 @@ class Oracle:
         out = np.zeros_like(src)
         self._chk(self.L.orc_block_preconditioner(self.h, int(expensive), _ptr(src, _dp), _ptr(out, _dp)))
         return out
+
+    def set_newton_terms(self, newton=False, symmetrize=False, average=False, dilation=False, strain_rate=None,
+                         d_eta_d_strain_rate=None, d_eta_d_pressure=None, dilation_lhs=None,
+                         d_dilation_d_strain_rate=None, d_dilation_d_pressure=None):
+        flags = int(newton) | int(symmetrize) << 1 | int(average) << 2 | int(dilation) << 3
+        arrs = [None if a is None else _d(a) for a in (strain_rate, d_eta_d_strain_rate, d_eta_d_pressure,
+                                                          dilation_lhs, d_dilation_d_strain_rate, d_dilation_d_pressure)]
+        self._chk(self.L.orc_set_newton(self.h, flags, *[None if a is None else _ptr(a, _dp) for a in arrs]))
 
     def adjoint_gradient(self, u, lam) -> np.ndarray:
         u, lam = _d(u), _d(lam)

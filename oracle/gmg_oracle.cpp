@@ -282,12 +282,81 @@ static void colour_cells(Level& L, const FE& fe) {
   for (int c = 0; c < L.n_cells; ++c) L.colour_cells[fill[col[c]]++] = c;
 }
 
+// ---------------------------------------------------------------- Newton / dilation terms
+// Per finest cell and quadrature point, the tables of OperatorCellData
+// (include/aspect/simulator/solver/matrix_free_operators.h:92-208) that the outer
+// Stokes operator reads when Newton derivatives or a prescribed dilation are
+// enabled (matrix_free_operators.cc:400-538). Symmetric tensors are stored as
+// deal.II unrolls them: (00, 11, 22, 01, 02, 12) in 3D, (00, 11, 01) in 2D.
+struct NewtonTerms {
+  bool newton = false, symmetrize = false, average = false, dilation = false;
+  std::vector<double> E;    // strain_rate_table (the linearisation point's strain rate)
+  std::vector<double> D;    // newton_factor_wrt_strain_rate_table
+  std::vector<double> dp;   // newton_factor_wrt_pressure_table
+  std::vector<double> lhs;  // dilation_lhs_term_table
+  std::vector<double> DD;   // dilation_derivative_wrt_strain_rate_table
+  std::vector<double> dpd;  // dilation_derivative_wrt_pressure_table
+};
+static inline int sym_index(int dim, int a, int b) {
+  if (a == b) return a;
+  if (a > b) std::swap(a, b);
+  return dim == 2 ? 2 : (a == 0 ? (b == 1 ? 3 : 4) : 5);
+}
+template <class T>
+static inline void sym_full(const double* t, int dim, T (&M)[3][3]) {
+  for (int a = 0; a < dim; ++a)
+    for (int b = 0; b < dim; ++b) M[a][b] = (T)t[sym_index(dim, a, b)];
+}
+
 // ---------------------------------------------------------------- cell kernel
 // Applies one operator to the cell-local vectors; results are added to yu/yp.
+// nt (outer Stokes operator of the finest level only): Newton / dilation terms.
 template <class T>
 static void cell_apply(const Level& L, const FE& fe, int c, int op, double s, int compressible,
-                       const T* eta_tab, const T* xu, const T* xp, T* yu, T* yp) {
+                       const T* eta_tab, const T* xu, const T* xp, T* yu, T* yp, const NewtonTerms* nt = nullptr) {
   const int d = L.dim, nq = fe.nq, nv = fe.nv, np = fe.np;
+  const int ns = d == 3 ? 6 : 3;
+  // a prescribed dilation makes the outer viscous term deviatoric, as compressibility does
+  const bool deviatoric = compressible || (nt && nt->dilation);
+  if (op != OP_STOKES && op != OP_A) nt = nullptr;
+  const NewtonTerms* ntS = op == OP_STOKES ? nt : nullptr;  // Newton / dilation terms: Stokes only
+  // real-space velocity gradient and pressure at a point
+  auto grad_at = [&](int q, T (&G)[3][3], T& pq) {
+    const double* iJ = &L.invJ[((size_t)c * nq + q) * d * d];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b) G[a][b] = 0;
+    for (int n = 0; n < nv; ++n)
+      for (int e = 0; e < d; ++e) {
+        double t = 0;
+        for (int a = 0; a < d; ++a) t += fe.vgrad[(q * nv + n) * d + a] * iJ[a * d + e];
+        for (int cc = 0; cc < d; ++cc) G[cc][e] += xu[cc * nv + n] * (T)t;
+      }
+    pq = 0;
+    for (int n = 0; n < np; ++n) pq += xp[n] * (T)fe.pval[q * np + n];
+  };
+  // averaged Newton factors: cell sums over the points (matrix_free_operators.cc:411-445)
+  T avg_a = 0, avg_bp = 0, avg_eu = 0, avg_th = 0;
+  if (ntS && ntS->newton && ntS->average) {
+    const NewtonTerms* nt = ntS;
+    for (int q = 0; q < nq; ++q) {
+      T G[3][3], pq;
+      grad_at(q, G, pq);
+      T Dm[3][3], Em[3][3];
+      sym_full(&nt->D[((size_t)c * nq + q) * ns], d, Dm);
+      sym_full(&nt->E[((size_t)c * nq + q) * ns], d, Em);
+      const T jxw = (T)L.JxW[(size_t)c * nq + q];
+      T div = 0, trE = 0;
+      for (int a = 0; a < d; ++a) { div += G[a][a]; trE += Em[a][a]; }
+      for (int a = 0; a < d; ++a)
+        for (int b = 0; b < d; ++b) {
+          const T eps = (T)0.5 * (G[a][b] + G[b][a]);
+          avg_a += Dm[a][b] * eps;
+          if (nt->symmetrize) avg_eu += Em[a][b] * eps * jxw;
+        }
+      avg_bp += (T)nt->dp[(size_t)c * nq + q] * pq;
+      if (nt->symmetrize && (compressible || nt->dilation)) avg_th += trE * div * jxw;
+    }
+  }
   for (int q = 0; q < nq; ++q) {
     const double* iJ = &L.invJ[((size_t)c * nq + q) * d * d];
     const T jxw = (T)L.JxW[(size_t)c * nq + q];
@@ -324,11 +393,58 @@ static void cell_apply(const Level& L, const FE& fe, int c, int op, double s, in
       const T eta2 = (T)2 * eta;
       for (int a = 0; a < d; ++a)
         for (int b = 0; b < d; ++b) F[a][b] = eta2 * (T)0.5 * (G[a][b] + G[b][a]);
-      if (compressible)
+      if (deviatoric)
         for (int a = 0; a < d; ++a) F[a][a] -= eta2 / (T)3 * div;
     }
     if (op == OP_STOKES || op == OP_BT)
       for (int a = 0; a < d; ++a) F[a][a] -= (T)s * pq;
+    T ptest = -(T)s * div;  // terms tested by the pressure basis
+    if (ntS) {
+      const NewtonTerms* nt = ntS;
+      const size_t cq = (size_t)c * nq + q;
+      if (nt->dilation) ptest -= (T)(s * s) * (T)nt->lhs[cq] * pq;
+      if (nt->newton) {
+        T Dm[3][3], Em[3][3];
+        sym_full(&nt->D[cq * ns], d, Dm);
+        sym_full(&nt->E[cq * ns], d, Em);
+        T de = 0, ee = 0, trE = 0;
+        for (int a = 0; a < d; ++a) {
+          trE += Em[a][a];
+          for (int b = 0; b < d; ++b) {
+            const T eps = (T)0.5 * (G[a][b] + G[b][a]);
+            de += Dm[a][b] * eps;
+            ee += Em[a][b] * eps;
+          }
+        }
+        T a_ = nt->average ? avg_a : de;                          // deta_deps : sym_grad_u
+        const T bp = nt->average ? avg_bp : (T)nt->dp[cq] * pq;   // deta_dp p
+        if (nt->symmetrize && nt->average) ee = avg_eu / jxw;    // eps : sym_grad_u
+        for (int x = 0; x < d; ++x)
+          for (int y = 0; y < d; ++y) {
+            if (nt->symmetrize) F[x][y] += Em[x][y] * a_ + Dm[x][y] * ee;
+            else F[x][y] += (T)2 * Em[x][y] * a_;
+            F[x][y] += (T)2 * Em[x][y] * bp;
+          }
+        if (deviatoric) {
+          if (nt->symmetrize) {
+            const T th = nt->average ? avg_th / jxw : trE * div;
+            for (int x = 0; x < d; ++x)
+              for (int y = 0; y < d; ++y) F[x][y] -= (T)(1.0 / 3.0) * Dm[x][y] * th;
+            for (int x = 0; x < d; ++x) F[x][x] -= (T)(1.0 / 3.0) * trE * a_;
+          } else {
+            for (int x = 0; x < d; ++x) F[x][x] -= (T)(2.0 / 3.0) * trE * a_;
+          }
+          if (nt->dilation) {
+            T DDm[3][3];
+            sym_full(&nt->DD[cq * ns], d, DDm);
+            T dde = 0;
+            for (int x = 0; x < d; ++x)
+              for (int y = 0; y < d; ++y) dde += DDm[x][y] * (T)0.5 * (G[x][y] + G[y][x]);
+            ptest += (dde + (T)nt->dpd[cq] * (T)s * pq) * (T)s;
+          }
+        }
+      }
+    }
     for (int cc = 0; cc < d; ++cc)
       for (int n = 0; n < nv; ++n) {
         T t = 0;
@@ -336,7 +452,7 @@ static void cell_apply(const Level& L, const FE& fe, int c, int op, double s, in
         yu[cc * nv + n] += t * jxw;
       }
     if (op == OP_STOKES) {
-      T f = -(T)s * div * jxw;
+      T f = ptest * jxw;
       for (int n = 0; n < np; ++n) yp[n] += f * (T)fe.pval[q * np + n];
     }
   }
@@ -500,13 +616,14 @@ static bool g_fast = false;
 
 template <class T>
 static void cell_apply_any(const Level& L, const FE& fe, int c, int op, double s, int compressible,
-                           const T* eta_tab, const T* xu, const T* xp, T* yu, T* yp) {
-  if (g_fast && op != OP_MASS) {
+                           const T* eta_tab, const T* xu, const T* xp, T* yu, T* yp,
+                           const NewtonTerms* nt = nullptr) {
+  if (g_fast && op != OP_MASS && !nt) {
     if (L.dim == 3) cell_apply_sf<T, 3>(L, fe, c, op, s, compressible, eta_tab, xu, xp, yu, yp);
     else cell_apply_sf<T, 2>(L, fe, c, op, s, compressible, eta_tab, xu, xp, yu, yp);
     return;
   }
-  cell_apply<T>(L, fe, c, op, s, compressible, eta_tab, xu, xp, yu, yp);
+  cell_apply<T>(L, fe, c, op, s, compressible, eta_tab, xu, xp, yu, yp, nt);
 }
 
 // sum a[i] b[i]: serial in the checker; in fast mode 256 fixed chunks summed
@@ -563,6 +680,16 @@ struct Oracle {
   // float copies of level data
   std::vector<std::vector<float>> eta_f, dA_f, dM_f;
   int a_cg_iterations = 0;
+  // Newton / prescribed-dilation tables of the outer operators (finest level)
+  NewtonTerms newton;
+  const NewtonTerms* apply_nt = nullptr;  // set while an outer operator is applied
+  struct OuterTerms {  // makes apply() add the Newton / dilation terms for one call
+    Oracle& o;
+    explicit OuterTerms(Oracle& o_) : o(o_) {
+      if (o.newton.newton || o.newton.dilation) o.apply_nt = &o.newton;
+    }
+    ~OuterTerms() { o.apply_nt = nullptr; }
+  };
 
   Level& fine() { return levels.back(); }
 
@@ -596,7 +723,7 @@ struct Oracle {
             for (int m = 0; m < e.n; ++m) v += (T)e.w[m] * src_p[e.g[m]];
             xp[i] = v;
           }
-        cell_apply_any<T>(L, fe, c, op, s, compressible, eta_tab, xu, xp, yu, yp);
+        cell_apply_any<T>(L, fe, c, op, s, compressible, eta_tab, xu, xp, yu, yp, apply_nt);
         if (wu)
           for (int i = 0; i < nu; ++i) {
             Expansion e = expand(L.cu, L.cdu[(size_t)c * nu + i]);
@@ -1145,11 +1272,13 @@ struct Oracle {
   // -------- outer (FP64) operators on the finest level
   void stokes_vmult(const double* x, double* y) {
     ActiveTable at(*this);
+    OuterTerms ot(*this);
     Level& F = fine();
     apply<double>((int)levels.size() - 1, OP_STOKES, x, x + F.n_u, y, y + F.n_u, F.eta.data());
   }
   void a_vmult(const double* x, double* y) {
     ActiveTable at(*this);
+    OuterTerms ot(*this);
     apply<double>((int)levels.size() - 1, OP_A, x, nullptr, y, nullptr, fine().eta.data());
   }
   void mass_vmult(const double* x, double* y) {
@@ -1509,6 +1638,40 @@ void* orc_create(int dim, int n_levels) {
 }
 void orc_destroy(void* p) { delete (Oracle*)p; }
 const char* orc_last_error(void* p) { return ((Oracle*)p)->err.c_str(); }
+// Newton / prescribed-dilation tables of the finest level (caller cell order, per
+// QGauss(3) point; symmetric tensors as deal.II unrolls them). flags: bit 0 Newton
+// derivatives, bit 1 symmetrize, bit 2 average Newton factors, bit 3 prescribed
+// dilation. Null arrays: not used by the flags set.
+int orc_set_newton(void* p, int flags, const double* E, const double* D, const double* dp, const double* lhs,
+                   const double* DD, const double* dpd) {
+  Oracle* h = (Oracle*)p;
+  GUARD({
+    orc::NewtonTerms& t = h->newton;
+    const auto& F = h->levels.back();
+    const size_t nq = (size_t)F.n_cells * h->fe.nq, ns = h->dim == 3 ? 6 : 3;
+    t = orc::NewtonTerms{};
+    t.newton = flags & 1;
+    t.symmetrize = flags & 2;
+    t.average = flags & 4;
+    t.dilation = flags & 8;
+    if (t.newton) {
+      if (!E || !D || !dp) throw std::runtime_error("Newton terms need E, D and dp");
+      t.E.assign(E, E + nq * ns);
+      t.D.assign(D, D + nq * ns);
+      t.dp.assign(dp, dp + nq);
+    }
+    if (t.dilation) {
+      if (!lhs) throw std::runtime_error("a prescribed dilation needs its lhs table");
+      t.lhs.assign(lhs, lhs + nq);
+      if (t.newton) {
+        if (!DD || !dpd) throw std::runtime_error("Newton terms with a dilation need DD and dpd");
+        t.DD.assign(DD, DD + nq * ns);
+        t.dpd.assign(dpd, dpd + nq);
+      }
+    }
+  })
+}
+
 // 1: sum-factorised cell operators and parallel reductions (CPU baseline timing);
 // 0 (default): the checker's plain quadrature loops and serial reductions
 int orc_set_fast(int on) {
@@ -1593,6 +1756,11 @@ int orc_vmult(void* p, int op, int lev, int use_float, const double* src, double
     int nout = op == 0 ? L.n_u + L.n_p : (op == 3 ? L.n_p : L.n_u);
     const double* su = op == 0 || op == 1 ? src : nullptr;
     const double* sp = op == 0 ? src + L.n_u : (op >= 2 ? src : nullptr);
+    // the Stokes operator of the finest level is the outer one (per-point table
+    // without averaging, Newton / dilation terms); everything else the multigrid's
+    const bool outer = op == 0 && lev == (int)h->levels.size() - 1;
+    std::unique_ptr<orc::Oracle::ActiveTable> at(outer ? new orc::Oracle::ActiveTable(*h) : nullptr);
+    std::unique_ptr<orc::Oracle::OuterTerms> ot(outer ? new orc::Oracle::OuterTerms(*h) : nullptr);
     if (!use_float) {
       double* du = op == 3 ? nullptr : dst;
       double* dp = op == 0 ? dst + L.n_u : (op == 3 ? dst : nullptr);
