@@ -93,8 +93,10 @@ struct Handle {
   // FP64 dense coarse solve: pseudo-inverses of the level-0 A and mass matrices
   DevBuf<double> coarse_pinv[2], coarse_x, coarse_y;
   bool coarse_ready = false;
-  // levels 0..mass_bottom_top of the FP32 mass V-cycle run in one single-block launch (-1: none)
+  // levels 0..mass_bottom_top of the FP32 mass V-cycle run in one single-block launch (-1: none),
+  // levels 0..mass_cluster_top in one cluster launch that includes them (-1: none)
   int mass_bottom_top = -1;
+  int mass_cluster_top = -1;
 
   Level& top() { return levels.back(); }
   void reset_graphs() {
@@ -532,7 +534,9 @@ void coarse_dense(Handle& H, int block, T* sol, const T* def) {
 
 // Levels 0..K of the FP32 mass V-cycle as one launch (see mass_bottom.cu): the
 // same steps, coefficients and vectors as the multi-launch recursion below.
-void mass_bottom(Handle& H, int K) {
+// bottom_top >= 0: levels bottom_top+1..K spread over a thread-block cluster and
+// 0..bottom_top on its first block; -1: all on one block.
+void mass_bottom(Handle& H, int K, int bottom_top = -1) {
   MassBottomArgs A{};
   A.n_levels = K + 1;
   for (int l = 0; l <= K; ++l) {
@@ -571,8 +575,31 @@ void mass_bottom(Handle& H, int K) {
       rhok = rhokp;
     }
   }
-  launch_mass_vcycle_bottom(A, mass_bottom_layout(A), H.st);
+  if (bottom_top >= 0) {
+    A.n_levels = bottom_top + 1;  // shared-memory copies of the single-block levels only
+    const int smem = mass_bottom_layout(A);
+    A.n_levels = K + 1;
+    launch_mass_vcycle_cluster(A, bottom_top, smem, H.st);
+  } else {
+    launch_mass_vcycle_bottom(A, mass_bottom_layout(A), H.st);
+  }
   ++H.cell_launches;
+}
+
+// the highest level K of the FP32 mass V-cycle that the cluster kernel takes
+// (levels above the single-block bottom of at most kMaxClusterNodes pressure
+// nodes, 3D lattice levels), or -1
+int plan_mass_cluster(const Handle& H) {
+  if (H.mass_bottom_top < 0 || H.opt.coarse_solver != GB_GMG_COARSE_CHEBYSHEV) return -1;
+  if (mass_cluster_reserve() <= 0) return -1;
+  int K = -1;
+  for (int l = H.mass_bottom_top + 1; l < H.n_levels && l < kMaxBottomLevels; ++l) {
+    const Level& L = H.levels[l];
+    if (!L.structured || L.dim != 3 || L.n_p > kMaxClusterNodes) break;
+    if (cheb_params(H, l).degree > kMaxBottomDegree) break;
+    K = l;
+  }
+  return K;
 }
 
 // the highest level K such that levels 0..K qualify for mass_bottom: 3D lattice
@@ -600,6 +627,10 @@ int plan_mass_bottom(const Handle& H) {
 template <typename T>
 void vcycle_level(Handle& H, int lev, int block) {
   if constexpr (std::is_same<T, float>::value) {
+    if (block == 1 && lev == H.mass_cluster_top) {
+      mass_bottom(H, lev, H.mass_bottom_top);
+      return;
+    }
     if (block == 1 && lev <= H.mass_bottom_top) {
       mass_bottom(H, lev);
       return;
@@ -1422,7 +1453,7 @@ void gb_gmg_default_options(gb_gmg_options* o) {
   o->schur_smoothing_steps = 4;
   o->force_indexed_layout = 0;
   o->coarse_solver = GB_GMG_COARSE_CHEBYSHEV;
-  o->fused_a_min_cells = 65536;
+  o->fused_a_min_cells = 0;  // measured slower than the two-pass form (see ablock_fused.cu)
 }
 
 void gb_gmg_default_solve_params(gb_gmg_solve_params* p) {
@@ -1693,6 +1724,7 @@ int gb_gmg_build_preconditioner(gb_gmg* g) {
     H.prec_done[0] = true;
     gb::build_preconditioner_T<float>(H);
     H.mass_bottom_top = gb::plan_mass_bottom(H);
+    H.mass_cluster_top = gb::plan_mass_cluster(H);
     H.prec_done[1] = true;
   })
 }

@@ -462,23 +462,44 @@ def run_gpu(args):
 
 PROFILE_OPS = {"a_cell_pass_fp32": ("TIME_A_CELL_PASS", "FP32"), "a_vmult_fp32": ("TIME_A_VMULT", "FP32"),
                "stokes_cell_pass_fp64": ("TIME_STOKES_CELL_PASS", "FP64"),
-               "stokes_vmult_fp64": ("TIME_STOKES_VMULT", "FP64"), "mass_vmult_fp32": ("TIME_MASS_VMULT", "FP32")}
+               "stokes_vmult_fp64": ("TIME_STOKES_VMULT", "FP64"), "mass_vmult_fp32": ("TIME_MASS_VMULT", "FP32"),
+               "s_preconditioner_fp32": ("TIME_S_PRECONDITIONER", "FP32"),
+               "a_preconditioner_fp32": ("TIME_A_PRECONDITIONER", "FP32"),
+               "build_preconditioner": (None, None), "solve_fp32": (None, None)}
 
 
 def run_profile_op(name: str):
-    """One operation of the workload, three times inside cudaProfilerStart/Stop."""
+    """One operation of the workload, three times (a solve or the preconditioner
+    set-up once) inside cudaProfilerStart/Stop, for ncu --profile-from-start off."""
     import torch
     from aspect_gb300 import gmg
     torch.cuda.init()
     P = build_problem()
     g = gmg.from_problem(P)
-    what, prec = getattr(gmg, PROFILE_OPS[name][0]), getattr(gmg, PROFILE_OPS[name][1])
-    g.time_operation(what, prec, 3)
-    torch.cuda.synchronize()
-    torch.cuda.profiler.start()
-    sec = g.time_operation(what, prec, 3)
-    torch.cuda.synchronize()
-    torch.cuda.profiler.stop()
+    if name == "build_preconditioner":
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        t0 = time.perf_counter()
+        g.build_preconditioner()
+        torch.cuda.synchronize()
+        sec = time.perf_counter() - t0
+        torch.cuda.profiler.stop()
+    elif name == "solve_fp32":
+        g.solve(P.rhs, linear_solver_tolerance=TOL, mg_precision=gmg.FP32)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        _, out = g.solve(P.rhs, linear_solver_tolerance=TOL, mg_precision=gmg.FP32)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        sec = out["solve_seconds"]
+    else:
+        what, prec = getattr(gmg, PROFILE_OPS[name][0]), getattr(gmg, PROFILE_OPS[name][1])
+        g.time_operation(what, prec, 3)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        sec = g.time_operation(what, prec, 3)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     print(json.dumps({"profile_op": name, "seconds_per_call": sec, "cells": P.fine.n_cells}), flush=True)
 
 
@@ -515,8 +536,7 @@ def run_sweep(sizes):
               "stokes_vmult_fp64": ("fp64", ALG_FLOPS_STOKES_CELL),
               "stokes_cell_pass_fp64": ("fp64", ALG_FLOPS_STOKES_CELL)}
         line = {"sweep": f"sinkers_{nc}^3", "cells": f.n_cells, "n_u": f.n_u, "n_p": f.n_p, "peak_gbs": peak,
-                "peak_kind": peak_kind, "peak_tflops": fp, "host_problem_seconds": t_problem,
-                "fused_a_block": nc % 16 == 0 and f.n_cells >= 65536, "ops": {}}
+                "peak_kind": peak_kind, "peak_tflops": fp, "host_problem_seconds": t_problem, "ops": {}}
         for k in t:
             gbs = b[k] / t[k] / 1e9
             row = {"seconds": t[k], "algorithmic_bytes": b[k], "gbs": gbs, "hbm_frac": gbs / peak,
@@ -530,8 +550,10 @@ def run_sweep(sizes):
         del g
 
 
-def _solve_pair(P, options=None, project=None):
-    """FP64-MG and FP32-MG solves of one workload (each timed after a warm-up solve)."""
+def _solve_pair(P, options=None, project=None, oracle_residual=False):
+    """FP64-MG and FP32-MG solves of one workload (each timed after a warm-up solve);
+    oracle_residual: also the FP64 residual of both solutions, measured by the CPU
+    oracle (the checker) on the same level meshes."""
     from aspect_gb300 import gmg
     t0 = time.perf_counter()
     g = gmg.from_problem(P, options)
@@ -541,7 +563,8 @@ def _solve_pair(P, options=None, project=None):
         g.solve(P.rhs, linear_solver_tolerance=TOL, mg_precision=prec)  # warm
         x, o = g.solve(P.rhs, linear_solver_tolerance=TOL, mg_precision=prec)
         res[key] = {"solve_s": o["solve_seconds"], "iterations": o["cheap_iterations"] + o["expensive_iterations"],
-                    "status": o["status"], "x": x}
+                    "status": o["status"], "tolerance": o["solver_tolerance"],
+                    "final_residual": o["final_linear_residual"], "x": x}
     f = P.fine
     u64, u32 = res["fp64_mg"]["x"][: f.n_u], res["fp32_mg"]["x"][: f.n_u]
     if project is not None:
@@ -555,6 +578,15 @@ def _solve_pair(P, options=None, project=None):
             "speedup_fp32_mg": res["fp64_mg"]["solve_s"] / res["fp32_mg"]["solve_s"],
             "velocity_rel_l2_fp32_vs_fp64": rel(u32, u64),
             "pressure_rel_l2_fp32_vs_fp64": rel(res["fp32_mg"]["x"][f.n_u:], res["fp64_mg"]["x"][f.n_u:])}
+    if oracle_residual:
+        from oracle import Oracle
+        t0 = time.perf_counter()
+        o = Oracle(P.levels)
+        o.set_viscosity(P.eta, P.projection, P.pressure_scaling)
+        for key in ("fp64_mg", "fp32_mg"):
+            r = P.rhs - o.vmult(0, len(P.levels) - 1, res[key]["x"])
+            res[key]["oracle_residual"] = float(np.linalg.norm(r))
+        line["oracle_seconds"] = time.perf_counter() - t0
     for key in ("fp64_mg", "fp32_mg"):
         line[key] = {k: v for k, v in res[key].items() if k != "x"}
     return line
@@ -567,10 +599,16 @@ def _config_line(name):
         return _solve_pair(problems.solcx(6, density_sign=1.0))
     if name == "sphere16":
         return _solve_pair(problems.adaptive_sphere(4, 2))
-    if name == "shell3":
-        P = problems.spherical_shell(3)
+    if name in ("shell3", "shell3a"):
+        # refinement 3, and for shell3a one adaptive level on the temperature gradient
+        t0 = time.perf_counter()
+        P = problems.spherical_shell(3, n_adaptive=1 if name == "shell3a" else 0)
+        t_mesh = time.perf_counter() - t0
         q, _ = np.linalg.qr(shell.rotation_modes(P.fine).T)
-        return _solve_pair(P, {"coarse_solver": gmg.COARSE_DENSE_FP64}, lambda u: u - q @ (q.T @ u))
+        line = _solve_pair(P, {"coarse_solver": gmg.COARSE_DENSE_FP64}, lambda u: u - q @ (q.T @ u),
+                           oracle_residual=name == "shell3a")
+        line["host_mesh_seconds"] = t_mesh
+        return line
     if name == "adjoint32":
         def factory(base):
             g = gmg.StokesMatrixFreeGPU(3, len(base.levels))
@@ -614,7 +652,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--profile-op", default=None, choices=sorted(PROFILE_OPS))
     ap.add_argument("--sweep", default=None, help="comma-separated cells per direction, e.g. 32,64")
-    ap.add_argument("--configs", default=None, help="comma-separated: solcx64,sphere16,adjoint32,shell3")
+    ap.add_argument("--configs", default=None,
+                    help="comma-separated: solcx64,sphere16,adjoint32,shell3,shell3a")
     args = ap.parse_args()
     if args.configs:
         run_configs(args.configs.split(","))

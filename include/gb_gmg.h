@@ -112,9 +112,10 @@ typedef struct gb_gmg_options {
   int schur_smoothing_steps;    /* SmootherRelaxation steps for the Schur block (4)  */
   int force_indexed_layout;     /* 1: never use the lattice fast path (testing)      */
   int coarse_solver;            /* gb_gmg_coarse_solver (Chebyshev as the reference)  */
-  int fused_a_min_cells;        /* FP32 A-block applications of 3D lattice levels with at
-                                   least this many cells (and 16 x 8 | cells in x, y) run
-                                   as one fused cell-and-gather pass (65536; 0: never)  */
+  int fused_a_min_cells;        /* > 0: FP32 A-block applications of 3D lattice levels
+                                   with at least this many cells (and 16 x 8 | cells in
+                                   x, y) run as one fused cell-and-gather pass (0: never,
+                                   the default: the two-pass form measured faster)      */
 } gb_gmg_options;
 
 enum gb_gmg_coarse_solver {
