@@ -93,10 +93,8 @@ struct Handle {
   // FP64 dense coarse solve: pseudo-inverses of the level-0 A and mass matrices
   DevBuf<double> coarse_pinv[2], coarse_x, coarse_y;
   bool coarse_ready = false;
-  // levels 0..mass_bottom_top of the FP32 mass V-cycle run in one single-block launch (-1: none),
-  // levels 0..mass_cluster_top in one cluster launch that includes them (-1: none)
+  // levels 0..mass_bottom_top of the FP32 mass V-cycle run in one single-block launch (-1: none)
   int mass_bottom_top = -1;
-  int mass_cluster_top = -1;
 
   Level& top() { return levels.back(); }
   void reset_graphs() {
@@ -534,9 +532,7 @@ void coarse_dense(Handle& H, int block, T* sol, const T* def) {
 
 // Levels 0..K of the FP32 mass V-cycle as one launch (see mass_bottom.cu): the
 // same steps, coefficients and vectors as the multi-launch recursion below.
-// bottom_top >= 0: levels bottom_top+1..K spread over a thread-block cluster and
-// 0..bottom_top on its first block; -1: all on one block.
-void mass_bottom(Handle& H, int K, int bottom_top = -1) {
+void mass_bottom(Handle& H, int K) {
   MassBottomArgs A{};
   A.n_levels = K + 1;
   for (int l = 0; l <= K; ++l) {
@@ -575,31 +571,8 @@ void mass_bottom(Handle& H, int K, int bottom_top = -1) {
       rhok = rhokp;
     }
   }
-  if (bottom_top >= 0) {
-    A.n_levels = bottom_top + 1;  // shared-memory copies of the single-block levels only
-    const int smem = mass_bottom_layout(A);
-    A.n_levels = K + 1;
-    launch_mass_vcycle_cluster(A, bottom_top, smem, H.st);
-  } else {
-    launch_mass_vcycle_bottom(A, mass_bottom_layout(A), H.st);
-  }
+  launch_mass_vcycle_bottom(A, mass_bottom_layout(A), H.st);
   ++H.cell_launches;
-}
-
-// the highest level K of the FP32 mass V-cycle that the cluster kernel takes
-// (levels above the single-block bottom of at most kMaxClusterNodes pressure
-// nodes, 3D lattice levels), or -1
-int plan_mass_cluster(const Handle& H) {
-  if (H.mass_bottom_top < 0 || H.opt.coarse_solver != GB_GMG_COARSE_CHEBYSHEV) return -1;
-  if (mass_cluster_reserve() <= 0) return -1;
-  int K = -1;
-  for (int l = H.mass_bottom_top + 1; l < H.n_levels && l < kMaxBottomLevels; ++l) {
-    const Level& L = H.levels[l];
-    if (!L.structured || L.dim != 3 || L.n_p > kMaxClusterNodes) break;
-    if (cheb_params(H, l).degree > kMaxBottomDegree) break;
-    K = l;
-  }
-  return K;
 }
 
 // the highest level K such that levels 0..K qualify for mass_bottom: 3D lattice
@@ -627,10 +600,6 @@ int plan_mass_bottom(const Handle& H) {
 template <typename T>
 void vcycle_level(Handle& H, int lev, int block) {
   if constexpr (std::is_same<T, float>::value) {
-    if (block == 1 && lev == H.mass_cluster_top) {
-      mass_bottom(H, lev, H.mass_bottom_top);
-      return;
-    }
     if (block == 1 && lev <= H.mass_bottom_top) {
       mass_bottom(H, lev);
       return;
@@ -654,10 +623,11 @@ void vcycle_level(Handle& H, int lev, int block) {
   const long nc = block == 0 ? C.n_u : C.n_p;
   smoother_apply<T>(H, lev, block, sol, def);
   level_op_resid<T>(H, lev, block, sol, def, t);
-  v_zero<T>(nc, cdef, H.st);
-  if (block == 0) v_spmv_add<T>(L.PuT_rows, L.PuT_ptr.p, L.PuT_col.p, D.PuT_val.p, t, cdef, H.st);
-  else v_spmv_add<T>(L.PpT_rows, L.PpT_ptr.p, L.PpT_col.p, D.PpT_val.p, t, cdef, H.st);
-  v_zero<T>(nc, csol, H.st);
+  // restriction (zero fill and product in one launch)
+  if (block == 0) v_spmv_set<T>(L.PuT_rows, nc, L.PuT_ptr.p, L.PuT_col.p, D.PuT_val.p, t, cdef, H.st);
+  else v_spmv_set<T>(L.PpT_rows, nc, L.PpT_ptr.p, L.PpT_col.p, D.PpT_val.p, t, cdef, H.st);
+  // the coarse solution needs no zero fill: every coarse solve (the smoother from
+  // a zero start, the single-block bottom, the dense coarse solve) writes all of it
   vcycle_level<T>(H, lev - 1, block);
   if (block == 0) v_spmv_add<T>(L.Pu_rows, L.Pu_ptr.p, L.Pu_col.p, D.Pu_val.p, csol, sol, H.st);
   else v_spmv_add<T>(L.Pp_rows, L.Pp_ptr.p, L.Pp_col.p, D.Pp_val.p, csol, sol, H.st);
@@ -1724,7 +1694,6 @@ int gb_gmg_build_preconditioner(gb_gmg* g) {
     H.prec_done[0] = true;
     gb::build_preconditioner_T<float>(H);
     H.mass_bottom_top = gb::plan_mass_bottom(H);
-    H.mass_cluster_top = gb::plan_mass_cluster(H);
     H.prec_done[1] = true;
   })
 }

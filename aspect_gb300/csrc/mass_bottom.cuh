@@ -5,7 +5,7 @@
 
 namespace gb {
 
-constexpr int kMaxBottomLevels = 6;
+constexpr int kMaxBottomLevels = 4;
 constexpr int kMaxBottomDegree = 16;
 // Levels above this many pressure nodes keep the per-step launches. Measured on
 // the 32^3 lattice hierarchy (Schur V-cycle, FP32, one GB300): nothing fused
@@ -39,9 +39,6 @@ struct MassBottomLevel {
   // offsets (in floats, multiples of 4) of this level's shared-memory copies:
   // Mc, dinv, sol, def, d, t
   int off[6];
-  // the global vectors while the single-block part works on shared copies
-  float *gsol, *gdef, *gd, *gt;
-  const float *gMc, *gdinv;
 };
 
 struct MassBottomArgs {
@@ -56,10 +53,5 @@ int mass_bottom_layout(MassBottomArgs& A);
 // attribute the first time; call outside stream capture).
 int mass_bottom_reserve();
 void launch_mass_vcycle_bottom(const MassBottomArgs& A, int smem_bytes, cudaStream_t s);
-// Levels 0..n_levels-1 with levels bottom_top+1.. spread over a thread-block
-// cluster and 0..bottom_top on its first block (mass_bottom.cu).
-constexpr int kMaxClusterNodes = 6000;  // pressure nodes of the largest cluster level
-int mass_cluster_reserve();
-void launch_mass_vcycle_cluster(const MassBottomArgs& A, int bottom_top, int smem_bytes, cudaStream_t s);
 
 }  // namespace gb

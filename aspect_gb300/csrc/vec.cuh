@@ -57,6 +57,9 @@ void v_permute_gather(long n, const int* perm, const Ts* in, Td* out, cudaStream
 // y += A x (CSR)
 template <typename T>
 void v_spmv_add(long rows, const int* ptr, const int* col, const T* val, const T* x, T* y, cudaStream_t s);
+// y[r] = (A x)[r] for r < rows, 0 for rows <= r < n
+template <typename T>
+void v_spmv_set(long rows, long n, const int* ptr, const int* col, const T* val, const T* x, T* y, cudaStream_t s);
 // The reductions and the multi-axpy take an optional device flag `active`: when
 // it points to 0 the launches return at once (a step that the device decided to
 // skip without a round trip to the host).
