@@ -1553,6 +1553,7 @@ int gb_gmg_finalize_setup(gb_gmg* g) {
     for (auto& L : H.levels) GB_CHECK(L.n_cells > 0, 2, "a level has no mesh");
     for (auto& L : H.levels) gb::setup_level(L, H.opt.force_indexed_layout != 0);
     for (int l = 1; l < H.n_levels; ++l) gb::setup_transfer(H.levels[l], H.levels[l - 1]);
+    gb::setup_coefficient_maps(H.levels);
     for (auto& L : H.levels) {  // FP32 A-block applications of large lattice levels: fused kernel
       L.fused_tz = 0;
       L.f32.Fa.release();
@@ -1593,9 +1594,9 @@ int gb_gmg_set_viscosity(gb_gmg* g, const double* eta, int n_per_cell, int proje
     H.compressible = compressible;
     H.projection = projection;
     H.visc_done = false;
-    gb::compute_level_viscosity(H.levels, eta, n_per_cell, projection, H.eta_min, H.eta_max);
+    GB_CHECK(eta, 1, "null viscosity");
+    gb::device_level_viscosity(H.levels, eta, n_per_cell, projection, s, H.eta_min, H.eta_max, H.st);
     H.visc_n_per_cell = n_per_cell;
-    for (auto& L : H.levels) gb::upload_viscosity(L, s);
     H.reset_graphs();
     H.visc_done = true;
     H.prec_done[0] = H.prec_done[1] = false;
@@ -1612,26 +1613,10 @@ int gb_gmg_update_viscosity(gb_gmg* g, const double* eta, int n_per_cell) {
     // V-cycles all assume the layout of the last set_viscosity: a different one
     // is rejected before anything changes.
     GB_CHECK(n_per_cell == H.visc_n_per_cell, 1, "viscosity layout differs from the last set_viscosity");
-    std::vector<std::vector<double>> saved_eta;
-    std::vector<int> saved_n;
-    for (auto& L : H.levels) {
-      saved_eta.push_back(L.eta);
-      saved_n.push_back(L.eta_n);
-    }
+    // the values are checked before any table changes; the tables keep their
+    // sizes, so device addresses (and captured graphs) stay valid
     double mn, mx;
-    try {
-      gb::compute_level_viscosity(H.levels, eta, n_per_cell, H.projection, mn, mx);
-      for (auto& L : H.levels)
-        GB_CHECK(L.eta.size() == L.f64.eta.n, 1, "viscosity layout differs from the last set_viscosity");
-    } catch (...) {
-      for (size_t l = 0; l < H.levels.size(); ++l) {
-        H.levels[l].eta = std::move(saved_eta[l]);
-        H.levels[l].eta_n = saved_n[l];
-      }
-      throw;
-    }
-    // same sizes on every level: device addresses (and captured graphs) stay valid
-    for (auto& L : H.levels) gb::upload_viscosity(L, H.s);
+    gb::device_level_viscosity(H.levels, eta, n_per_cell, H.projection, H.s, mn, mx, H.st);
     H.eta_min = mn;
     H.eta_max = mx;
   })

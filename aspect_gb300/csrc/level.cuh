@@ -103,10 +103,15 @@ struct Level {
   // viscosity table, internal cell order
   std::vector<double> eta;
   int eta_n = 1;
-  // without averaging (GB_GMG_VISC_NONE), finest level only: the per-point table
-  // of the outer operators, caller cell order (eta_active_n = 0: none)
-  std::vector<double> eta_active;
+  // without averaging (GB_GMG_VISC_NONE), finest level only: the outer operators
+  // also have a per-point table (eta_active_n = 0: none)
   int eta_active_n = 0;
+  // device coefficient pipeline (coefficients.cu): caller -> internal cells, the
+  // children of every cell of the next coarser level (CSR by fine-cell index),
+  // child indices, the finest level's JxW per point and input values, DG fields
+  DevBuf<int> ioc_d, kid_ptr_d, kid_d;
+  DevBuf<unsigned char> child_d;
+  DevBuf<double> jxw_d, eta_in_d, dg_d;
 
   template <typename T>
   LevelDev<T>& dev();
@@ -139,8 +144,11 @@ inline LevelDev<double>& Level::dev<double>() { return f64; }
 // set-up steps (level_setup.cu)
 void setup_level(Level& L, bool force_indexed);
 void setup_transfer(Level& fine, const Level& coarse);
-void compute_level_viscosity(std::vector<Level>& levels, const double* eta_in, int n_per_cell, int projection,
-                             double& eta_min, double& eta_max);
-void upload_viscosity(Level& L, double pressure_scaling);
+// device coefficient pipeline (coefficients.cu): the static maps once per mesh,
+// then every level's viscosity table (both precisions, internal cell order) and
+// the lattice levels' pressure mass matrices from the finest level's values
+void setup_coefficient_maps(std::vector<Level>& levels);
+void device_level_viscosity(std::vector<Level>& levels, const double* eta_in, int n_per_cell, int projection,
+                            double pressure_scaling, double& eta_min, double& eta_max, cudaStream_t st);
 
 }  // namespace gb

@@ -556,217 +556,6 @@ void setup_transfer(Level& F, const Level& C) {
   }
 }
 
-// Level viscosity tables (stokes_matrix_free_local_smoothing.cc:174-294), in
-// caller cell order into Level::eta (then permuted by upload_viscosity).
-void compute_level_viscosity(std::vector<Level>& levels, const double* eta_in, int n_per_cell, int projection,
-                             double& eta_min, double& eta_max) {
-  const int nlev = (int)levels.size();
-  Level& Fl = levels.back();
-  const int d = Fl.dim, nq = nv_of(d), ncv = np_of(d);
-  eta_min = 1e300;
-  eta_max = -1e300;
-  for (long i = 0; i < Fl.n_cells * n_per_cell; ++i) {
-    GB_CHECK(eta_in[i] > 0 && std::isfinite(eta_in[i]), 6, "viscosity must be positive and finite");
-    eta_min = std::min(eta_min, eta_in[i]);
-    eta_max = std::max(eta_max, eta_in[i]);
-  }
-  // JxW of the finest level per quadrature point (for the DGQ0 projection)
-  const double g3[3] = {0.5 - std::sqrt(15.0) / 10, 0.5, 0.5 + std::sqrt(15.0) / 10};
-  const double w3[3] = {5.0 / 18, 8.0 / 18, 5.0 / 18};
-  double psi[27][8];
-  for (int q = 0; q < nq; ++q) {
-    const int qi[3] = {q % 3, (q / 3) % 3, q / 9};
-    for (int n = 0; n < ncv; ++n) {
-      double t = 1;
-      for (int e = 0; e < d; ++e) t *= ((n >> e) & 1) ? g3[qi[e]] : 1 - g3[qi[e]];
-      psi[q][n] = t;
-    }
-  }
-  auto jxw_of = [&](long c, int q) {
-    // volume weight; cells of one level have their own Jacobians
-    const int qi[3] = {q % 3, (q / 3) % 3, q / 9};
-    double w = 1;
-    for (int e = 0; e < d; ++e) w *= w3[qi[e]];
-    if (Fl.geom_kind == 0) {
-      double det = 1;
-      for (int e = 0; e < d; ++e) det *= Fl.geom[c * 2 * d + d + e];
-      return w * det;
-    }
-    if (Fl.geom_kind == 2) return w * Fl.geom[((size_t)c * nq + q) * (d * d + 1) + d * d];
-    // Q2 geometry: recompute |det J| at the point
-    const double q2n[3] = {0.0, 0.5, 1.0};
-    double v1[3][3], d1[3][3];
-    for (int e = 0; e < d; ++e) lagrange(q2n, 3, g3[qi[e]], v1[e], d1[e]);
-    double J[3][3] = {{0}};
-    const double* X = &Fl.geom[(size_t)c * nq * d];
-    for (int n = 0; n < nq; ++n) {
-      const int ni[3] = {n % 3, (n / 3) % 3, n / 9};
-      for (int b = 0; b < d; ++b) {
-        double t = 1;
-        for (int e = 0; e < d; ++e) t *= (e == b ? d1[e][ni[e]] : v1[e][ni[e]]);
-        for (int a = 0; a < d; ++a) J[a][b] += X[n * d + a] * t;
-      }
-    }
-    double det = d == 2 ? J[0][0] * J[1][1] - J[0][1] * J[1][0]
-                        : J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
-                              J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-                              J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
-    return w * std::fabs(det);
-  };
-  std::vector<std::vector<double>> dg(nlev);
-  for (auto& L : levels) {
-    L.eta_active.clear();
-    L.eta_active_n = 0;
-  }
-  if (projection == 2) {
-    // no averaging: the outer operators keep the per-point values, every level's
-    // table (the finest included) is the cellwise projection below
-    GB_CHECK(n_per_cell == nq, 1, "no averaging needs one value per quadrature point");
-    Fl.eta_active.assign(eta_in, eta_in + (size_t)Fl.n_cells * nq);
-    Fl.eta_active_n = nq;
-  }
-  if (projection == 0 || projection == 2) {
-    dg[nlev - 1].assign(Fl.n_cells, 0.0);
-    for (long c = 0; c < Fl.n_cells; ++c) {
-      if (n_per_cell == 1) {
-        dg[nlev - 1][c] = eta_in[c];
-      } else {
-        double a = 0, v = 0;
-        for (int q = 0; q < nq; ++q) {
-          const double jw = jxw_of(c, q);
-          a += jw * eta_in[c * nq + q];
-          v += jw;
-        }
-        dg[nlev - 1][c] = a / v;
-      }
-    }
-    for (int l = nlev - 1; l > 0; --l) {
-      Level& F = levels[l];
-      std::vector<double> sum(levels[l - 1].n_cells, 0.0), cnt(levels[l - 1].n_cells, 0.0);
-      for (long c = 0; c < F.n_cells; ++c) {
-        sum[F.parent[c]] += dg[l][c];
-        cnt[F.parent[c]] += 1;
-      }
-      dg[l - 1].resize(levels[l - 1].n_cells);
-      for (size_t c = 0; c < sum.size(); ++c) dg[l - 1][c] = sum[c] / cnt[c];
-    }
-    for (int l = 0; l < nlev; ++l) {
-      Level& L = levels[l];
-      const bool per_q = (l == nlev - 1 && n_per_cell == nq && projection == 0);
-      L.eta_n = per_q ? nq : 1;
-      L.eta.assign((size_t)L.n_cells * L.eta_n, 0);
-      for (long c = 0; c < L.n_cells; ++c) {
-        if (per_q)
-          for (int q = 0; q < nq; ++q) L.eta[c * nq + q] = eta_in[c * nq + q];
-        else
-          L.eta[c] = dg[l][c];
-      }
-    }
-  } else {
-    GB_CHECK(projection == 1, 1, "unknown viscosity projection");
-    GB_CHECK(n_per_cell == nq, 1, "projection to Q1 needs one value per quadrature point");
-    dg[nlev - 1].assign((size_t)Fl.n_cells * ncv, 0.0);
-    for (long c = 0; c < Fl.n_cells; ++c) {
-      double M[8][8] = {{0}}, b[8] = {0}, x[8];
-      for (int q = 0; q < nq; ++q) {
-        const double jw = jxw_of(c, q);
-        for (int i = 0; i < ncv; ++i) {
-          b[i] += jw * psi[q][i] * eta_in[c * nq + q];
-          for (int j = 0; j < ncv; ++j) M[i][j] += jw * psi[q][i] * psi[q][j];
-        }
-      }
-      for (int i = 0; i < ncv; ++i)
-        for (int r = i + 1; r < ncv; ++r) {
-          const double f = M[r][i] / M[i][i];
-          for (int k = i; k < ncv; ++k) M[r][k] -= f * M[i][k];
-          b[r] -= f * b[i];
-        }
-      for (int i = ncv - 1; i >= 0; --i) {
-        double t = b[i];
-        for (int k = i + 1; k < ncv; ++k) t -= M[i][k] * x[k];
-        x[i] = t / M[i][i];
-      }
-      for (int i = 0; i < ncv; ++i) dg[nlev - 1][c * ncv + i] = x[i];
-    }
-    for (int l = nlev - 1; l > 0; --l) {
-      Level& F = levels[l];
-      dg[l - 1].assign((size_t)levels[l - 1].n_cells * ncv, 0.0);
-      for (long c = 0; c < F.n_cells; ++c) {
-        const int ch = F.child[c], p = F.parent[c];
-        if (ch == kSameCell) {
-          for (int i = 0; i < ncv; ++i) dg[l - 1][(size_t)p * ncv + i] = dg[l][c * ncv + i];
-        } else {
-          dg[l - 1][(size_t)p * ncv + ch] = dg[l][c * ncv + ch];
-        }
-      }
-    }
-    for (int l = 0; l < nlev; ++l) {
-      Level& L = levels[l];
-      L.eta_n = nq;
-      L.eta.assign((size_t)L.n_cells * nq, 0);
-      for (long c = 0; c < L.n_cells; ++c)
-        for (int q = 0; q < nq; ++q) {
-          double v = 0;
-          for (int i = 0; i < ncv; ++i) v += psi[q][i] * dg[l][c * ncv + i];
-          L.eta[c * nq + q] = std::min(std::max(v, eta_min), eta_max);
-        }
-    }
-  }
-}
-
-void upload_viscosity(Level& L, double s) {
-  std::vector<double> e((size_t)L.n_cells * L.eta_n);
-  for (long c = 0; c < L.n_cells; ++c) {
-    const long ic = L.internal_of_cell[c];
-    for (int k = 0; k < L.eta_n; ++k) e[ic * L.eta_n + k] = L.eta[c * L.eta_n + k];
-  }
-  L.f64.eta.upload(e);
-  L.f32.eta.upload(std::vector<float>(e.begin(), e.end()));
-  if (L.eta_active_n > 0) {
-    std::vector<double> ea((size_t)L.n_cells * L.eta_active_n);
-    for (long c = 0; c < L.n_cells; ++c) {
-      const long ic = L.internal_of_cell[c];
-      for (int k = 0; k < L.eta_active_n; ++k) ea[ic * L.eta_active_n + k] = L.eta_active[c * L.eta_active_n + k];
-    }
-    L.f64.eta_active.upload(ea);
-    L.f32.eta_active.upload(std::vector<float>(ea.begin(), ea.end()));
-  } else {
-    L.f64.eta_active.release();
-    L.f32.eta_active.release();
-  }
-  if (!L.structured) return;
-  // per-cell local pressure mass matrices of a lattice level:
-  // M[i][j] = sum_q s^2 / eta_q * |det J| w_q psi_i(q) psi_j(q)
-  const int d = L.dim, nq = nv_of(d), np = np_of(d);
-  const double g3[3] = {0.5 - std::sqrt(15.0) / 10, 0.5, 0.5 + std::sqrt(15.0) / 10};
-  const double w3[3] = {5.0 / 18, 8.0 / 18, 5.0 / 18};
-  double det = 1;
-  for (int k = 0; k < d; ++k) det *= L.h[k];
-  std::vector<double> psi(nq * np), wq(nq);
-  for (int q = 0; q < nq; ++q) {
-    const int qi[3] = {q % 3, (q / 3) % 3, q / 9};
-    wq[q] = 1;
-    for (int k = 0; k < d; ++k) wq[q] *= w3[qi[k]];
-    for (int n = 0; n < np; ++n) {
-      double t = 1;
-      for (int k = 0; k < d; ++k) t *= ((n >> k) & 1) ? g3[qi[k]] : 1 - g3[qi[k]];
-      psi[q * np + n] = t;
-    }
-  }
-  std::vector<double> M((size_t)L.n_cells * np * np, 0.0);
-  for (long ic = 0; ic < L.n_cells; ++ic) {
-    double* m = &M[(size_t)ic * np * np];
-    for (int q = 0; q < nq; ++q) {
-      const double eta = e[ic * L.eta_n + (L.eta_n == 1 ? 0 : q)];
-      const double f = s * s / eta * det * wq[q];
-      for (int i = 0; i < np; ++i)
-        for (int j = 0; j < np; ++j) m[i * np + j] += f * psi[q * np + i] * psi[q * np + j];
-    }
-  }
-  L.f64.Mp.upload(M);
-  L.f32.Mp.upload(std::vector<float>(M.begin(), M.end()));
-}
-
 template <typename T>
 LevelView<T> Level::view(double s, int compressible) {
   LevelView<T> v{};
@@ -821,6 +610,8 @@ size_t Level::device_bytes() const {
          D.solM.bytes() + D.defM.bytes() + D.tM.bytes() + D.dM.bytes() + D.gu_w.bytes() + D.gp_w.bytes() +
          D.Eu.bytes() + D.Ep.bytes() + D.Mp.bytes() + D.Fa.bytes() + D.eta_active.bytes();
   };
+  b += ioc_d.bytes() + kid_ptr_d.bytes() + kid_d.bytes() + child_d.bytes() + jxw_d.bytes() + eta_in_d.bytes() +
+       dg_d.bytes();
   add(f32);
   add(f64);
   return b;
