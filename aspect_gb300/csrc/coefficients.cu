@@ -170,6 +170,35 @@ __global__ void k_mass_matrices(long n_cells, int eta_n, const double* __restric
   }
 }
 
+// Body-force right-hand side of one finest cell and velocity component:
+// V[n] = sum_q JxW_q f_comp(q) phi_n(q) (source/simulator/assemblers/stokes.cc:
+// 285-400, the rho g . phi_u term), by the transposed interpolation of the
+// point values; one thread per (cell, component), output cell-major
+// [cell][comp][node] as the velocity cell pass writes it.
+template <int dim>
+__global__ void __launch_bounds__(128) k_body_force(LevelView<double> L, const double* __restrict__ force,
+                                                   double* __restrict__ Eu) {
+  pdl_wait();
+  constexpr int nv = fe::pow3(dim), nq = nv;
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= (long)L.n_cells * dim) return;
+  const long cell = t / dim;
+  const int comp = (int)(t - cell * dim);
+  double V[nv];
+  static_for<nq>([&](auto qc) {
+    constexpr int q = decltype(qc)::value;
+    double jxw;
+    if (L.geom == GEOM_CART) jxw = L.det * qweight<dim, q>();
+    else if (L.geom == GEOM_BOX) jxw = L.gbox[cell * (dim + 1) + dim] * qweight<dim, q>();
+    else jxw = L.gtab[(cell * nq + q) * (dim * dim + 1) + dim * dim] * qweight<dim, q>();
+    V[q] = jxw * force[(cell * nq + q) * dim + comp];
+  });
+  interpolate<double, dim, true>(V);
+  double* e = Eu + (cell * dim + comp) * nv;
+#pragma unroll
+  for (int n = 0; n < nv; ++n) e[n] = V[n];
+}
+
 int grid(long n) { return (int)((n + kCoefThreads - 1) / kCoefThreads); }
 
 // Q2 basis on nodes {0, 1/2, 1}: values and derivatives at x
@@ -340,6 +369,13 @@ void device_level_viscosity(std::vector<Level>& levels, const double* eta_in, in
     GB_CUDA(cudaGetLastError());
   }
   GB_CUDA(cudaStreamSynchronize(st));
+}
+
+void launch_body_force(const LevelView<double>& L, const double* force, double* Eu, cudaStream_t st) {
+  const long n = (long)L.n_cells * L.dim;
+  if (L.dim == 3) k_body_force<3><<<grid(n), kCoefThreads, 0, st>>>(L, force, Eu);
+  else k_body_force<2><<<grid(n), kCoefThreads, 0, st>>>(L, force, Eu);
+  GB_CUDA(cudaGetLastError());
 }
 
 }  // namespace gb

@@ -1742,6 +1742,41 @@ int gb_gmg_correct_stokes_rhs(gb_gmg* g, const double* u0, double* rhs) {
   })
 }
 
+int gb_gmg_assemble_rhs(gb_gmg* g, const double* force, double* rhs) {
+  if (!g || !force || !rhs) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(H.setup_done, GB_GMG_NOT_READY, "finalize_setup has not been called");
+    const int top = H.n_levels - 1;
+    gb::Level& F = H.levels[top];
+    const int d = F.dim, nq = d == 3 ? 27 : 9;
+    const size_t per_cell = (size_t)nq * d;
+    std::vector<double> f((size_t)F.n_cells * per_cell);  // internal cell order
+    for (long c = 0; c < F.n_cells; ++c) {
+      const long ic = F.internal_of_cell[c];
+      for (size_t k = 0; k < per_cell; ++k) {
+        GB_CHECK(std::isfinite(force[c * per_cell + k]), GB_GMG_NAN_DETECTED, "non-finite body force");
+        f[ic * per_cell + k] = force[c * per_cell + k];
+      }
+    }
+    F.eta_in_d.release();  // the upload buffer of the viscosity pipeline is free between calls
+    gb::DevBuf<double> fd;
+    fd.upload(f);
+    gb::LevelDev<double>& D = F.f64;
+    const gb::LevelView<double> v = F.view<double>(H.s, H.compressible);
+    gb::launch_body_force(v, fd.p, D.Eu.p, H.st);
+    ++H.cell_launches;
+    gb::GatherArgs<double> a{};
+    a.E = D.Eu.p;
+    a.y = H.tv.p;
+    gb::gather<double>(H, F, v, 0, gb::EPI_BT, a, gb::OPK_STOKES);  // constrained rows zero
+    gb::to_caller(H, top, H.tv.p, H.stage_a.p, true, false);
+    GB_CUDA(cudaMemcpyAsync(rhs, H.stage_a.p, F.n_u * sizeof(double), cudaMemcpyDeviceToHost, H.st));
+    GB_CUDA(cudaStreamSynchronize(H.st));
+    std::fill(rhs + F.n_u, rhs + F.n_u + F.n_p, 0.0);
+  })
+}
+
 int gb_gmg_vmult(gb_gmg* g, int op, int level, int precision, const double* src, double* dst) {
   if (!g) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {

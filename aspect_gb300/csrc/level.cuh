@@ -150,5 +150,7 @@ void setup_transfer(Level& fine, const Level& coarse);
 void setup_coefficient_maps(std::vector<Level>& levels);
 void device_level_viscosity(std::vector<Level>& levels, const double* eta_in, int n_per_cell, int projection,
                             double pressure_scaling, double& eta_min, double& eta_max, cudaStream_t st);
+// per-cell body-force contributions sum_q JxW f . phi (internal cells, cell-major)
+void launch_body_force(const LevelView<double>& L, const double* force, double* Eu, cudaStream_t st);
 
 }  // namespace gb

@@ -87,7 +87,8 @@ EXPORTS = ["gb_gmg_default_options", "gb_gmg_default_solve_params", "gb_gmg_crea
            "gb_gmg_set_eigenvalues", "gb_gmg_transfer", "gb_gmg_vcycle", "gb_gmg_block_preconditioner",
            "gb_gmg_solve", "gb_gmg_solve_device", "gb_gmg_adjoint_gradient", "gb_gmg_memory_consumption",
            "gb_gmg_kernel_launches", "gb_gmg_time_operation", "gb_gmg_ablock_apply_lattice_noalloc",
-           "gb_gmg_update_viscosity", "gb_gmg_correct_stokes_rhs", "gb_gmg_set_newton_terms"]
+           "gb_gmg_update_viscosity", "gb_gmg_correct_stokes_rhs", "gb_gmg_set_newton_terms",
+           "gb_gmg_assemble_rhs"]
 
 TIME_STOKES_VMULT, TIME_A_VMULT, TIME_MASS_VMULT = 0, 1, 2
 TIME_STOKES_PRECONDITIONER, TIME_A_PRECONDITIONER, TIME_S_PRECONDITIONER = 3, 4, 5
@@ -127,6 +128,7 @@ def load_library(path: str = LIB_PATH):
     L.gb_gmg_set_newton_terms.argtypes = [vp, ctypes.POINTER(NewtonTerms)]
     L.gb_gmg_vmult.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp]
     L.gb_gmg_correct_stokes_rhs.argtypes = [vp, dp, dp]
+    L.gb_gmg_assemble_rhs.argtypes = [vp, dp, dp]
     L.gb_gmg_vmult_device.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, dp]
     L.gb_gmg_get_diagonal_inverse.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
     L.gb_gmg_get_eigenvalues.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
@@ -285,6 +287,14 @@ class StokesMatrixFreeGPU:
         u0 = _d(u0)
         out = _d(rhs).copy()
         self._chk(self.L.gb_gmg_correct_stokes_rhs(self.h, _p(u0), _p(out)))
+        return out
+
+    def assemble_rhs(self, force_q):
+        """Body-force right-hand side int f . phi_u of the finest level on the device,
+        condensed with the velocity constraints; force_q: (n_cells, 3**dim, dim)."""
+        f = _d(force_q)
+        out = np.zeros(self.levels[-1].n_u + self.levels[-1].n_p)
+        self._chk(self.L.gb_gmg_assemble_rhs(self.h, _p(f), _p(out)))
         return out
 
     def vmult_device(self, d_src: int, d_dst: int, precision: int = FP64):

@@ -50,10 +50,11 @@ N_CELLS_1D = 32
 ALG_FLOPS_A_CELL = 6912
 ALG_FLOPS_STOKES_CELL = 7638
 # dram__bytes_read.sum + dram__bytes_write.sum of one finest-level launch of the
-# FP64 Stokes cell pass (ncu, cold cache, `bench.py --profile-op
-# stokes_cell_pass_fp64`, profiles/): the reads of u, p and eta and the writes
-# of the per-cell contributions that leave L2
-STOKES_CELL_PASS_F64_DRAM_BYTES = None
+# FP64 Stokes cell pass at 32^3 (ncu --metrics dram__bytes_read.sum,
+# dram__bytes_write.sum of `bench.py --profile-op stokes_cell_pass_fp64`, two
+# launches: 13,968,128 and 13,968,384 bytes read, 0 written -- the reads of u, p
+# and eta; the per-cell contributions stay in L2)
+STOKES_CELL_PASS_F64_DRAM_BYTES = 13968256
 
 
 def measured_fp_peaks():

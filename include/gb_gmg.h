@@ -253,6 +253,16 @@ int gb_gmg_vmult(gb_gmg* h, int op, int level, int precision, const double* src,
    the constraints) afterwards, as the reference does. */
 int gb_gmg_correct_stokes_rhs(gb_gmg* h, const double* u0, double* rhs);
 
+/* The body-force right-hand side of the finest level on the device
+ * (source/simulator/assemblers/stokes.cc:285-400, the rho g . phi_u term):
+ * rhs_u = int f . phi_u over QGauss(3), condensed with the velocity constraints
+ * as AffineConstraints::distribute_local_to_global does (contributions of a
+ * constrained DoF go to the DoFs of its line, constrained rows are zero);
+ * the pressure part is zero. force: host array [n_cells][3^dim][dim] (caller
+ * cell order, lexicographic points), e.g. rho g at the points; rhs: host array
+ * of n_u + n_p doubles (caller numbering), overwritten. */
+int gb_gmg_assemble_rhs(gb_gmg* h, const double* force, double* rhs);
+
 /* Same, on device arrays of the finest level in the caller's numbering. */
 int gb_gmg_vmult_device(gb_gmg* h, int op, int precision, const double* d_src, double* d_dst);
 

@@ -53,3 +53,24 @@ def test_correct_stokes_rhs_matches_assembled(case, force, comp):
     assert rel_err(got - rhs, -corr) < 1e-12
     assert np.array_equal(got[: f.n_u][mu], rhs[: f.n_u][mu])
     assert rel_err(got, ref) < 1e-12
+
+
+@pytest.mark.parametrize("case", ["box3d", "box2d", "adaptive2d", "shell"])
+def test_body_force_rhs_on_device(case):
+    """gb_gmg_assemble_rhs (the rho g . phi_u term of source/simulator/assemblers/
+    stokes.cc:285-400, condensed with the constraints) against the harness's numpy
+    assembly: lattice, indexed hanging-node and curved Q2 levels, 1e-12."""
+    from aspect_gb300 import problems, shell
+    if case == "shell":
+        levels = shell.hierarchy(1, 4, 0.55, 1.0)
+    else:
+        levels = _levels(case)
+    f = levels[-1]
+    rng = np.random.default_rng(4)
+    force = rng.normal(size=(f.n_cells, 3 ** f.dim, f.dim))
+    g = gmg.StokesMatrixFreeGPU(f.dim, len(levels))
+    g.setup_dofs(levels)
+    ref = problems.assemble_rhs(f, force)
+    got = g.assemble_rhs(force)
+    assert rel_err(got, ref) < 1e-12
+    assert np.all(got[f.n_u:] == 0.0) and np.all(got[f.constraints_u.rows] == 0.0)
