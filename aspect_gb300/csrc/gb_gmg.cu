@@ -68,6 +68,30 @@ struct Handle {
       for (auto& b : t32) b.release();
     }
   } newton_terms;
+  // free-surface faces of the outer Stokes operator (finest level; see FreeSurfaceView):
+  // codes read through the constraints (operator) or plain (rhs correction)
+  struct FreeSurface {
+    int n_groups = 0;
+    long n_faces = 0;
+    DevBuf<int> gptr, gcell, fno, codes, raw;
+    DevBuf<double> t64;
+    DevBuf<float> t32;
+    bool on() const { return n_faces > 0; }
+    template <typename T>
+    FreeSurfaceView<T> view(bool plain = false) const {
+      const T* tab;
+      if constexpr (std::is_same<T, double>::value) tab = t64.p;
+      else tab = t32.p;
+      return FreeSurfaceView<T>{n_groups, gptr.p, gcell.p, fno.p, plain ? raw.p : codes.p, tab};
+    }
+    void clear() {
+      n_groups = 0;
+      n_faces = 0;
+      for (auto* b : {&gptr, &gcell, &fno, &codes, &raw}) b->release();
+      t64.release();
+      t32.release();
+    }
+  } free_surface;
   int n_sm = 1;             // streaming multiprocessors of the handle's GPU
   double eta_min = 0, eta_max = 0;
   bool setup_done = false, visc_done = false;
@@ -209,12 +233,18 @@ void apply_op(Handle& H, int lev, int op, const T* su, const T* sp, T* du, T* dp
   const bool own_table = outer && L.eta_active_n > 0;
   LevelView<T> v = own_table ? L.view_outer<T>(H.s, H.compressible) : L.view<T>(H.s, H.compressible);
   const bool newton = outer && lev == H.n_levels - 1 && H.newton_terms.on();
+  // free-surface faces: the outer Stokes operator of the finest level only
+  const bool free_surface = outer && lev == H.n_levels - 1 && op == OPK_STOKES && H.free_surface.on();
   // a prescribed dilation makes the outer viscous terms deviatoric (not the levels')
   if (newton && H.newton_terms.dilation) v.compressible = 1;
   if (newton && op == OPK_STOKES) {
     launch_newton_stokes<T>(v, H.newton_terms.view<T>(), su, sp, D.Eu.p, D.Ep.p, cell_pass_slot_major<T>(v, op),
                             H.st);
     ++H.cell_launches;
+    if (free_surface) {
+      launch_free_surface<T>(v, H.free_surface.view<T>(), su, D.Eu.p, cell_pass_slot_major<T>(v, op), H.st);
+      ++H.cell_launches;
+    }
     for (int block = 0; block < 2; ++block) {
       GatherArgs<T> a{};
       a.E = block == 0 ? D.Eu.p : D.Ep.p;
@@ -239,6 +269,10 @@ void apply_op(Handle& H, int lev, int op, const T* su, const T* sp, T* du, T* dp
   }
   launch_cell_pass<T>(v, op, su, sp, D.Eu.p, D.Ep.p, H.st);
   ++H.cell_launches;
+  if (free_surface) {
+    launch_free_surface<T>(v, H.free_surface.view<T>(), su, D.Eu.p, cell_pass_slot_major<T>(v, op), H.st);
+    ++H.cell_launches;
+  }
   if (op == OPK_STOKES || op == OPK_A || op == OPK_BT) {
     GatherArgs<T> a{};
     a.E = D.Eu.p;
@@ -1576,6 +1610,7 @@ int gb_gmg_finalize_setup(gb_gmg* g) {
       L.cdp_raw_d.release();
     }
     H.newton_terms.clear();
+    H.free_surface.clear();
     H.setup_done = true;
     H.visc_done = false;
     H.prec_done[0] = H.prec_done[1] = false;
@@ -1668,6 +1703,94 @@ int gb_gmg_set_newton_terms(gb_gmg* g, const gb_gmg_newton_terms* t) {
   })
 }
 
+int gb_gmg_set_free_surface(gb_gmg* g, int64_t n_faces, const int32_t* face_cell, const int32_t* face_no,
+                            const double* stabilization, const double* normal_jxw) {
+  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  ABI_TRY(g, {
+    Handle& H = g->h;
+    GB_CHECK(H.setup_done, GB_GMG_NOT_READY, "finalize_setup has not been called");
+    auto& FS = H.free_surface;
+    if (n_faces <= 0 || !face_cell || !face_no || !stabilization) {
+      GB_CHECK(n_faces <= 0, 1, "free-surface faces need face_cell, face_no and stabilization");
+      FS.clear();
+      return GB_GMG_OK;
+    }
+    gb::Level& F = H.top();
+    const int d = F.dim, nv = d == 3 ? 27 : 9, nf = d == 3 ? 9 : 3, ncu = d * nv;
+    GB_CHECK(normal_jxw || F.geom_kind != GB_GMG_GEOM_TABLE, 1,
+             "a geometry table level needs the caller's normal_jxw for free-surface faces");
+    std::vector<long> order(n_faces);
+    std::set<long> seen;
+    for (long i = 0; i < n_faces; ++i) {
+      GB_CHECK(face_cell[i] >= 0 && face_cell[i] < F.n_cells, 1, "free-surface face_cell out of range");
+      GB_CHECK(face_no[i] >= 0 && face_no[i] < 2 * d, 1, "free-surface face_no out of range");
+      GB_CHECK(seen.insert((long)face_cell[i] * 6 + face_no[i]).second, 1, "free-surface face listed twice");
+      order[i] = i;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](long a, long b) {
+      return F.internal_of_cell[face_cell[a]] < F.internal_of_cell[face_cell[b]];
+    });
+    // constraint-line ids as the level's device tables number them (lines with
+    // entries); indexed levels keep the caller's numbering (perm_u is the identity)
+    std::vector<int> lid;
+    if (!F.structured) {
+      lid.assign(F.n_u, -1);
+      int next = 0;
+      for (long gd = 0; gd < F.n_u; ++gd)
+        if (F.cu.constrained((int)gd) && F.cu.n_entries((int)gd) > 0) lid[gd] = next++;
+    }
+    std::vector<int> gptr{0}, gcell, fno(n_faces), codes((size_t)n_faces * d * nf), raw(codes.size());
+    std::vector<double> tab((size_t)n_faces * nf * 2 * d);
+    std::vector<double> nj(nf * d);
+    for (long j = 0; j < n_faces; ++j) {
+      const long i = order[j];
+      const long cc = face_cell[i], ic = F.internal_of_cell[cc];
+      if (gcell.empty() || gcell.back() != ic) {
+        if (!gcell.empty()) gptr.push_back((int)j);
+        gcell.push_back((int)ic);
+      }
+      const int fn = face_no[i], dn = fn >> 1, side = fn & 1;
+      const int ta = dn == 0 ? 1 : 0, tb = d == 3 ? (dn == 2 ? 1 : 2) : 0;
+      const int st[3] = {1, 3, 9};
+      fno[j] = fn;
+      for (int c = 0; c < d; ++c)
+        for (int k = 0; k < nf; ++k) {
+          const int l = 2 * side * st[dn] + (k % 3) * st[ta] + (d == 3 ? (k / 3) * st[tb] : 0);
+          const int gd = F.cdu[(size_t)cc * ncu + c * nv + l];
+          const int in = F.perm_u.empty() ? gd : F.perm_u[gd];
+          int code = in;
+          if (F.cu.constrained(gd)) code = F.structured || lid[gd] < 0 ? -1 : -(lid[gd] + 2);
+          codes[((size_t)j * d + c) * nf + k] = code;
+          raw[((size_t)j * d + c) * nf + k] = in;
+        }
+      if (normal_jxw) {
+        for (int q = 0; q < nf * d; ++q) nj[q] = normal_jxw[(size_t)i * nf * d + q];
+      } else {
+        const size_t per = F.geom_kind == GB_GMG_GEOM_BOX ? 2 * d : (size_t)nv * d;
+        gb::face_normal_jxw(d, F.geom_kind, &F.geom[(size_t)cc * per], fn, nj.data());
+      }
+      for (int q = 0; q < nf; ++q)
+        for (int e = 0; e < d; ++e) {
+          const double t = stabilization[((size_t)i * nf + q) * d + e], n = nj[q * d + e];
+          GB_CHECK(std::isfinite(t) && std::isfinite(n), GB_GMG_NAN_DETECTED, "non-finite free-surface table entry");
+          tab[((size_t)j * nf + q) * 2 * d + e] = t;
+          tab[((size_t)j * nf + q) * 2 * d + d + e] = n;
+        }
+    }
+    gptr.push_back((int)n_faces);
+    FS.clear();
+    FS.gptr.upload(gptr);
+    FS.gcell.upload(gcell);
+    FS.fno.upload(fno);
+    FS.codes.upload(codes);
+    FS.raw.upload(raw);
+    FS.t64.upload(tab);
+    FS.t32.upload(std::vector<float>(tab.begin(), tab.end()));
+    FS.n_groups = (int)gcell.size();
+    FS.n_faces = n_faces;
+  })
+}
+
 int gb_gmg_build_preconditioner(gb_gmg* g) {
   if (!g) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
@@ -1727,6 +1850,10 @@ int gb_gmg_correct_stokes_rhs(gb_gmg* g, const double* u0, double* rhs) {
     plain.cdp = F.cdp_raw_d.p;
     gb::launch_cell_pass<double>(plain, gb::OPK_STOKES, b, b + nu, D.Eu.p, D.Ep.p, H.st);
     ++H.cell_launches;
+    if (H.free_surface.on()) {  // the face term of K u0, plain reads (the reference's :709-746)
+      gb::launch_free_surface<double>(plain, H.free_surface.view<double>(true), b, D.Eu.p, false, H.st);
+      ++H.cell_launches;
+    }
     for (int block = 0; block < 2; ++block) {
       gb::GatherArgs<double> ga{};
       ga.E = block == 0 ? D.Eu.p : D.Ep.p;

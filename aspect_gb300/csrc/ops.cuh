@@ -46,6 +46,28 @@ template <typename T>
 void launch_newton_stokes(const LevelView<T>& L, const NewtonView<T>& N, const T* su, const T* sp, T* Eu, T* Ep,
                           bool slot_major, cudaStream_t s);
 
+// Free-surface faces of the finest level (free_surface.cu), grouped by internal
+// cell: the faces of cell gcell[g] are gptr[g] .. gptr[g+1]-1; per face its
+// number 2*d + side, the constraint codes of its 3^(dim-1) nodes per component
+// ([face][comp][node], first tangential axis fastest) and per point the
+// stabilisation vector T and the outward normal times JxW ([face][point][2*dim]).
+template <typename T>
+struct FreeSurfaceView {
+  int n_groups;
+  const int* gptr;
+  const int* gcell;
+  const int* fno;
+  const int* codes;
+  const T* tab;
+};
+// adds the face terms of src to the per-cell velocity contributions E (before the gather)
+template <typename T>
+void launch_free_surface(const LevelView<T>& L, const FreeSurfaceView<T>& F, const T* src, T* E, bool slot_major,
+                         cudaStream_t s);
+// host: outward normal x surface JxW at the face's QGauss(3) points ([point][dim]);
+// geom_kind 0: cell_geom = (x0[dim], h[dim]), 1: the 3^dim Q2 support points
+void face_normal_jxw(int dim, int geom_kind, const double* cell_geom, int fno, double* out);
+
 // Fused FP32 A-block operator of large 3D lattice levels (ablock_fused.cu):
 // cell layers per tile for a level (0: the level does not qualify), the face
 // buffer it needs (floats), the one-time kernel attribute set-up (call outside

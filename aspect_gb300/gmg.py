@@ -88,7 +88,7 @@ EXPORTS = ["gb_gmg_default_options", "gb_gmg_default_solve_params", "gb_gmg_crea
            "gb_gmg_solve", "gb_gmg_solve_device", "gb_gmg_adjoint_gradient", "gb_gmg_memory_consumption",
            "gb_gmg_kernel_launches", "gb_gmg_time_operation", "gb_gmg_ablock_apply_lattice_noalloc",
            "gb_gmg_update_viscosity", "gb_gmg_correct_stokes_rhs", "gb_gmg_set_newton_terms",
-           "gb_gmg_assemble_rhs"]
+           "gb_gmg_assemble_rhs", "gb_gmg_set_free_surface"]
 
 TIME_STOKES_VMULT, TIME_A_VMULT, TIME_MASS_VMULT = 0, 1, 2
 TIME_STOKES_PRECONDITIONER, TIME_A_PRECONDITIONER, TIME_S_PRECONDITIONER = 3, 4, 5
@@ -129,6 +129,7 @@ def load_library(path: str = LIB_PATH):
     L.gb_gmg_vmult.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp]
     L.gb_gmg_correct_stokes_rhs.argtypes = [vp, dp, dp]
     L.gb_gmg_assemble_rhs.argtypes = [vp, dp, dp]
+    L.gb_gmg_set_free_surface.argtypes = [vp, ctypes.c_int64, vp, vp, vp, vp]
     L.gb_gmg_vmult_device.argtypes = [vp, ctypes.c_int, ctypes.c_int, dp, dp]
     L.gb_gmg_get_diagonal_inverse.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
     L.gb_gmg_get_eigenvalues.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
@@ -251,6 +252,22 @@ class StokesMatrixFreeGPU:
         t = NewtonTerms(int(newton), int(symmetrize), int(average), int(dilation),
                         *[None if a is None else a.ctypes.data for a in arrs])
         self._chk(self.L.gb_gmg_set_newton_terms(self.h, ctypes.byref(t)))
+
+    def set_free_surface(self, face_cell=None, face_no=None, stabilization=None, normal_jxw=None):
+        """Free-surface stabilisation faces of the outer Stokes operator
+        (StokesOperator::local_apply_boundary_face): face_cell / face_no per face,
+        stabilization (n_faces, 3**(dim-1), dim) = rho dt theta |g| g_hat at the
+        face points, normal_jxw the same shape or None (from the level geometry).
+        No arguments: the term is removed."""
+        if face_cell is None or len(face_cell) == 0:
+            self._chk(self.L.gb_gmg_set_free_surface(self.h, 0, None, None, None, None))
+            return
+        fc = np.ascontiguousarray(face_cell, dtype=np.int32)
+        fn = np.ascontiguousarray(face_no, dtype=np.int32)
+        st = _d(stabilization)
+        nj = None if normal_jxw is None else _d(normal_jxw)
+        self._chk(self.L.gb_gmg_set_free_surface(self.h, len(fc), _p(fc), _p(fn), _p(st),
+                                                 None if nj is None else _p(nj)))
 
     def build_preconditioner(self):
         self._chk(self.L.gb_gmg_build_preconditioner(self.h))

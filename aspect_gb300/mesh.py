@@ -146,6 +146,67 @@ class LevelMesh:
         return np.einsum("qne,cnd->cqde", dphi, X)
 
 
+def face_reference_points(dim: int, face_no: int) -> tuple[np.ndarray, np.ndarray]:
+    """QGauss(3) points of a cell face in reference coordinates, (3**(dim-1), dim),
+    and their weights: face_no = 2*d + side (xi_d = side); the two tangential axes
+    in increasing order, the lower fastest (the C ABI's free-surface point order)."""
+    from . import fe
+    d, side = divmod(face_no, 2)
+    tang = [a for a in range(dim) if a != d]
+    g, w = fe.gauss(3)
+    pts = np.zeros((3 ** (dim - 1), dim))
+    wts = np.ones(3 ** (dim - 1))
+    for q in range(3 ** (dim - 1)):
+        for m, a in enumerate(tang):
+            i = (q // 3 ** m) % 3
+            pts[q, a] = g[i]
+            wts[q] *= w[i]
+        pts[q, d] = side
+    return pts, wts
+
+
+def face_normal_jxw(level: "LevelMesh", face_cell: np.ndarray, face_no: np.ndarray) -> np.ndarray:
+    """Outward unit normal times surface JxW at the face points (n_faces, 3**(dim-1), dim),
+    from the level's box or Q2 geometry (cross product of the tangential Jacobian columns)."""
+    dim = level.dim
+    out = np.zeros((len(face_cell), 3 ** (dim - 1), dim))
+    for fno in range(2 * dim):
+        sel = np.nonzero(np.asarray(face_no) == fno)[0]
+        if len(sel) == 0:
+            continue
+        pts, wts = face_reference_points(dim, fno)
+        J = level.jacobians(pts)[np.asarray(face_cell)[sel]]  # (nf, nq, dim x, dim xi)
+        d, side = divmod(fno, 2)
+        tang = [a for a in range(dim) if a != d]
+        if dim == 3:
+            N = np.cross(J[..., tang[0]], J[..., tang[1]])
+        else:
+            t = J[..., tang[0]]
+            N = np.stack([t[..., 1], -t[..., 0]], axis=-1)
+        dn = np.einsum("fqi,fqi->fq", N, J[..., d])
+        sgn = np.where((dn >= 0) == (side == 1), 1.0, -1.0)
+        out[sel] = N * (sgn * wts[None, :])[..., None]
+    return out
+
+
+def boundary_faces(level: "LevelMesh", on_surface) -> tuple[np.ndarray, np.ndarray]:
+    """(face_cell, face_no) of the cell faces whose centre x satisfies on_surface(x)
+    (a vectorised predicate on (n, dim) points), in cell order."""
+    dim = level.dim
+    cells, nos = [], []
+    for fno in range(2 * dim):
+        d, side = divmod(fno, 2)
+        c = np.full((1, dim), 0.5)
+        c[0, d] = side
+        x = level.map_points(c)[:, 0, :]
+        hit = np.nonzero(on_surface(x))[0]
+        cells.append(hit)
+        nos.append(np.full(len(hit), fno))
+    fc, fn = np.concatenate(cells), np.concatenate(nos)
+    order = np.lexsort((fn, fc))
+    return fc[order].astype(np.int32), fn[order].astype(np.int32)
+
+
 def _lex(idx: tuple, shape: tuple) -> int:
     out, stride = 0, 1
     for i, n in zip(idx, shape):
@@ -155,7 +216,7 @@ def _lex(idx: tuple, shape: tuple) -> int:
 
 
 def box_level(dim: int, ncells: tuple, extent: tuple, origin: tuple | None = None,
-              free_slip: bool = True, no_slip: bool = False) -> LevelMesh:
+              free_slip: bool = True, no_slip: bool = False, open_faces: tuple = ()) -> LevelMesh:
     """Uniform axis-aligned box with lexicographic cells, component-blocked
     Q2 velocity numbering and lexicographic Q1 pressure numbering.
 
@@ -163,7 +224,8 @@ def box_level(dim: int, ncells: tuple, extent: tuple, origin: tuple | None = Non
     Dirichlet-zero line), as ``Tangential velocity boundary indicators`` gives
     on a box (VectorTools::compute_no_normal_flux_constraints on axis-aligned
     faces). ``no_slip``: every component is zero on every face, as ``Zero
-    velocity boundary indicators`` on all faces gives."""
+    velocity boundary indicators`` on all faces gives. ``open_faces``: face
+    numbers 2*d + side left without constraints (e.g. a free surface)."""
     origin = origin or (0.0,) * dim
     ncells = tuple(ncells)
     h = tuple(extent[d] / ncells[d] for d in range(dim))
@@ -200,16 +262,23 @@ def box_level(dim: int, ncells: tuple, extent: tuple, origin: tuple | None = Non
     pts_p = np.array([origin[d] + pidx[:, d] * h[d] for d in range(dim)]).T
 
     lines = {}
+    def face_nodes(d, side):
+        return nidx[:, d] == (nn[d] - 1 if side else 0)
+
+    closed = [f for f in range(2 * dim) if f not in tuple(open_faces)]
     if no_slip:
         on_bnd = np.zeros(n_nodes, bool)
-        for d in range(dim):
-            on_bnd |= (nidx[:, d] == 0) | (nidx[:, d] == nn[d] - 1)
+        for f in closed:
+            on_bnd |= face_nodes(f // 2, f % 2)
         for c in range(dim):
             for nd in np.nonzero(on_bnd)[0]:
                 lines[int(nd + c * n_nodes)] = ([], 0.0)
     elif free_slip:
         for c in range(dim):
-            on_face = (nidx[:, c] == 0) | (nidx[:, c] == nn[c] - 1)
+            on_face = np.zeros(n_nodes, bool)
+            for f in closed:
+                if f // 2 == c:
+                    on_face |= face_nodes(c, f % 2)
             for nd in np.nonzero(on_face)[0]:
                 lines[int(nd + c * n_nodes)] = ([], 0.0)
     cu = Constraints.from_dict(lines)
@@ -223,14 +292,15 @@ def box_level(dim: int, ncells: tuple, extent: tuple, origin: tuple | None = Non
 
 
 def box_hierarchy(dim: int, n_fine: int, extent=None, n_coarse: int = 1,
-                  free_slip: bool = True, no_slip: bool = False) -> list[LevelMesh]:
+                  free_slip: bool = True, no_slip: bool = False, open_faces: tuple = ()) -> list[LevelMesh]:
     """Global-coarsening hierarchy of uniform boxes: level l has n_coarse*2**l
     cells per direction, up to n_fine on the finest level."""
     extent = tuple(extent or (1.0,) * dim)
     levels = []
     n = n_coarse
     while n <= n_fine:
-        levels.append(box_level(dim, (n,) * dim, extent, free_slip=free_slip, no_slip=no_slip))
+        levels.append(box_level(dim, (n,) * dim, extent, free_slip=free_slip, no_slip=no_slip,
+                                open_faces=open_faces))
         n *= 2
     assert levels and n // 2 == n_fine, "n_fine must be n_coarse * 2**k"
     for l in range(1, len(levels)):

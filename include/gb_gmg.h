@@ -253,6 +253,27 @@ int gb_gmg_vmult(gb_gmg* h, int op, int level, int precision, const double* src,
    the constraints) afterwards, as the reference does. */
 int gb_gmg_correct_stokes_rhs(gb_gmg* h, const double* u0, double* rhs);
 
+/* Free-surface stabilisation of the outer Stokes operator
+ * (StokesOperator::local_apply_boundary_face, source/simulator/solver/
+ * matrix_free_operators.cc:563-602; table of stokes_matrix_free_local_smoothing.cc:
+ * 520-612): on each listed boundary face F of the finest level
+ *     dst_u(phi) += int_F -(T . u) (n . phi) dS,   T = rho dt theta |g| g_hat,
+ * at the face's QGauss(3) points. Applied by the finest level's outer Stokes
+ * operator (FGMRES products, gb_gmg_vmult of GB_GMG_OP_STOKES on the finest level)
+ * and by gb_gmg_correct_stokes_rhs; not by the multigrid levels or the A block,
+ * as in the reference.
+ *   face_cell[i]: caller cell index; face_no[i] = 2*d + side (side 0: xi_d = 0),
+ *   at most once per (cell, face).
+ *   Points: 3^(dim-1) per face, lexicographic in the face's two tangential
+ *   reference axes taken in increasing axis order, the lower axis fastest.
+ *   stabilization: [n_faces][points][dim], T at the points;
+ *   normal_jxw: [n_faces][points][dim], outward unit normal times the surface
+ *   JxW, or NULL: computed from the level's geometry (GB_GMG_GEOM_BOX and
+ *   GB_GMG_GEOM_Q2; a GB_GMG_GEOM_TABLE level needs it).
+ * n_faces = 0 removes the term. finalize_setup clears it. */
+int gb_gmg_set_free_surface(gb_gmg* h, int64_t n_faces, const int32_t* face_cell, const int32_t* face_no,
+                            const double* stabilization, const double* normal_jxw);
+
 /* The body-force right-hand side of the finest level on the device
  * (source/simulator/assemblers/stokes.cc:285-400, the rho g . phi_u term):
  * rhs_u = int f . phi_u over QGauss(3), condensed with the velocity constraints

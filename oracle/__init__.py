@@ -45,7 +45,7 @@ def lib():
                      "orc_build_preconditioner", "orc_vmult", "orc_get_diagonal", "orc_transfer",
                      "orc_estimate_eigenvalues", "orc_get_eigenvalues", "orc_set_eigenvalues",
                      "orc_vcycle", "orc_block_preconditioner", "orc_solve", "orc_adjoint_gradient",
-                     "orc_set_fast", "orc_set_newton"]:
+                     "orc_set_fast", "orc_set_newton", "orc_set_free_surface"]:
             getattr(L, name).restype = ctypes.c_int
         _lib = L
     return _lib
@@ -184,6 +184,22 @@ class Oracle:
         arrs = [None if a is None else _d(a) for a in (strain_rate, d_eta_d_strain_rate, d_eta_d_pressure,
                                                           dilation_lhs, d_dilation_d_strain_rate, d_dilation_d_pressure)]
         self._chk(self.L.orc_set_newton(self.h, flags, *[None if a is None else _ptr(a, _dp) for a in arrs]))
+
+    def set_free_surface(self, face_cell=None, face_no=None, stabilization=None, normal_jxw=None):
+        """Free-surface faces of the outer Stokes operator (finest level): T per
+        face point (n_faces, 3**(dim-1), dim) and the outward normal times JxW
+        (same shape; None: from the level geometry by the harness). No arguments:
+        the term is removed."""
+        if face_cell is None or len(face_cell) == 0:
+            self._chk(self.L.orc_set_free_surface(self.h, 0, None, None, None))
+            return
+        from aspect_gb300 import mesh
+        fc = np.ascontiguousarray(face_cell, dtype=np.int32)
+        fn = np.ascontiguousarray(face_no, dtype=np.int32)
+        nj = mesh.face_normal_jxw(self.fine, fc, fn) if normal_jxw is None else _d(normal_jxw)
+        tab = _d(np.concatenate([_d(stabilization), _d(nj)], axis=-1))
+        self._chk(self.L.orc_set_free_surface(self.h, len(fc), _ptr(fc, ctypes.POINTER(ctypes.c_int)),
+                                              _ptr(fn, ctypes.POINTER(ctypes.c_int)), _ptr(tab, _dp)))
 
     def adjoint_gradient(self, u, lam) -> np.ndarray:
         u, lam = _d(u), _d(lam)

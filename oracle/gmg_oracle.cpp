@@ -683,13 +683,67 @@ struct Oracle {
   // Newton / prescribed-dilation tables of the outer operators (finest level)
   NewtonTerms newton;
   const NewtonTerms* apply_nt = nullptr;  // set while an outer operator is applied
-  struct OuterTerms {  // makes apply() add the Newton / dilation terms for one call
+  // free-surface stabilisation faces of the outer Stokes operator (finest level):
+  // caller cell, face number 2*d + side, per face point T then n JxW (2*dim values)
+  struct FreeSurface {
+    std::vector<int> cell, fno;
+    std::vector<double> tab;
+  } fs;
+  bool apply_fs = false;
+  struct OuterTerms {  // makes apply() add the Newton / dilation / face terms for one call
     Oracle& o;
     explicit OuterTerms(Oracle& o_) : o(o_) {
       if (o.newton.newton || o.newton.dilation) o.apply_nt = &o.newton;
+      o.apply_fs = !o.fs.cell.empty();
     }
-    ~OuterTerms() { o.apply_nt = nullptr; }
+    ~OuterTerms() {
+      o.apply_nt = nullptr;
+      o.apply_fs = false;
+    }
   };
+
+  // Free-surface face term (StokesOperator::local_apply_boundary_face,
+  // matrix_free_operators.cc:563-602): dst_u(phi) += sum_q -(T_q . u(x_q)) (n JxW)_q . phi(x_q)
+  // over each face's QGauss(3) points, u read and the result distributed through
+  // the constraints; plain basis evaluation at the face points.
+  template <class T>
+  void face_terms(const Level& L, const T* src_u, T* dst_u, bool plain = false) {
+    const int d = dim, nv = fe.nv, nf = d == 3 ? 9 : 3;
+    const double gp[3] = {0.5 - std::sqrt(15.0) / 10, 0.5, 0.5 + std::sqrt(15.0) / 10};
+    for (size_t f = 0; f < fs.cell.size(); ++f) {
+      const int c = fs.cell[f], dn = fs.fno[f] >> 1, side = fs.fno[f] & 1;
+      int tang[2], m = 0;
+      for (int a = 0; a < d; ++a)
+        if (a != dn) tang[m++] = a;
+      T xu[81] = {0}, yu[81] = {0};
+      for (int i = 0; i < d * nv; ++i) {
+        const int gd = L.cdu[(size_t)c * d * nv + i];
+        if (plain) { xu[i] = src_u[gd]; continue; }
+        Expansion e = expand(L.cu, gd);
+        for (int k = 0; k < e.n; ++k) xu[i] += (T)e.w[k] * src_u[e.g[k]];
+      }
+      for (int q = 0; q < nf; ++q) {
+        double xi[3] = {0, 0, 0};
+        xi[dn] = side;
+        xi[tang[0]] = gp[q % 3];
+        if (d == 3) xi[tang[1]] = gp[q / 3];
+        double phi[27];
+        q2_basis_at(d, xi, phi);
+        const double* t = &fs.tab[(f * nf + q) * 2 * d];
+        T uq[3] = {0, 0, 0};
+        for (int a = 0; a < d; ++a)
+          for (int n = 0; n < nv; ++n) uq[a] += (T)phi[n] * xu[a * nv + n];
+        T tu = 0;
+        for (int a = 0; a < d; ++a) tu += (T)t[a] * uq[a];
+        for (int a = 0; a < d; ++a)
+          for (int n = 0; n < nv; ++n) yu[a * nv + n] += (T)phi[n] * (-tu * (T)t[d + a]);
+      }
+      for (int i = 0; i < d * nv; ++i) {
+        Expansion e = expand(L.cu, L.cdu[(size_t)c * d * nv + i]);
+        for (int k = 0; k < e.n; ++k) dst_u[e.g[k]] += (T)e.w[k] * yu[i];
+      }
+    }
+  }
 
   Level& fine() { return levels.back(); }
 
@@ -736,6 +790,7 @@ struct Oracle {
           }
       }
     }
+    if (apply_fs && op == OP_STOKES && lev == (int)levels.size() - 1) face_terms<T>(L, src_u, dst_u);
     // identity on constrained rows (Base::vmult: dst = src there)
     if (op == OP_BT) {
       for (int g = 0; g < L.n_u; ++g)
@@ -1668,6 +1723,21 @@ int orc_set_newton(void* p, int flags, const double* E, const double* D, const d
         t.DD.assign(DD, DD + nq * ns);
         t.dpd.assign(dpd, dpd + nq);
       }
+    }
+  })
+}
+
+// Free-surface faces of the finest level's outer Stokes operator: caller cell,
+// face number 2*d + side, per face point T[dim] then n JxW[dim]. n = 0 removes them.
+int orc_set_free_surface(void* p, int n, const int* cell, const int* fno, const double* tab) {
+  Oracle* h = (Oracle*)p;
+  GUARD({
+    const int nf = h->dim == 3 ? 9 : 3;
+    h->fs = orc::Oracle::FreeSurface{};
+    if (n > 0) {
+      h->fs.cell.assign(cell, cell + n);
+      h->fs.fno.assign(fno, fno + n);
+      h->fs.tab.assign(tab, tab + (size_t)n * nf * 2 * h->dim);
     }
   })
 }

@@ -71,3 +71,22 @@ def constrained_operator(K, C_row, C_col, mask_row=None, identity=True):
         R[:, mask_row] = 0.0
         R[mask_row, mask_row] = 1.0
     return R
+
+
+def free_surface_matrix(level, face_cell, face_no, stab, normal_jxw):
+    """Dense velocity matrix (caller numbering, no constraints) of the free-surface
+    face term: K[i, j] = sum_faces sum_q -(T_q . phi_j(x_q)) (nJxW_q . phi_i(x_q))."""
+    from aspect_gb300 import mesh
+    dim = level.dim
+    nv = 3 ** dim
+    K = np.zeros((level.n_u, level.n_u))
+    for f, (c, fno) in enumerate(zip(face_cell, face_no)):
+        pts, _ = mesh.face_reference_points(dim, int(fno))
+        phi = fe.shape_values(dim, fe.Q2_NODES, pts)  # (nq, nv)
+        dofs = level.cell_dofs_u[c].reshape(dim, nv)
+        for q in range(len(pts)):
+            for a in range(dim):
+                for b in range(dim):
+                    coef = -stab[f, q, b] * normal_jxw[f, q, a]
+                    K[np.ix_(dofs[a], dofs[b])] += coef * np.outer(phi[q], phi[q])
+    return K

@@ -52,6 +52,9 @@ def test_null_handle_is_rejected_by_every_entry_point(L):
     assert L.gb_gmg_finalize_setup(None) == INVALID
     assert L.gb_gmg_build_preconditioner(None) == INVALID
     assert L.gb_gmg_set_viscosity(None, p, 1, 0, 1.0, 0) == INVALID
+    assert L.gb_gmg_set_newton_terms(None, None) == INVALID
+    assert L.gb_gmg_set_free_surface(None, 0, None, None, None, None) == INVALID
+    assert L.gb_gmg_assemble_rhs(None, p, p) == INVALID
     L.gb_gmg_destroy(None)  # a no-op
 
 
