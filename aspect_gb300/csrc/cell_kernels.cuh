@@ -31,6 +31,7 @@ enum GeomKind { GEOM_CART = 0, GEOM_BOX = 1, GEOM_TABLE = 2 };
 template <typename T>
 struct LevelView {
   int dim;
+  int deg;        // velocity degree: 2 (Q2-Q1) or 3 (Q3-Q2, general levels only)
   int n_cells, n_u, n_p;
   int structured;
   // structured box levels (internal lexicographic numbering, components blocked)

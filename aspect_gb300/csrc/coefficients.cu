@@ -30,18 +30,29 @@ namespace {
 
 constexpr int kCoefThreads = 128;
 
-template <int dim>
+// Gauss points of QGauss(4) on [0, 1]: (1 -+ sqrt(3/7 +- 2/7 sqrt(6/5))) / 2
+__device__ __forceinline__ double gauss4(int i) {
+  return i == 0 ? 0.069431844202973712388 : i == 1 ? 0.33000947820757186760
+       : i == 2 ? 0.66999052179242813240 : 0.93056815579702628761;
+}
+// Q1 basis {1 - x, x} at 1D Gauss point i of NQ1 points
+template <int NQ1>
+__device__ __forceinline__ double p1(int i, int n) {
+  if constexpr (NQ1 == 3) return fe::P1v(i, n);
+  else return n ? gauss4(i) : 1.0 - gauss4(i);
+}
+template <int dim, int NQ1 = 3>
 __device__ __forceinline__ double psi1(int q, int n) {
   // Q1 basis n at Gauss point q (lexicographic digits)
-  double v = fe::P1v(q % 3, n & 1) * fe::P1v((q / 3) % 3, (n >> 1) & 1);
-  if (dim == 3) v *= fe::P1v(q / 9, (n >> 2) & 1);
+  double v = p1<NQ1>(q % NQ1, n & 1) * p1<NQ1>((q / NQ1) % NQ1, (n >> 1) & 1);
+  if (dim == 3) v *= p1<NQ1>(q / (NQ1 * NQ1), (n >> 2) & 1);
   return v;
 }
 
-template <int dim>
+template <int dim, int NQ1>
 __global__ void k_dgq0_finest(long n_cells, int n_per_cell, const double* __restrict__ eta_in,
                               const double* __restrict__ jxw, double* __restrict__ dg) {
-  constexpr int nq = fe::pow3(dim);
+  constexpr int nq = NQ1 * NQ1 * (dim == 3 ? NQ1 : 1);
   const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (c >= n_cells) return;
   if (n_per_cell == 1) {
@@ -69,10 +80,10 @@ __global__ void k_dgq0_restrict(long n_coarse, const int* __restrict__ ptr, cons
   coarse[p] = sum / cnt;
 }
 
-template <int dim>
+template <int dim, int NQ1>
 __global__ void k_dgq1_finest(long n_cells, const double* __restrict__ eta_in, const double* __restrict__ jxw,
                               double* __restrict__ dg) {
-  constexpr int nq = fe::pow3(dim), ncv = fe::pow2(dim);
+  constexpr int nq = NQ1 * NQ1 * (dim == 3 ? NQ1 : 1), ncv = fe::pow2(dim);
   const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (c >= n_cells) return;
   double M[ncv][ncv], b[ncv], x[ncv];
@@ -83,8 +94,8 @@ __global__ void k_dgq1_finest(long n_cells, const double* __restrict__ eta_in, c
   for (int q = 0; q < nq; ++q) {
     const double jw = jxw[c * nq + q];
     for (int i = 0; i < ncv; ++i) {
-      b[i] += jw * psi1<dim>(q, i) * eta_in[c * nq + q];
-      for (int j = 0; j < ncv; ++j) M[i][j] += jw * psi1<dim>(q, i) * psi1<dim>(q, j);
+      b[i] += jw * psi1<dim, NQ1>(q, i) * eta_in[c * nq + q];
+      for (int j = 0; j < ncv; ++j) M[i][j] += jw * psi1<dim, NQ1>(q, i) * psi1<dim, NQ1>(q, j);
     }
   }
   for (int i = 0; i < ncv; ++i)
@@ -121,11 +132,11 @@ __global__ void k_dgq1_restrict(long n_coarse, int ncv, const int* __restrict__ 
 // a level's table in internal cell order, FP64 and FP32: mode 0 = one value per
 // cell (dg), 1 = the caller's per-point values, 2 = the Q1 interpolation of dg
 // clamped to [lo, hi]
-template <int dim>
+template <int dim, int NQ1>
 __global__ void k_level_table(long n_cells, int mode, const int* __restrict__ ioc, const double* __restrict__ dg,
                               const double* __restrict__ eta_in, double lo, double hi, double* __restrict__ t64,
                               float* __restrict__ t32) {
-  constexpr int nq = fe::pow3(dim), ncv = fe::pow2(dim);
+  constexpr int nq = NQ1 * NQ1 * (dim == 3 ? NQ1 : 1), ncv = fe::pow2(dim);
   const long c = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (c >= n_cells) return;
   const long ic = ioc[c];
@@ -140,7 +151,7 @@ __global__ void k_level_table(long n_cells, int mode, const int* __restrict__ io
       v = eta_in[c * nq + q];
     } else {
       v = 0;
-      for (int i = 0; i < ncv; ++i) v += psi1<dim>(q, i) * dg[c * ncv + i];
+      for (int i = 0; i < ncv; ++i) v += psi1<dim, NQ1>(q, i) * dg[c * ncv + i];
       v = fmin(fmax(v, lo), hi);
     }
     t64[ic * nq + q] = v;
@@ -201,6 +212,15 @@ __global__ void __launch_bounds__(128) k_body_force(LevelView<double> L, const d
 
 int grid(long n) { return (int)((n + kCoefThreads - 1) / kCoefThreads); }
 
+// calls f(dim, points per direction) with both as compile-time constants
+template <class F>
+void dispatch_dq(int dim, int n1, F&& f) {
+  if (dim == 3 && n1 == 3) f(std::integral_constant<int, 3>{}, std::integral_constant<int, 3>{});
+  else if (dim == 3) f(std::integral_constant<int, 3>{}, std::integral_constant<int, 4>{});
+  else if (n1 == 3) f(std::integral_constant<int, 2>{}, std::integral_constant<int, 3>{});
+  else f(std::integral_constant<int, 2>{}, std::integral_constant<int, 4>{});
+}
+
 // Q2 basis on nodes {0, 1/2, 1}: values and derivatives at x
 void q2_basis(double x, double* v, double* dv) {
   v[0] = 2.0 * (x - 0.5) * (x - 1.0);
@@ -219,7 +239,7 @@ void q2_basis(double x, double* v, double* dv) {
 void setup_coefficient_maps(std::vector<Level>& levels) {
   const int nlev = (int)levels.size();
   Level& Fl = levels.back();
-  const int d = Fl.dim, nq = d == 3 ? 27 : 9;
+  const int d = Fl.dim, nq = Fl.nq();
   for (int l = 0; l < nlev; ++l) {
     Level& L = levels[l];
     L.ioc_d.upload(L.internal_of_cell);
@@ -234,17 +254,17 @@ void setup_coefficient_maps(std::vector<Level>& levels) {
     L.kid_d.upload(kids);
     L.child_d.upload(L.child);
   }
-  // finest JxW per point, from the caller's geometry
-  const double g3[3] = {0.5 - std::sqrt(15.0) / 10, 0.5, 0.5 + std::sqrt(15.0) / 10};
-  const double w3[3] = {5.0 / 18, 8.0 / 18, 5.0 / 18};
-  double v1[3][3], d1[3][3];
-  for (int q = 0; q < 3; ++q) q2_basis(g3[q], v1[q], d1[q]);
+  // finest JxW per point (QGauss(degree+1)), from the caller's geometry
+  const Basis1D B = basis1d(Fl.degree);
+  const int n1 = B.nq1, nm = ipow(3, d);  // points per direction, Q2 mapping support points
+  double v1[4][3], d1[4][3];
+  for (int q = 0; q < n1; ++q) q2_basis(B.gq[q], v1[q], d1[q]);
   std::vector<double> jxw((size_t)Fl.n_cells * nq);
   for (long c = 0; c < Fl.n_cells; ++c)
     for (int q = 0; q < nq; ++q) {
-      const int qi[3] = {q % 3, (q / 3) % 3, q / 9};
+      const int qi[3] = {q % n1, (q / n1) % n1, q / (n1 * n1)};
       double w = 1;
-      for (int e = 0; e < d; ++e) w *= w3[qi[e]];
+      for (int e = 0; e < d; ++e) w *= B.gw[qi[e]];
       double det;
       if (Fl.geom_kind == 0) {
         det = 1;
@@ -253,8 +273,8 @@ void setup_coefficient_maps(std::vector<Level>& levels) {
         det = Fl.geom[((size_t)c * nq + q) * (d * d + 1) + d * d];
       } else {
         double J[3][3] = {{0}};
-        const double* X = &Fl.geom[(size_t)c * nq * d];
-        for (int n = 0; n < nq; ++n) {
+        const double* X = &Fl.geom[(size_t)c * nm * d];
+        for (int n = 0; n < nm; ++n) {
           const int ni[3] = {n % 3, (n / 3) % 3, n / 9};
           for (int b = 0; b < d; ++b) {
             double t = 1;
@@ -276,7 +296,7 @@ void device_level_viscosity(std::vector<Level>& levels, const double* eta_in, in
                             double s, double& eta_min, double& eta_max, cudaStream_t st) {
   const int nlev = (int)levels.size();
   Level& Fl = levels.back();
-  const int d = Fl.dim, nq = d == 3 ? 27 : 9, ncv = d == 3 ? 8 : 4;
+  const int d = Fl.dim, nq = Fl.nq(), ncv = d == 3 ? 8 : 4, n1 = Fl.degree + 1;
   GB_CHECK(projection >= 0 && projection <= 2, 1, "unknown viscosity projection");
   GB_CHECK(projection == 0 || n_per_cell == nq, 1,
            "projection to Q1 and no averaging need one value per quadrature point");
@@ -294,8 +314,10 @@ void device_level_viscosity(std::vector<Level>& levels, const double* eta_in, in
   const int per = projection == 1 ? ncv : 1;
   for (auto& L : levels) L.dg_d.alloc((size_t)L.n_cells * per);
   if (projection == 1) {
-    if (d == 3) k_dgq1_finest<3><<<grid(Fl.n_cells), kCoefThreads, 0, st>>>(Fl.n_cells, ein, Fl.jxw_d.p, Fl.dg_d.p);
-    else k_dgq1_finest<2><<<grid(Fl.n_cells), kCoefThreads, 0, st>>>(Fl.n_cells, ein, Fl.jxw_d.p, Fl.dg_d.p);
+    dispatch_dq(d, n1, [&](auto dc, auto nc) {
+      k_dgq1_finest<decltype(dc)::value, decltype(nc)::value>
+          <<<grid(Fl.n_cells), kCoefThreads, 0, st>>>(Fl.n_cells, ein, Fl.jxw_d.p, Fl.dg_d.p);
+    });
     for (int l = nlev - 1; l > 0; --l) {
       Level& C = levels[l - 1];
       k_dgq1_restrict<<<grid(C.n_cells), kCoefThreads, 0, st>>>(C.n_cells, ncv, levels[l].kid_ptr_d.p,
@@ -303,10 +325,10 @@ void device_level_viscosity(std::vector<Level>& levels, const double* eta_in, in
                                                                  levels[l].dg_d.p, C.dg_d.p);
     }
   } else {
-    if (d == 3)
-      k_dgq0_finest<3><<<grid(Fl.n_cells), kCoefThreads, 0, st>>>(Fl.n_cells, n_per_cell, ein, Fl.jxw_d.p, Fl.dg_d.p);
-    else
-      k_dgq0_finest<2><<<grid(Fl.n_cells), kCoefThreads, 0, st>>>(Fl.n_cells, n_per_cell, ein, Fl.jxw_d.p, Fl.dg_d.p);
+    dispatch_dq(d, n1, [&](auto dc, auto nc) {
+      k_dgq0_finest<decltype(dc)::value, decltype(nc)::value>
+          <<<grid(Fl.n_cells), kCoefThreads, 0, st>>>(Fl.n_cells, n_per_cell, ein, Fl.jxw_d.p, Fl.dg_d.p);
+    });
     for (int l = nlev - 1; l > 0; --l) {
       Level& C = levels[l - 1];
       k_dgq0_restrict<<<grid(C.n_cells), kCoefThreads, 0, st>>>(C.n_cells, levels[l].kid_ptr_d.p, levels[l].kid_d.p,
@@ -332,23 +354,19 @@ void device_level_viscosity(std::vector<Level>& levels, const double* eta_in, in
     const size_t n = (size_t)L.n_cells * L.eta_n;
     L.f64.eta.alloc(n);  // same size: same address, so captured V-cycles stay valid
     L.f32.eta.alloc(n);
-    if (d == 3)
-      k_level_table<3><<<grid(L.n_cells), kCoefThreads, 0, st>>>(L.n_cells, mode, L.ioc_d.p, L.dg_d.p, ein, eta_min,
-                                                                 eta_max, L.f64.eta.p, L.f32.eta.p);
-    else
-      k_level_table<2><<<grid(L.n_cells), kCoefThreads, 0, st>>>(L.n_cells, mode, L.ioc_d.p, L.dg_d.p, ein, eta_min,
-                                                                 eta_max, L.f64.eta.p, L.f32.eta.p);
+    dispatch_dq(d, n1, [&](auto dc, auto nc) {
+      k_level_table<decltype(dc)::value, decltype(nc)::value><<<grid(L.n_cells), kCoefThreads, 0, st>>>(
+          L.n_cells, mode, L.ioc_d.p, L.dg_d.p, ein, eta_min, eta_max, L.f64.eta.p, L.f32.eta.p);
+    });
     // no averaging: the outer operators' per-point table of the finest level
     L.eta_active_n = top && projection == 2 ? nq : 0;
     if (L.eta_active_n) {
       L.f64.eta_active.alloc((size_t)L.n_cells * nq);
       L.f32.eta_active.alloc((size_t)L.n_cells * nq);
-      if (d == 3)
-        k_level_table<3><<<grid(L.n_cells), kCoefThreads, 0, st>>>(L.n_cells, 1, L.ioc_d.p, nullptr, ein, 0, 0,
-                                                                   L.f64.eta_active.p, L.f32.eta_active.p);
-      else
-        k_level_table<2><<<grid(L.n_cells), kCoefThreads, 0, st>>>(L.n_cells, 1, L.ioc_d.p, nullptr, ein, 0, 0,
-                                                                   L.f64.eta_active.p, L.f32.eta_active.p);
+      dispatch_dq(d, n1, [&](auto dc, auto nc) {
+        k_level_table<decltype(dc)::value, decltype(nc)::value><<<grid(L.n_cells), kCoefThreads, 0, st>>>(
+            L.n_cells, 1, L.ioc_d.p, nullptr, ein, 0, 0, L.f64.eta_active.p, L.f32.eta_active.p);
+      });
     } else {
       L.f64.eta_active.release();
       L.f32.eta_active.release();

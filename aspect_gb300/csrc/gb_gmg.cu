@@ -38,6 +38,7 @@ void launch_adjoint_gradient_impl(const LevelView<double>& L, int colour, int be
 struct Handle {
   gb_gmg_options opt{};
   int dim = 3, n_levels = 0;
+  int degree = 2;  // velocity degree (2: Q2-Q1, 3: Q3-Q2)
   std::vector<Level> levels;
   cudaStream_t st = nullptr;
   std::string err;
@@ -184,7 +185,7 @@ double dot_host_T(Handle& H, long n, const T* a, const T* b) {
 // ---------------------------------------------------------------- operators
 template <typename T>
 void gather(Handle& H, Level& L, const LevelView<T>& v, int block, int epi, GatherArgs<T> a, int op) {
-  const int nl = block == 0 ? L.dim * (L.dim == 3 ? 27 : 9) : (L.dim == 3 ? 8 : 4);
+  const int nl = block == 0 ? L.dim * L.nv() : L.np();
   if (cell_pass_slot_major<T>(v, op)) {
     a.cs = 1;
     a.ss = L.n_cells;
@@ -383,6 +384,12 @@ void compute_diagonals(Handle& H, int lev) {
     const int cnt = L.colour_count[k];
     if (!cnt) continue;
     const int begin = L.structured ? 0 : L.colour_begin[k];
+    if (L.degree == 3) {  // Q3-Q2: the cell operators on the colour's probes
+      launch_ho_diag<T>(v, 0, begin, cnt, pu, L.probe_ptr_h[begin + cnt] - L.probe_ptr_h[begin], D.dinvA.p, H.st);
+      launch_ho_diag<T>(v, 1, begin, cnt, pp, L.pprobe_ptr_h[begin + cnt] - L.pprobe_ptr_h[begin], D.dinvM.p, H.st);
+      H.cell_launches += 2;
+      continue;
+    }
     if (!direct) {
       launch_velocity_diag<T>(v, k, begin, cnt, pu, D.dinvA.p, H.st);
       ++H.cell_launches;
@@ -1478,14 +1485,18 @@ void gb_gmg_default_solve_params(gb_gmg_solve_params* p) {
 int gb_gmg_create(const gb_gmg_options* opt, int dim, int degree_v, int n_levels, gb_gmg** out) {
   if (!out) return GB_GMG_INVALID_ARGUMENT;
   *out = nullptr;
-  if ((dim != 2 && dim != 3) || degree_v != 2 || n_levels < 1) return GB_GMG_INVALID_ARGUMENT;
+  if ((dim != 2 && dim != 3) || (degree_v != 2 && degree_v != 3) || n_levels < 1) return GB_GMG_INVALID_ARGUMENT;
   gb_gmg* g = new gb_gmg();
   if (opt) g->h.opt = *opt;
   else gb_gmg_default_options(&g->h.opt);
   g->h.dim = dim;
+  g->h.degree = degree_v;
   g->h.n_levels = n_levels;
   g->h.levels.resize(n_levels);
-  for (auto& L : g->h.levels) L.dim = dim;
+  for (auto& L : g->h.levels) {
+    L.dim = dim;
+    L.degree = degree_v;
+  }
   int dev = 0;
   if (cudaStreamCreateWithFlags(&g->h.st, cudaStreamNonBlocking) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&g->h.n_sm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
@@ -1519,7 +1530,9 @@ int gb_gmg_set_level_mesh(gb_gmg* g, int level, int64_t n_cells, const int32_t* 
     GB_CHECK(n_u < (1LL << 31) && n_p < (1LL << 31), 1, "more than 2^31 DoFs per block");
     GB_CHECK(geometry_kind >= 0 && geometry_kind <= 2, 1, "unknown geometry kind");
     gb::Level& L = H.levels[level];
-    const int nv = H.dim == 3 ? 27 : 9, np = H.dim == 3 ? 8 : 4;
+    L.dim = H.dim;
+    L.degree = H.degree;
+    const int nv = L.nv(), np = L.np(), nq = L.nq(), nm = H.dim == 3 ? 27 : 9;  // nm: Q2 mapping points
     L.n_cells = n_cells;
     L.n_u = n_u;
     L.n_p = n_p;
@@ -1529,8 +1542,8 @@ int gb_gmg_set_level_mesh(gb_gmg* g, int level, int64_t n_cells, const int32_t* 
     for (int v : L.cdp) GB_CHECK(v >= 0 && v < n_p, 1, "pressure DoF index out of range");
     L.geom_kind = geometry_kind;
     const size_t ng = geometry_kind == 0   ? (size_t)n_cells * 2 * H.dim
-                      : geometry_kind == 1 ? (size_t)n_cells * nv * H.dim
-                                           : (size_t)n_cells * nv * (H.dim * H.dim + 1);
+                      : geometry_kind == 1 ? (size_t)n_cells * nm * H.dim
+                                           : (size_t)n_cells * nq * (H.dim * H.dim + 1);
     L.geom.assign(geom, geom + ng);
     L.cu.init(n_u);
     L.cp.init(n_p);
@@ -1622,8 +1635,8 @@ int gb_gmg_set_viscosity(gb_gmg* g, const double* eta, int n_per_cell, int proje
   ABI_TRY(g, {
     Handle& H = g->h;
     GB_CHECK(H.setup_done, GB_GMG_NOT_READY, "finalize_setup has not been called");
-    const int nq = H.dim == 3 ? 27 : 9;
-    GB_CHECK(n_per_cell == 1 || n_per_cell == nq, 1, "n_per_cell must be 1 or 3^dim");
+    const int nq = H.top().nq();
+    GB_CHECK(n_per_cell == 1 || n_per_cell == nq, 1, "n_per_cell must be 1 or (degree+1)^dim");
     GB_CHECK(s > 0 && std::isfinite(s), 1, "pressure scaling must be positive");
     H.s = s;
     H.compressible = compressible;
@@ -1667,6 +1680,7 @@ int gb_gmg_set_newton_terms(gb_gmg* g, const gb_gmg_newton_terms* t) {
       N.clear();
       return GB_GMG_OK;
     }
+    GB_CHECK(H.degree == 2, 1, "Newton / dilation terms are built for velocity degree 2");
     const bool newton = t->enable_newton_derivatives != 0, dil = t->enable_prescribed_dilation != 0;
     GB_CHECK(!newton || (t->strain_rate && t->newton_factor_wrt_strain_rate && t->newton_factor_wrt_pressure), 1,
              "Newton derivatives need the strain-rate and both Newton-factor tables");
@@ -1715,6 +1729,7 @@ int gb_gmg_set_free_surface(gb_gmg* g, int64_t n_faces, const int32_t* face_cell
       FS.clear();
       return GB_GMG_OK;
     }
+    GB_CHECK(H.degree == 2, 1, "free-surface faces are built for velocity degree 2");
     gb::Level& F = H.top();
     const int d = F.dim, nv = d == 3 ? 27 : 9, nf = d == 3 ? 9 : 3, ncu = d * nv;
     GB_CHECK(normal_jxw || F.geom_kind != GB_GMG_GEOM_TABLE, 1,
@@ -1820,7 +1835,7 @@ int gb_gmg_correct_stokes_rhs(gb_gmg* g, const double* u0, double* rhs) {
     const int top = H.n_levels - 1;
     gb::Level& F = H.levels[top];
     const long nu = F.n_u, n = F.n_u + F.n_p;
-    const int nv = F.dim == 3 ? 27 : 9, npc = F.dim == 3 ? 8 : 4, ncu = F.dim * nv;
+    const int nv = F.nv(), npc = F.np(), ncu = F.dim * nv;
     if (!F.cdu_raw_d.p) {
       std::vector<int> ru((size_t)F.n_cells * ncu), rp((size_t)F.n_cells * npc);
       for (long ic = 0; ic < F.n_cells; ++ic) {
@@ -1876,6 +1891,7 @@ int gb_gmg_assemble_rhs(gb_gmg* g, const double* force, double* rhs) {
     GB_CHECK(H.setup_done, GB_GMG_NOT_READY, "finalize_setup has not been called");
     const int top = H.n_levels - 1;
     gb::Level& F = H.levels[top];
+    GB_CHECK(H.degree == 2, 1, "the device body force is built for velocity degree 2");
     const int d = F.dim, nq = d == 3 ? 27 : 9;
     const size_t per_cell = (size_t)nq * d;
     std::vector<double> f((size_t)F.n_cells * per_cell);  // internal cell order
@@ -2148,6 +2164,7 @@ int gb_gmg_adjoint_gradient(gb_gmg* g, const double* u, const double* lambda, do
   ABI_TRY(g, {
     Handle& H = g->h;
     GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
+    GB_CHECK(H.degree == 2, 1, "the adjoint gradient is built for velocity degree 2");
     const int top = H.n_levels - 1;
     gb::Level& F = H.levels[top];
     GB_CUDA(cudaMemcpyAsync(H.stage_a.p, u, F.n_u * sizeof(double), cudaMemcpyHostToDevice, H.st));

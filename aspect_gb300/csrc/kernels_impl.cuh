@@ -65,6 +65,10 @@ template <>
 void launch_cell_pass<GB_T>(const LevelView<GB_T>& L, int op, const GB_T* su, const GB_T* sp, GB_T* Eu, GB_T* Ep,
                             cudaStream_t s) {
   if (L.n_cells <= 0) return;
+  if (L.deg == 3) {  // Q3-Q2 (indexed levels only)
+    launch_ho_cell_pass<GB_T>(L, op, su, sp, Eu, Ep, s);
+    return;
+  }
 #if defined(GB_T_IS_FLOAT)
   {
     if (cell_pass_slot_major<GB_T>(L, op) && op == OPK_A && L.n_cells <= kSmallLatticeMaxCells) {

@@ -64,8 +64,23 @@ struct LevelDev {
   bool eig_given[2] = {false, false};
 };
 
+// 1D data of a velocity degree (2 or 3): velocity nodes (deal.II's FE_Q(p):
+// Gauss-Lobatto points), pressure nodes (FE_Q(p-1)), and QGauss(p+1) on [0, 1]
+struct Basis1D {
+  int deg = 2, nvn = 3, npn = 2, nq1 = 3;  // per direction: velocity nodes, pressure nodes, points
+  double vn[4], pn[3], gq[4], gw[4];
+};
+Basis1D basis1d(int degree);
+// Lagrange basis on `nodes` at x: values and first derivatives
+void lagrange_basis(const double* nodes, int n, double x, double* val, double* der);
+inline int ipow(int b, int e) { return e == 0 ? 1 : b * ipow(b, e - 1); }
+
 struct Level {
   int dim = 3;
+  int degree = 2;  // velocity degree
+  int nv() const { return ipow(degree + 1, dim); }  // velocity nodes per cell (one component)
+  int np() const { return ipow(degree, dim); }      // pressure nodes per cell
+  int nq() const { return ipow(degree + 1, dim); }  // quadrature points per cell
   long n_cells = 0, n_u = 0, n_p = 0;
   // caller data
   std::vector<int> cdu, cdp;
@@ -92,6 +107,7 @@ struct Level {
   DevBuf<int> perm_u_d, perm_p_d, cons_u_d, cons_p_d;
   DevBuf<int> cdu_raw_d, cdp_raw_d;  // internal cells x internal DoFs, no constraint codes (plain reads)
   DevBuf<int> probe_ptr, probe_g, probe_eptr, probe_li;
+  std::vector<int> probe_ptr_h, pprobe_ptr_h;  // host copies of the per-cell probe offsets
   DevBuf<int> pprobe_ptr, pprobe_g, pprobe_eptr, pprobe_li;
   DevBuf<int> Pu_ptr, Pu_col, PuT_ptr, PuT_col, Pp_ptr, Pp_col, PpT_ptr, PpT_col;
   long Pu_rows = 0, PuT_rows = 0, Pp_rows = 0, PpT_rows = 0;

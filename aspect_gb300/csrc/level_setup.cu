@@ -52,10 +52,57 @@ Csr Csr::transpose(long n_cols) const {
   return t;
 }
 
+Basis1D basis1d(int degree) {
+  Basis1D b;
+  b.deg = degree;
+  b.nvn = degree + 1;
+  b.npn = degree;
+  b.nq1 = degree + 1;
+  if (degree == 2) {
+    const double vn[3] = {0.0, 0.5, 1.0}, g[3] = {0.5 - std::sqrt(15.0) / 10, 0.5, 0.5 + std::sqrt(15.0) / 10};
+    const double w[3] = {5.0 / 18, 8.0 / 18, 5.0 / 18};
+    for (int i = 0; i < 3; ++i) { b.vn[i] = vn[i]; b.gq[i] = g[i]; b.gw[i] = w[i]; }
+    b.pn[0] = 0.0;
+    b.pn[1] = 1.0;
+  } else {
+    // Gauss-Lobatto nodes of 4 points: 0, (1 -+ 1/sqrt 5) / 2, 1; Gauss-Legendre
+    // of 4 points: (1 -+ sqrt(3/7 +- 2/7 sqrt(6/5))) / 2, weights (18 -+ sqrt 30) / 72
+    const double a = 0.5 / std::sqrt(5.0);
+    const double vn[4] = {0.0, 0.5 - a, 0.5 + a, 1.0};
+    const double t1 = std::sqrt(3.0 / 7 - 2.0 / 7 * std::sqrt(6.0 / 5)), t2 = std::sqrt(3.0 / 7 + 2.0 / 7 * std::sqrt(6.0 / 5));
+    const double g[4] = {0.5 - 0.5 * t2, 0.5 - 0.5 * t1, 0.5 + 0.5 * t1, 0.5 + 0.5 * t2};
+    const double wi = (18.0 + std::sqrt(30.0)) / 72, wo = (18.0 - std::sqrt(30.0)) / 72;
+    const double w[4] = {wo, wi, wi, wo};
+    for (int i = 0; i < 4; ++i) { b.vn[i] = vn[i]; b.gq[i] = g[i]; b.gw[i] = w[i]; }
+    b.pn[0] = 0.0;
+    b.pn[1] = 0.5;
+    b.pn[2] = 1.0;
+  }
+  return b;
+}
+
+void lagrange_basis(const double* nodes, int n, double x, double* val, double* der) {
+  for (int i = 0; i < n; ++i) {
+    double v = 1, d = 0, den = 1;
+    for (int m = 0; m < n; ++m)
+      if (m != i) den *= nodes[i] - nodes[m];
+    for (int m = 0; m < n; ++m) {
+      if (m == i) continue;
+      double t = 1;
+      for (int k = 0; k < n; ++k)
+        if (k != i && k != m) t *= x - nodes[k];
+      d += t;
+      v *= x - nodes[m];
+    }
+    val[i] = v / den;
+    der[i] = d / den;
+  }
+}
+
 namespace {
 
-int nv_of(int dim) { return dim == 3 ? 27 : 9; }
-int np_of(int dim) { return dim == 3 ? 8 : 4; }
+int nv_of(const Level& L) { return L.nv(); }
+int np_of(const Level& L) { return L.np(); }
 
 // ---------------------------------------------------------------- 1D basis (host)
 void lagrange(const double* nodes, int n, double x, double* val, double* der) {
@@ -78,8 +125,9 @@ void lagrange(const double* nodes, int n, double x, double* val, double* der) {
 
 // ---------------------------------------------------------------- structure detection
 bool detect_structured(Level& L) {
-  const int d = L.dim, nv = nv_of(d), np = np_of(d), nu = d * nv;
-  if (L.geom_kind != 0 || L.n_cells == 0) return false;
+  const int d = L.dim, nv = nv_of(L), np = np_of(L), nu = d * nv;
+  // the lattice kernels are Q2-Q1 kernels
+  if (L.degree != 2 || L.geom_kind != 0 || L.n_cells == 0) return false;
   // pressure constraints are not part of the lattice fast path
   for (long g = 0; g < L.n_p; ++g)
     if (L.cp.constrained((int)g)) return false;
@@ -216,7 +264,7 @@ bool detect_structured(Level& L) {
 
 // ---------------------------------------------------------------- general levels
 void setup_general(Level& L) {
-  const int d = L.dim, nv = nv_of(d), np = np_of(d), nu = d * nv, nq = nv;
+  const int d = L.dim, nv = nv_of(L), np = np_of(L), nu = d * nv, nq = L.nq();
   L.structured = false;
   L.perm_u.resize(L.n_u);
   L.perm_p.resize(L.n_p);
@@ -341,19 +389,21 @@ void setup_general(Level& L) {
     L.f64.gtab.upload(gt);
     L.f32.gtab.upload(std::vector<float>(gt.begin(), gt.end()));
   } else {
-    const double g3[3] = {0.5 - std::sqrt(15.0) / 10, 0.5, 0.5 + std::sqrt(15.0) / 10};
+    // Q2 mapping (3^dim support points per cell) at the QGauss(degree+1) points
+    const Basis1D B = basis1d(L.degree);
     const double q2n[3] = {0.0, 0.5, 1.0};
-    double v1[3][3], d1[3][3];
-    for (int q = 0; q < 3; ++q) lagrange(q2n, 3, g3[q], v1[q], d1[q]);
+    const int nm = ipow(3, d), n1 = B.nq1;
+    double v1[4][3], d1[4][3];
+    for (int q = 0; q < n1; ++q) lagrange(q2n, 3, B.gq[q], v1[q], d1[q]);
     const int stride = d * d + 1;
     std::vector<double> gt((size_t)L.n_cells * nq * stride);
     for (long c = 0; c < L.n_cells; ++c) {
       const long ic = L.internal_of_cell[c];
-      const double* X = &L.geom[(size_t)c * nv * d];
+      const double* X = &L.geom[(size_t)c * nm * d];
       for (int q = 0; q < nq; ++q) {
-        const int qi[3] = {q % 3, (q / 3) % 3, q / 9};
+        const int qi[3] = {q % n1, (q / n1) % n1, q / (n1 * n1)};
         double J[3][3] = {{0}};
-        for (int n = 0; n < nv; ++n) {
+        for (int n = 0; n < nm; ++n) {
           const int ni[3] = {n % 3, (n / 3) % 3, n / 9};
           for (int b = 0; b < d; ++b) {
             double t = 1;
@@ -425,7 +475,8 @@ void setup_general(Level& L) {
   build_gather(L.cdp, L.cp, np, L.n_p, L.gp_ptr, L.gp_slot, L.f64.gp_w, L.f32.gp_w, L.cmask_p);
   // diagonal probes: per internal cell, the unconstrained DoFs it touches
   auto build_probes = [&](const std::vector<int>& cd, const HostCons& C, int nl, DevBuf<int>& pptr, DevBuf<int>& pg,
-                          DevBuf<int>& peptr, DevBuf<int>& pli, DevBuf<double>& pw64, DevBuf<float>& pw32) {
+                          DevBuf<int>& peptr, DevBuf<int>& pli, DevBuf<double>& pw64, DevBuf<float>& pw32,
+                          std::vector<int>& ptr_h) {
     std::vector<int> ptr(1, 0), g, eptr(1, 0), li;
     std::vector<double> w;
     for (long ic = 0; ic < L.n_cells; ++ic) {
@@ -446,22 +497,24 @@ void setup_general(Level& L) {
       ptr.push_back((int)g.size());
     }
     pptr.upload(ptr);
+    ptr_h = ptr;
     pg.upload(g);
     peptr.upload(eptr);
     pli.upload(li);
     pw64.upload(w);
     pw32.upload(std::vector<float>(w.begin(), w.end()));
   };
-  build_probes(L.cdu, L.cu, nu, L.probe_ptr, L.probe_g, L.probe_eptr, L.probe_li, L.f64.probe_w, L.f32.probe_w);
+  build_probes(L.cdu, L.cu, nu, L.probe_ptr, L.probe_g, L.probe_eptr, L.probe_li, L.f64.probe_w, L.f32.probe_w,
+               L.probe_ptr_h);
   build_probes(L.cdp, L.cp, np, L.pprobe_ptr, L.pprobe_g, L.pprobe_eptr, L.pprobe_li, L.f64.pprobe_w,
-               L.f32.pprobe_w);
+               L.f32.pprobe_w, L.pprobe_ptr_h);
 }
 
 }  // namespace
 
 void setup_level(Level& L, bool force_indexed) {
   if (force_indexed || !detect_structured(L)) setup_general(L);
-  const int nu = L.dim * nv_of(L.dim), np = np_of(L.dim);
+  const int nu = L.dim * nv_of(L), np = np_of(L);
   L.f64.Eu.alloc((size_t)L.n_cells * nu);
   L.f64.Ep.alloc((size_t)L.n_cells * np);
   L.f32.Eu.alloc((size_t)L.n_cells * nu);
@@ -477,10 +530,12 @@ void setup_level(Level& L, bool force_indexed) {
 // resolved, evaluated at the fine support points (reference coordinates of the
 // child inside its parent). Restriction is the transpose.
 void setup_transfer(Level& F, const Level& C) {
-  const int d = F.dim, nv = nv_of(d), np = np_of(d), nu = d * nv;
+  const int d = F.dim, nv = nv_of(F), np = np_of(F), nu = d * nv;
   GB_CHECK(F.has_transfer, 2, "missing child/parent data for a level");
-  const double q2n[3] = {0.0, 0.5, 1.0}, q1n[2] = {0.0, 1.0};
+  const Basis1D B = basis1d(F.degree);
   for (int block = 0; block < 2; ++block) {
+    const int n1 = block == 0 ? B.nvn : B.npn;  // nodes per direction
+    const double* nodes = block == 0 ? B.vn : B.pn;
     const int nl = block == 0 ? nv : np;
     const int ncomp = block == 0 ? d : 1;
     const long nf = block == 0 ? F.n_u : F.n_p;
@@ -496,21 +551,16 @@ void setup_transfer(Level& F, const Level& C) {
       for (int n = 0; n < nl; ++n) {
         double xi[3];
         for (int e = 0; e < d; ++e) {
-          const int idx = block == 0 ? (e == 0 ? n % 3 : e == 1 ? (n / 3) % 3 : n / 9)
-                                     : (e == 0 ? n % 2 : e == 1 ? (n / 2) % 2 : n / 4);
-          const double loc = block == 0 ? 0.5 * idx : (double)idx;
+          const int idx = (e == 0 ? n : e == 1 ? n / n1 : n / (n1 * n1)) % n1;
+          const double loc = nodes[idx];
           xi[e] = ch == kSameCell ? loc : 0.5 * (((ch >> e) & 1) + loc);
         }
-        double phi[27];
-        double vv[3][3], dd[3][3];
-        for (int e = 0; e < d; ++e) lagrange(block == 0 ? q2n : q1n, block == 0 ? 3 : 2, xi[e], vv[e], dd[e]);
+        double phi[64];
+        double vv[3][4], dd[3][4];
+        for (int e = 0; e < d; ++e) lagrange(nodes, n1, xi[e], vv[e], dd[e]);
         for (int m = 0; m < nl; ++m) {
           double t = 1;
-          for (int e = 0; e < d; ++e) {
-            const int mi = block == 0 ? (e == 0 ? m % 3 : e == 1 ? (m / 3) % 3 : m / 9)
-                                      : (e == 0 ? m % 2 : e == 1 ? (m / 2) % 2 : m / 4);
-            t *= vv[e][mi];
-          }
+          for (int e = 0; e < d; ++e) t *= vv[e][(e == 0 ? m : e == 1 ? m / n1 : m / (n1 * n1)) % n1];
           phi[m] = t;
         }
         for (int comp = 0; comp < ncomp; ++comp) {
@@ -561,6 +611,7 @@ LevelView<T> Level::view(double s, int compressible) {
   LevelView<T> v{};
   LevelDev<T>& D = dev<T>();
   v.dim = dim;
+  v.deg = degree;
   v.n_cells = (int)n_cells;
   v.n_u = (int)n_u;
   v.n_p = (int)n_p;

@@ -106,6 +106,7 @@ extern "C" int gb_gmg_ablock_apply_lattice_noalloc(int dim, const int32_t* n_cel
   }
 
   LevelView<float> L{};
+  L.deg = 2;
   L.dim = dim;
   L.n_cells = (int)n_cells;
   L.structured = 1;

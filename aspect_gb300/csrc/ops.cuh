@@ -46,6 +46,15 @@ template <typename T>
 void launch_newton_stokes(const LevelView<T>& L, const NewtonView<T>& N, const T* su, const T* sp, T* Eu, T* Ep,
                           bool slot_major, cudaStream_t s);
 
+// Degree-3 velocity (Q3-Q2) cell operators of indexed levels (ho_kernels.cu):
+// the cell pass of any operator, and the A-block (block 0) / mass (block 1)
+// diagonal of one cell colour from its probes (n_probes of the colour's cells)
+template <typename T>
+void launch_ho_cell_pass(const LevelView<T>& L, int op, const T* su, const T* sp, T* Eu, T* Ep, cudaStream_t s);
+template <typename T>
+void launch_ho_diag(const LevelView<T>& L, int block, int begin, int count, const ProbesView<T>& pr, int n_probes,
+                    T* diag, cudaStream_t s);
+
 // Free-surface faces of the finest level (free_surface.cu), grouped by internal
 // cell: the faces of cell gcell[g] are gptr[g] .. gptr[g+1]-1; per face its
 // number 2*d + side, the constraint codes of its 3^(dim-1) nodes per component

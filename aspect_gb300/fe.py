@@ -20,6 +20,18 @@ import numpy as np
 
 Q2_NODES = np.array([0.0, 0.5, 1.0])
 Q1_NODES = np.array([0.0, 1.0])
+# FE_Q(3): deal.II's default support points are the Gauss-Lobatto points
+Q3_NODES = np.array([0.0, 0.5 - 0.5 / np.sqrt(5.0), 0.5 + 0.5 / np.sqrt(5.0), 1.0])
+
+
+def velocity_nodes(degree: int) -> np.ndarray:
+    """1D support points of the velocity element FE_Q(degree) (degree 2 or 3)."""
+    return {2: Q2_NODES, 3: Q3_NODES}[degree]
+
+
+def pressure_nodes(degree: int) -> np.ndarray:
+    """1D support points of the pressure element FE_Q(degree - 1)."""
+    return {2: Q1_NODES, 3: Q2_NODES}[degree]
 
 
 def gauss(n: int) -> tuple[np.ndarray, np.ndarray]:

@@ -174,18 +174,21 @@ def default_solve_params(**kw) -> SolveParams:
 class StokesMatrixFreeGPU:
     """GPU matrix-free GMG Stokes solver behind the C ABI; name() = "GMG-GB300"."""
 
-    def __init__(self, dim: int, n_levels: int, options: dict | None = None):
+    def __init__(self, dim: int, n_levels: int, options: dict | None = None, degree: int = 2):
+        """degree: the velocity degree ("Stokes velocity polynomial degree"), 2 (Q2-Q1)
+        or 3 (Q3-Q2)."""
         self.L = load_library()
         opt = Options()
         self.L.gb_gmg_default_options(ctypes.byref(opt))
         for k, v in (options or {}).items():
             setattr(opt, k, v)
         h = ctypes.c_void_p()
-        rc = self.L.gb_gmg_create(ctypes.byref(opt), dim, 2, n_levels, ctypes.byref(h))
+        rc = self.L.gb_gmg_create(ctypes.byref(opt), dim, degree, n_levels, ctypes.byref(h))
         if rc != 0:
             raise GmgError(rc, "gb_gmg_create failed")
         self.h = h
         self.dim = dim
+        self.degree = degree
         self.n_levels = n_levels
         self.levels = None
 
@@ -211,8 +214,14 @@ class StokesMatrixFreeGPU:
         """Hand over the level meshes, constraints and parent/child data."""
         self.levels = levels
         keep = []
+        d, k = self.dim, self.degree
         for l, m in enumerate(levels):
             cdu, cdp, g = _i(m.cell_dofs_u), _i(m.cell_dofs_p), _d(m.geometry)
+            # the library reads these many entries (gb_gmg_set_level_mesh)
+            n_geom = {0: 2 * d, 1: 3 ** d * d, 2: (k + 1) ** d * (d * d + 1)}[m.geom_kind]
+            if (cdu.size != m.n_cells * d * (k + 1) ** d or cdp.size != m.n_cells * k ** d
+                    or g.size != m.n_cells * n_geom):
+                raise ValueError(f"level {l}: cell DoF or geometry arrays do not match degree {k}")
             keep += [cdu, cdp, g]
             self._chk(self.L.gb_gmg_set_level_mesh(self.h, l, m.n_cells, _p(cdu), _p(cdp), m.geom_kind, _p(g),
                                                    m.n_u, m.n_p))

@@ -112,6 +112,7 @@ class LevelMesh:
     dof_points_p: np.ndarray | None = None
     # Optional extra information used by the harness only.
     cell_level: np.ndarray | None = None
+    degree: int = 2  # velocity degree: FE_Q(degree)^dim x FE_Q(degree - 1)
 
     def q2_support_points(self) -> np.ndarray:
         """Q2 mapping support points per cell, shape (n_cells, 3**dim, dim)."""
@@ -216,7 +217,7 @@ def _lex(idx: tuple, shape: tuple) -> int:
 
 
 def box_level(dim: int, ncells: tuple, extent: tuple, origin: tuple | None = None,
-              free_slip: bool = True, no_slip: bool = False, open_faces: tuple = ()) -> LevelMesh:
+              free_slip: bool = True, no_slip: bool = False, open_faces: tuple = (), degree: int = 2) -> LevelMesh:
     """Uniform axis-aligned box with lexicographic cells, component-blocked
     Q2 velocity numbering and lexicographic Q1 pressure numbering.
 
@@ -225,12 +226,16 @@ def box_level(dim: int, ncells: tuple, extent: tuple, origin: tuple | None = Non
     on a box (VectorTools::compute_no_normal_flux_constraints on axis-aligned
     faces). ``no_slip``: every component is zero on every face, as ``Zero
     velocity boundary indicators`` on all faces gives. ``open_faces``: face
-    numbers 2*d + side left without constraints (e.g. a free surface)."""
+    numbers 2*d + side left without constraints (e.g. a free surface).
+    ``degree``: velocity degree (2: Q2-Q1, 3: Q3-Q2 with Gauss-Lobatto velocity
+    nodes)."""
+    from . import fe
     origin = origin or (0.0,) * dim
     ncells = tuple(ncells)
     h = tuple(extent[d] / ncells[d] for d in range(dim))
-    nn = tuple(2 * n + 1 for n in ncells)  # Q2 nodes per direction
-    npn = tuple(n + 1 for n in ncells)  # Q1 nodes per direction
+    pd = degree - 1  # pressure degree
+    nn = tuple(degree * n + 1 for n in ncells)  # velocity nodes per direction
+    npn = tuple(pd * n + 1 for n in ncells)  # pressure nodes per direction
     n_nodes = int(np.prod(nn))
     n_pnodes = int(np.prod(npn))
     n_cells = int(np.prod(ncells))
@@ -238,13 +243,13 @@ def box_level(dim: int, ncells: tuple, extent: tuple, origin: tuple | None = Non
     # cell multi-indices, x fastest
     cidx = np.stack(np.meshgrid(*[np.arange(n) for n in ncells], indexing="ij"), -1)
     cidx = cidx.transpose(*reversed(range(dim)), dim).reshape(-1, dim)  # x fastest
-    loc = np.array(list(itertools.product(range(3), repeat=dim)))[:, ::-1]  # x fastest
-    locp = np.array(list(itertools.product(range(2), repeat=dim)))[:, ::-1]
+    loc = np.array(list(itertools.product(range(degree + 1), repeat=dim)))[:, ::-1]  # x fastest
+    locp = np.array(list(itertools.product(range(pd + 1), repeat=dim)))[:, ::-1]
 
     strides = np.cumprod((1,) + nn[:-1])
     pstrides = np.cumprod((1,) + npn[:-1])
-    node = ((2 * cidx[:, None, :] + loc[None, :, :]) * strides).sum(-1)  # (n_cells, 3^d)
-    pnode = ((cidx[:, None, :] + locp[None, :, :]) * pstrides).sum(-1)
+    node = ((degree * cidx[:, None, :] + loc[None, :, :]) * strides).sum(-1)  # (n_cells, (degree+1)^d)
+    pnode = ((pd * cidx[:, None, :] + locp[None, :, :]) * pstrides).sum(-1)
     cell_dofs_u = np.concatenate([node + c * n_nodes for c in range(dim)], axis=1).astype(np.int32)
     cell_dofs_p = pnode.astype(np.int32)
 
@@ -253,13 +258,22 @@ def box_level(dim: int, ncells: tuple, extent: tuple, origin: tuple | None = Non
         geom[:, d] = origin[d] + cidx[:, d] * h[d]
         geom[:, dim + d] = h[d]
 
-    # DoF positions
+    # DoF positions: global node G along a direction lies in cell G // degree at
+    # the local node G % degree (the last node closes the last cell)
+    def coord(G, k, nodes):
+        c = np.minimum(G // k, ncells[d_] - 1)
+        return origin[d_] + (c + nodes[G - k * c]) * h[d_]
+
+    vnodes, pnodes = fe.velocity_nodes(degree), fe.pressure_nodes(degree)
     nidx = np.stack(np.meshgrid(*[np.arange(n) for n in nn], indexing="ij"), -1)
     nidx = nidx.transpose(*reversed(range(dim)), dim).reshape(-1, dim)
-    pts_u = np.array([origin[d] + nidx[:, d] * 0.5 * h[d] for d in range(dim)]).T
     pidx = np.stack(np.meshgrid(*[np.arange(n) for n in npn], indexing="ij"), -1)
     pidx = pidx.transpose(*reversed(range(dim)), dim).reshape(-1, dim)
-    pts_p = np.array([origin[d] + pidx[:, d] * h[d] for d in range(dim)]).T
+    pts_u, pts_p = [], []
+    for d_ in range(dim):
+        pts_u.append(coord(nidx[:, d_], degree, vnodes))
+        pts_p.append(coord(pidx[:, d_], pd, pnodes))
+    pts_u, pts_p = np.array(pts_u).T, np.array(pts_p).T
 
     lines = {}
     def face_nodes(d, side):
@@ -288,11 +302,12 @@ def box_level(dim: int, ncells: tuple, extent: tuple, origin: tuple | None = Non
                      geometry=geom, constraints_u=cu, constraints_p=Constraints.empty(),
                      dof_points_u=np.tile(pts_u, (dim, 1)),
                      dof_component_u=np.repeat(np.arange(dim), n_nodes),
-                     dof_points_p=pts_p)
+                     dof_points_p=pts_p, degree=degree)
 
 
 def box_hierarchy(dim: int, n_fine: int, extent=None, n_coarse: int = 1,
-                  free_slip: bool = True, no_slip: bool = False, open_faces: tuple = ()) -> list[LevelMesh]:
+                  free_slip: bool = True, no_slip: bool = False, open_faces: tuple = (),
+                  degree: int = 2) -> list[LevelMesh]:
     """Global-coarsening hierarchy of uniform boxes: level l has n_coarse*2**l
     cells per direction, up to n_fine on the finest level."""
     extent = tuple(extent or (1.0,) * dim)
@@ -300,7 +315,7 @@ def box_hierarchy(dim: int, n_fine: int, extent=None, n_coarse: int = 1,
     n = n_coarse
     while n <= n_fine:
         levels.append(box_level(dim, (n,) * dim, extent, free_slip=free_slip, no_slip=no_slip,
-                                open_faces=open_faces))
+                                open_faces=open_faces, degree=degree))
         n *= 2
     assert levels and n // 2 == n_fine, "n_fine must be n_coarse * 2**k"
     for l in range(1, len(levels)):
@@ -354,12 +369,12 @@ def to_q2_geometry(level: LevelMesh, distortion=None) -> LevelMesh:
 
 
 def to_table_geometry(level: LevelMesh, jacobians: np.ndarray | None = None) -> LevelMesh:
-    """Same level with GEOM_TABLE cell geometry: per cell and QGauss(3) point the
-    inverse Jacobian (d xi_d / d x_e at [d*dim+e]) and |det J|. ``jacobians``
-    (n_cells, 3**dim, dim, dim) [x-component, xi-direction] are the caller's
-    mapping at the Gauss points; by default the level's own mapping."""
+    """Same level with GEOM_TABLE cell geometry: per cell and QGauss(degree+1)
+    point the inverse Jacobian (d xi_d / d x_e at [d*dim+e]) and |det J|.
+    ``jacobians`` (n_cells, (degree+1)**dim, dim, dim) [x-component, xi-direction]
+    are the caller's mapping at the Gauss points; by default the level's own mapping."""
     from . import fe
-    gp = fe.tensor_points(level.dim, fe.gauss(3)[0])
+    gp = fe.tensor_points(level.dim, fe.gauss(level.degree + 1)[0])
     J = level.jacobians(gp) if jacobians is None else np.asarray(jacobians, float)
     inv = np.linalg.inv(J)
     det = np.abs(np.linalg.det(J))

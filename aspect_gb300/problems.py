@@ -80,13 +80,13 @@ def q_points_real(level: LevelMesh, n1d: int = 3) -> tuple[np.ndarray, np.ndarra
 
 
 def assemble_rhs(level: LevelMesh, force_q: np.ndarray) -> np.ndarray:
-    """f_u = int force . phi_u over QGauss(3); force_q: (n_cells, n_q, dim).
+    """f_u = int force . phi_u over QGauss(degree+1); force_q: (n_cells, n_q, dim).
     Pressure block zero (incompressible). Condensed with the constraints."""
-    dim = level.dim
-    pts, w = fe.quadrature(dim, 3)
-    phi = fe.shape_values(dim, fe.Q2_NODES, pts)  # (nq, nv)
-    _, jxw = q_points_real(level)
-    nv = 3 ** dim
+    dim, deg = level.dim, level.degree
+    pts, w = fe.quadrature(dim, deg + 1)
+    phi = fe.shape_values(dim, fe.velocity_nodes(deg), pts)  # (nq, nv)
+    _, jxw = q_points_real(level, deg + 1)
+    nv = (deg + 1) ** dim
     f = np.zeros(level.n_u + level.n_p)
     loc = np.einsum("cqd,qn,cq->cdn", force_q, phi, jxw).reshape(level.n_cells, dim * nv)
     np.add.at(f, level.cell_dofs_u.ravel(), loc.ravel())
@@ -145,11 +145,11 @@ def normalize_pressure_volume(level: LevelMesh, p: np.ndarray) -> float:
 
 def evaluate_fields(level: LevelMesh, u: np.ndarray, p: np.ndarray, n1d: int):
     """Velocity and pressure at QGauss(n1d) points: (n_cells, nq, dim), (n_cells, nq)."""
-    dim = level.dim
+    dim, deg = level.dim, level.degree
     pts, w = fe.quadrature(dim, n1d)
-    phi = fe.shape_values(dim, fe.Q2_NODES, pts)
-    psi = fe.shape_values(dim, fe.Q1_NODES, pts)
-    nv = 3 ** dim
+    phi = fe.shape_values(dim, fe.velocity_nodes(deg), pts)
+    psi = fe.shape_values(dim, fe.pressure_nodes(deg), pts)
+    nv = (deg + 1) ** dim
     ul = u[level.cell_dofs_u].reshape(level.n_cells, dim, nv)
     uq = np.einsum("qn,cdn->cqd", phi, ul)
     pq = np.einsum("qn,cn->cq", psi, p[level.cell_dofs_p])

@@ -37,6 +37,8 @@ def lib():
         L = ctypes.CDLL(LIB_PATH)
         L.orc_create.restype = ctypes.c_void_p
         L.orc_create.argtypes = [ctypes.c_int, ctypes.c_int]
+        L.orc_create_degree.restype = ctypes.c_void_p
+        L.orc_create_degree.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.orc_destroy.argtypes = [ctypes.c_void_p]
         L.orc_last_error.restype = ctypes.c_char_p
         L.orc_last_error.argtypes = [ctypes.c_void_p]
@@ -79,7 +81,8 @@ class Oracle:
             self.L.orc_set_num_threads(int(n_threads))
         self.levels = levels
         self.dim = levels[0].dim
-        self.h = ctypes.c_void_p(self.L.orc_create(self.dim, len(levels)))
+        self.degree = getattr(levels[0], "degree", 2)  # velocity degree of the level meshes
+        self.h = ctypes.c_void_p(self.L.orc_create_degree(self.dim, self.degree, len(levels)))
         for l, m in enumerate(levels):
             cdu, cdp, g = _i(m.cell_dofs_u), _i(m.cell_dofs_p), _d(m.geometry)
             self._chk(self.L.orc_set_level_mesh(self.h, l, m.n_cells, _ptr(cdu, _ip), _ptr(cdp, _ip),

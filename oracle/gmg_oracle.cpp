@@ -69,54 +69,109 @@ static void lagrange1d(const double* nodes, int n, double x, double* val, double
 }
 
 struct FE {
-  int dim = 3, nv = 27, np = 8, nq = 27, nu = 81;
-  std::vector<double> qpts, qw;          // [nq][dim], [nq]
-  std::vector<double> vval, vgrad;       // Q2: [nq][nv], [nq][nv][dim]
-  std::vector<double> pval;              // Q1: [nq][np]
-  void init(int d) {
+  int dim = 3, degree = 2, n1 = 3, nv = 27, np = 8, nq = 27, nu = 81, nm = 27;
+  double vnodes[4], pnodes[3];           // 1D velocity (FE_Q(degree), Gauss-Lobatto) / pressure nodes
+  std::vector<double> qpts, qw;          // QGauss(degree+1): [nq][dim], [nq]
+  std::vector<double> vval, vgrad;       // velocity basis: [nq][nv], [nq][nv][dim]
+  std::vector<double> pval;              // pressure basis (FE_Q(degree-1)): [nq][np]
+  std::vector<double> q1val;             // Q1 basis (viscosity projection): [nq][2^dim]
+  std::vector<double> mgrad;             // Q2 mapping basis gradients: [nq][nm][dim]
+  void init(int d, int deg = 2) {
     dim = d;
-    nv = d == 3 ? 27 : 9;
-    np = d == 3 ? 8 : 4;
+    degree = deg;
+    n1 = deg + 1;
+    const int pn = deg;  // pressure nodes per direction
+    nv = d == 3 ? n1 * n1 * n1 : n1 * n1;
+    np = d == 3 ? pn * pn * pn : pn * pn;
     nq = nv;
     nu = d * nv;
-    const double g[3] = {0.5 - 0.5 * std::sqrt(0.6), 0.5, 0.5 + 0.5 * std::sqrt(0.6)};
-    const double gw[3] = {5.0 / 18.0, 8.0 / 18.0, 5.0 / 18.0};
+    nm = d == 3 ? 27 : 9;
+    double g[4], gw[4];
+    if (deg == 2) {
+      const double g3[3] = {0.5 - 0.5 * std::sqrt(0.6), 0.5, 0.5 + 0.5 * std::sqrt(0.6)};
+      const double w3[3] = {5.0 / 18.0, 8.0 / 18.0, 5.0 / 18.0};
+      for (int i = 0; i < 3; ++i) { g[i] = g3[i]; gw[i] = w3[i]; }
+      vnodes[0] = 0.0; vnodes[1] = 0.5; vnodes[2] = 1.0;
+      pnodes[0] = 0.0; pnodes[1] = 1.0;
+    } else {
+      // QGauss(4): (1 -+ sqrt(3/7 +- 2/7 sqrt(6/5))) / 2, weights (18 -+ sqrt 30) / 72;
+      // FE_Q(3) nodes: Gauss-Lobatto 0, (1 -+ 1/sqrt 5) / 2, 1
+      const double t1 = std::sqrt(3.0 / 7 - 2.0 / 7 * std::sqrt(1.2)), t2 = std::sqrt(3.0 / 7 + 2.0 / 7 * std::sqrt(1.2));
+      g[0] = 0.5 - 0.5 * t2; g[1] = 0.5 - 0.5 * t1; g[2] = 0.5 + 0.5 * t1; g[3] = 0.5 + 0.5 * t2;
+      gw[0] = gw[3] = (18.0 - std::sqrt(30.0)) / 72;
+      gw[1] = gw[2] = (18.0 + std::sqrt(30.0)) / 72;
+      vnodes[0] = 0.0; vnodes[1] = 0.5 - 0.5 / std::sqrt(5.0); vnodes[2] = 0.5 + 0.5 / std::sqrt(5.0); vnodes[3] = 1.0;
+      pnodes[0] = 0.0; pnodes[1] = 0.5; pnodes[2] = 1.0;
+    }
     const double q2n[3] = {0.0, 0.5, 1.0}, q1n[2] = {0.0, 1.0};
+    const int nc1 = d == 3 ? 8 : 4;
     qpts.assign(nq * dim, 0.0);
     qw.assign(nq, 1.0);
     vval.assign(nq * nv, 1.0);
     vgrad.assign(nq * nv * dim, 1.0);
     pval.assign(nq * np, 1.0);
+    q1val.assign(nq * nc1, 1.0);
+    mgrad.assign(nq * nm * dim, 1.0);
     for (int q = 0; q < nq; ++q) {
-      int qi[3] = {q % 3, (q / 3) % 3, q / 9};
-      double v2[3][3], d2[3][3], v1[3][2], d1[3][2];
+      int qi[3] = {q % n1, (q / n1) % n1, q / (n1 * n1)};
+      double vv[3][4], dv[3][4], vp[3][3], dp_[3][3], v1[3][2], d1[3][2], vm[3][3], dm[3][3];
       for (int e = 0; e < dim; ++e) {
         qpts[q * dim + e] = g[qi[e]];
         qw[q] *= gw[qi[e]];
-        lagrange1d(q2n, 3, g[qi[e]], v2[e], d2[e]);
+        lagrange1d(vnodes, n1, g[qi[e]], vv[e], dv[e]);
+        lagrange1d(pnodes, pn, g[qi[e]], vp[e], dp_[e]);
         lagrange1d(q1n, 2, g[qi[e]], v1[e], d1[e]);
+        lagrange1d(q2n, 3, g[qi[e]], vm[e], dm[e]);
       }
       for (int n = 0; n < nv; ++n) {
-        int ni[3] = {n % 3, (n / 3) % 3, n / 9};
+        int ni[3] = {n % n1, (n / n1) % n1, n / (n1 * n1)};
         double v = 1.0;
-        for (int e = 0; e < dim; ++e) v *= v2[e][ni[e]];
+        for (int e = 0; e < dim; ++e) v *= vv[e][ni[e]];
         vval[q * nv + n] = v;
         for (int gdir = 0; gdir < dim; ++gdir) {
           double t = 1.0;
-          for (int e = 0; e < dim; ++e) t *= (e == gdir ? d2[e][ni[e]] : v2[e][ni[e]]);
+          for (int e = 0; e < dim; ++e) t *= (e == gdir ? dv[e][ni[e]] : vv[e][ni[e]]);
           vgrad[(q * nv + n) * dim + gdir] = t;
         }
       }
+      for (int n = 0; n < nm; ++n) {
+        int ni[3] = {n % 3, (n / 3) % 3, n / 9};
+        for (int gdir = 0; gdir < dim; ++gdir) {
+          double t = 1.0;
+          for (int e = 0; e < dim; ++e) t *= (e == gdir ? dm[e][ni[e]] : vm[e][ni[e]]);
+          mgrad[(q * nm + n) * dim + gdir] = t;
+        }
+      }
       for (int n = 0; n < np; ++n) {
+        int ni[3] = {n % pn, (n / pn) % pn, n / (pn * pn)};
+        double v = 1.0;
+        for (int e = 0; e < dim; ++e) v *= vp[e][ni[e]];
+        pval[q * np + n] = v;
+      }
+      for (int n = 0; n < nc1; ++n) {
         int ni[3] = {n % 2, (n / 2) % 2, n / 4};
         double v = 1.0;
         for (int e = 0; e < dim; ++e) v *= v1[e][ni[e]];
-        pval[q * np + n] = v;
+        q1val[q * nc1 + n] = v;
       }
     }
   }
+  // basis values of the velocity (block 0) or pressure (block 1) element at a
+  // reference point
+  void basis_at(int block, const double* xi, double* out) const {
+    const int n = block == 0 ? n1 : degree;
+    const double* nodes = block == 0 ? vnodes : pnodes;
+    double v[3][4], dd[3][4];
+    for (int e = 0; e < dim; ++e) lagrange1d(nodes, n, xi[e], v[e], dd[e]);
+    const int cnt = dim == 3 ? n * n * n : n * n;
+    for (int m = 0; m < cnt; ++m) {
+      const int mi[3] = {m % n, (m / n) % n, m / (n * n)};
+      double t = 1.0;
+      for (int e = 0; e < dim; ++e) t *= v[e][mi[e]];
+      out[m] = t;
+    }
+  }
 };
-
 // Value of the Q2 / Q1 basis at a reference point (for transfer matrices).
 static void q2_basis_at(int dim, const double* xi, double* out) {
   const double nodes[3] = {0.0, 0.5, 1.0};
@@ -213,10 +268,10 @@ static void compute_geometry(Level& L, const FE& fe) {
       if (L.geom_kind == 0) {
         for (int e = 0; e < d; ++e) J[e][e] = L.geom[(size_t)c * 2 * d + d + e];
       } else {
-        const double* X = &L.geom[(size_t)c * fe.nv * d];
-        for (int n = 0; n < fe.nv; ++n)
+        const double* X = &L.geom[(size_t)c * fe.nm * d];  // Q2 mapping support points
+        for (int n = 0; n < fe.nm; ++n)
           for (int a = 0; a < d; ++a)
-            for (int b = 0; b < d; ++b) J[a][b] += X[n * d + a] * fe.vgrad[(q * fe.nv + n) * d + b];
+            for (int b = 0; b < d; ++b) J[a][b] += X[n * d + a] * fe.mgrad[(q * fe.nm + n) * d + b];
       }
       double det, inv[3][3];
       if (d == 2) {
@@ -364,7 +419,7 @@ static void cell_apply(const Level& L, const FE& fe, int c, int op, double s, in
     // real-space gradients of the velocity basis at q
     T G[3][3] = {{0}};
     T pq = 0;
-    T grad_phi[27][3];
+    T grad_phi[64][3];
     if (op != OP_MASS) {
       for (int n = 0; n < nv; ++n)
         for (int e = 0; e < d; ++e) {
@@ -618,7 +673,7 @@ template <class T>
 static void cell_apply_any(const Level& L, const FE& fe, int c, int op, double s, int compressible,
                            const T* eta_tab, const T* xu, const T* xp, T* yu, T* yp,
                            const NewtonTerms* nt = nullptr) {
-  if (g_fast && op != OP_MASS && !nt) {
+  if (g_fast && op != OP_MASS && !nt && fe.degree == 2) {
     if (L.dim == 3) cell_apply_sf<T, 3>(L, fe, c, op, s, compressible, eta_tab, xu, xp, yu, yp);
     else cell_apply_sf<T, 2>(L, fe, c, op, s, compressible, eta_tab, xu, xp, yu, yp);
     return;
@@ -762,7 +817,7 @@ struct Oracle {
 #pragma omp parallel for schedule(static)
       for (int ci = L.colour_ptr[k]; ci < L.colour_ptr[k + 1]; ++ci) {
         int c = L.colour_cells[ci];
-        T xu[81] = {0}, xp[8] = {0}, yu[81] = {0}, yp[8] = {0};
+        T xu[192] = {0}, xp[27] = {0}, yu[192] = {0}, yp[27] = {0};
         if (ru)
           for (int i = 0; i < nu; ++i) {
             Expansion e = expand(L.cu, L.cdu[(size_t)c * nu + i]);
@@ -829,13 +884,13 @@ struct Oracle {
         // element matrix by unit vectors
         std::vector<double> K((size_t)nl * nl, 0.0);
         for (int j = 0; j < nl; ++j) {
-          double xu[81] = {0}, xp[8] = {0}, yu[81] = {0}, yp[8] = {0};
+          double xu[192] = {0}, xp[27] = {0}, yu[192] = {0}, yp[27] = {0};
           if (block == 0) xu[j] = 1.0; else xp[j] = 1.0;
           cell_apply_any<double>(L, fe, c, block == 0 ? OP_A : OP_MASS, s, compressible, L.eta.data(), xu, xp, yu, yp);
           for (int i = 0; i < nl; ++i) K[(size_t)i * nl + j] = block == 0 ? yu[i] : yp[i];
         }
         for (int g : gs) {
-          double v[81];
+          double v[192];
           for (int i = 0; i < nl; ++i) {
             v[i] = 0;
             for (int m = 0; m < ex[i].n; ++m)
@@ -875,14 +930,15 @@ struct Oracle {
         int pc = F.parent[fc], ch = F.child[fc];
         for (int n = 0; n < nl; ++n) {
           double xi[3];
+          const int n1 = block == 0 ? fe.n1 : fe.degree;  // nodes per direction
+          const double* nodes = block == 0 ? fe.vnodes : fe.pnodes;
           for (int e = 0; e < d; ++e) {
-            int idx = block == 0 ? (e == 0 ? n % 3 : e == 1 ? (n / 3) % 3 : n / 9)
-                                 : (e == 0 ? n % 2 : e == 1 ? (n / 2) % 2 : n / 4);
-            double loc = block == 0 ? 0.5 * idx : (double)idx;
+            int idx = (e == 0 ? n : e == 1 ? n / n1 : n / (n1 * n1)) % n1;
+            double loc = nodes[idx];
             xi[e] = ch == 255 ? loc : 0.5 * (((ch >> e) & 1) + loc);  // 255: the same cell
           }
-          double phi[27];
-          if (block == 0) q2_basis_at(d, xi, phi); else q1_basis_at(d, xi, phi);
+          double phi[64];
+          fe.basis_at(block, xi, phi);
           for (int comp = 0; comp < ncomp; ++comp) {
             int gf = block == 0 ? F.cdu[(size_t)fc * fe.nu + comp * nl + n] : F.cdp[(size_t)fc * fe.np + n];
             const Constraints& FC = block == 0 ? F.cu : F.cp;
@@ -1055,8 +1111,8 @@ struct Oracle {
         for (int q = 0; q < nq; ++q) {
           double jw = Fl.JxW[(size_t)c * nq + q];
           for (int i = 0; i < nc_v; ++i) {
-            b[i] += jw * fe.pval[q * nc_v + i] * eta_in[(size_t)c * nq + q];
-            for (int j = 0; j < nc_v; ++j) M[i][j] += jw * fe.pval[q * nc_v + i] * fe.pval[q * nc_v + j];
+            b[i] += jw * fe.q1val[q * nc_v + i] * eta_in[(size_t)c * nq + q];
+            for (int j = 0; j < nc_v; ++j) M[i][j] += jw * fe.q1val[q * nc_v + i] * fe.q1val[q * nc_v + j];
           }
         }
         // Gaussian elimination (SPD, small)
@@ -1094,7 +1150,7 @@ struct Oracle {
         for (int c = 0; c < L.n_cells; ++c)
           for (int q = 0; q < nq; ++q) {
             double v = 0;
-            for (int i = 0; i < nc_v; ++i) v += fe.pval[q * nc_v + i] * dg[l][(size_t)c * nc_v + i];
+            for (int i = 0; i < nc_v; ++i) v += fe.q1val[q * nc_v + i] * dg[l][(size_t)c * nc_v + i];
             L.eta[(size_t)c * nq + q] = std::clamp(v, eta_min, eta_max);
           }
       }
@@ -1691,6 +1747,16 @@ void* orc_create(int dim, int n_levels) {
   for (auto& L : h->levels) L.dim = dim;
   return h;
 }
+// velocity degree 2 (Q2-Q1) or 3 (Q3-Q2)
+void* orc_create_degree(int dim, int degree, int n_levels) {
+  if (degree != 2 && degree != 3) return nullptr;
+  Oracle* h = new Oracle();
+  h->dim = dim;
+  h->fe.init(dim, degree);
+  h->levels.resize(n_levels);
+  for (auto& L : h->levels) L.dim = dim;
+  return h;
+}
 void orc_destroy(void* p) { delete (Oracle*)p; }
 const char* orc_last_error(void* p) { return ((Oracle*)p)->err.c_str(); }
 // Newton / prescribed-dilation tables of the finest level (caller cell order, per
@@ -1734,6 +1800,7 @@ int orc_set_free_surface(void* p, int n, const int* cell, const int* fno, const 
   GUARD({
     const int nf = h->dim == 3 ? 9 : 3;
     h->fs = orc::Oracle::FreeSurface{};
+    if (n > 0 && h->fe.degree != 2) throw std::runtime_error("free-surface faces are built for velocity degree 2");
     if (n > 0) {
       h->fs.cell.assign(cell, cell + n);
       h->fs.fno.assign(fno, fno + n);
@@ -1768,7 +1835,7 @@ int orc_set_level_mesh(void* p, int lev, int n_cells, const int* cdu, const int*
     L.cdp.assign(cdp, cdp + (size_t)n_cells * h->fe.np);
     L.geom_kind = geom_kind;
     size_t ng = geom_kind == 0   ? (size_t)n_cells * 2 * h->dim
-                : geom_kind == 1 ? (size_t)n_cells * h->fe.nv * h->dim
+                : geom_kind == 1 ? (size_t)n_cells * h->fe.nm * h->dim
                                  : (size_t)n_cells * h->fe.nq * (h->dim * h->dim + 1);
     L.geom.assign(geom, geom + ng);
     L.cu.init(n_u); L.cp.init(n_p);
@@ -1900,6 +1967,7 @@ int orc_adjoint_gradient(void* p, const double* u, const double* lam, double* gr
     auto& L = h->fine();
     const auto& fe = h->fe;
     const int d = L.dim, nq = fe.nq, nv = fe.nv, nu = fe.nu;
+    if (fe.degree != 2) throw std::runtime_error("the adjoint gradient is built for velocity degree 2");
     for (int c = 0; c < L.n_cells; ++c) {
       double xu[81], xl[81];
       for (int i = 0; i < nu; ++i) {

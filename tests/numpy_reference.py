@@ -22,10 +22,10 @@ def constraint_matrix(n, cons):
 
 
 def element_data(level, eta_cell_q):
-    dim = level.dim
-    pts, w = fe.quadrature(dim, 3)
-    G = fe.shape_grads(dim, fe.Q2_NODES, pts)  # (nq, nv, dim) reference
-    psi = fe.shape_values(dim, fe.Q1_NODES, pts)
+    dim, deg = level.dim, getattr(level, "degree", 2)
+    pts, w = fe.quadrature(dim, deg + 1)
+    G = fe.shape_grads(dim, fe.velocity_nodes(deg), pts)  # (nq, nv, dim) reference
+    psi = fe.shape_values(dim, fe.pressure_nodes(deg), pts)
     J = level.jacobians(pts)  # (nc, nq, dim, dim)
     invJ = np.linalg.inv(J)
     jxw = np.abs(np.linalg.det(J)) * w[None, :]
@@ -36,7 +36,7 @@ def element_data(level, eta_cell_q):
 def stokes_blocks(level, eta_q, s, compressible=False):
     """Dense A (n_u x n_u), B^T-part (n_u x n_p: -s p div v), M (n_p x n_p: s^2/eta)."""
     dim = level.dim
-    nv = 3 ** dim
+    nv = (getattr(level, "degree", 2) + 1) ** dim
     grad, psi, jxw = element_data(level, eta_q)
     A = np.zeros((level.n_u, level.n_u))
     BT = np.zeros((level.n_u, level.n_p))

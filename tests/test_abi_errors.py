@@ -31,7 +31,7 @@ def test_solve_parameter_defaults_follow_the_reference(L):
 
 def test_create_rejects_invalid_shapes(L):
     h = ctypes.c_void_p(1)
-    for dim, deg, nl in [(1, 2, 3), (4, 2, 3), (3, 1, 3), (3, 3, 3), (3, 2, 0)]:
+    for dim, deg, nl in [(1, 2, 3), (4, 2, 3), (3, 1, 3), (3, 4, 3), (3, 2, 0)]:
         assert L.gb_gmg_create(None, dim, deg, nl, ctypes.byref(h)) == INVALID
         assert h.value is None
     assert L.gb_gmg_create(None, 3, 2, 3, None) == INVALID
