@@ -24,9 +24,14 @@
  *  - One host thread per handle. Each handle drives one GPU (the current CUDA
  *    device when gb_gmg_create is called).
  *  - Levels are numbered 0 (coarsest) .. n_levels-1 (finest = active mesh).
- *  - Cell-local DoF order: velocity FE_Q(2)^dim with components blocked and
- *    nodes lexicographic (x fastest): local = c*3^dim + lex(i,j[,k]), nodes at
- *    {0,1/2,1}; pressure FE_Q(1): local = lex(i,j[,k]), nodes at {0,1}.
+ *  - Cell-local DoF order: velocity FE_Q(k)^dim with components blocked and
+ *    nodes lexicographic (x fastest): local = c*(k+1)^dim + lex(i,j[,k]);
+ *    pressure FE_Q(k-1): local = lex(i,j[,k]). k = degree_v of gb_gmg_create:
+ *    2 (velocity nodes {0,1/2,1}, pressure {0,1}) or 3 (velocity nodes the
+ *    Gauss-Lobatto points {0, (1-1/sqrt5)/2, (1+1/sqrt5)/2, 1} as deal.II's FE_Q(3),
+ *    pressure {0,1/2,1}). Quadrature: QGauss(k+1), points lexicographic.
+ *    Degree 3 runs on indexed levels; the Newton / dilation and free-surface
+ *    terms, the device body force and the adjoint gradient are degree 2 only.
  *  - Pressure is the scaled unknown p/s on input and output, as in the
  *    reference (stokes_matrix_free_local_smoothing.cc:975,1421). Constraint
  *    distribution, p *= s, nullspace removal and pressure normalisation stay on
@@ -59,7 +64,7 @@ enum gb_gmg_status {
 enum gb_gmg_geometry {
   GB_GMG_GEOM_BOX = 0,  /* per cell: lower corner x0[dim], edge lengths h[dim]    */
   GB_GMG_GEOM_Q2 = 1,   /* per cell: 3^dim Q2 mapping support points [node][dim]  */
-  GB_GMG_GEOM_TABLE = 2 /* per cell and QGauss(3) point (lexicographic): the
+  GB_GMG_GEOM_TABLE = 2 /* per cell and QGauss(k+1) point (lexicographic): the
                            inverse Jacobian [d*dim+e] = d xi_d / d x_e, then
                            |det J|; dim*dim+1 values per point. The caller's own
                            mapping, e.g. ASPECT's MappingQCache of degree 4 on
@@ -161,13 +166,14 @@ typedef struct gb_gmg_outputs {
 void gb_gmg_default_options(gb_gmg_options* opt);
 void gb_gmg_default_solve_params(gb_gmg_solve_params* prm);
 
-/* Replaces create_matrix_free_solver (source/simulator/solver/stokes_matrix_free.cc:30-62). */
+/* Replaces create_matrix_free_solver (source/simulator/solver/stokes_matrix_free.cc:30-62):
+ * degree_v 2 (Q2-Q1) or 3 (Q3-Q2), the reference's two instantiations (:39-40,53-54). */
 int gb_gmg_create(const gb_gmg_options* opt, int dim, int degree_v, int n_levels, gb_gmg** out);
 void gb_gmg_destroy(gb_gmg* h);
 const char* gb_gmg_last_error(const gb_gmg* h);
 
 /* setup_dofs (stokes_matrix_free_global_coarsening.cc:1456-1636): one level's
- * cell-to-DoF maps (n_cells x dim*3^dim and n_cells x 2^dim, in the caller's
+ * cell-to-DoF maps (n_cells x dim*(k+1)^dim and n_cells x k^dim, in the caller's
  * numbering) and geometry (gb_gmg_geometry). */
 int gb_gmg_set_level_mesh(gb_gmg* h, int level, int64_t n_cells, const int32_t* cell_dofs_u,
                           const int32_t* cell_dofs_p, int geometry_kind, const double* cell_geometry,
@@ -192,8 +198,8 @@ int gb_gmg_set_transfer(gb_gmg* h, int level, const int32_t* child_to_parent, co
 int gb_gmg_finalize_setup(gb_gmg* h);
 
 /* assemble() -> evaluate_material_model (stokes_matrix_free_local_smoothing.cc:174-294):
- * finest-level viscosity, n_per_cell = 1 (averaged) or 3^dim (per quadrature
- * point, QGauss(3) lexicographic), in the caller's cell order; the level tables
+ * finest-level viscosity, n_per_cell = 1 (averaged) or (k+1)^dim (per quadrature
+ * point, QGauss(k+1) lexicographic), in the caller's cell order; the level tables
  * follow from `projection`. */
 int gb_gmg_set_viscosity(gb_gmg* h, const double* eta, int n_per_cell, int projection,
                          double pressure_scaling, int compressible);
