@@ -120,6 +120,9 @@ struct Handle {
   bool coarse_ready = false;
   // levels 0..mass_bottom_top of the FP32 mass V-cycle run in one single-block launch (-1: none)
   int mass_bottom_top = -1;
+  // levels 0..mass_dense_top of the FP32 mass V-cycle as one column-major matrix (-1: none)
+  int mass_dense_top = -1;
+  DevBuf<float> mass_dense;
 
   Level& top() { return levels.back(); }
   void reset_graphs() {
@@ -573,8 +576,8 @@ void coarse_dense(Handle& H, int block, T* sol, const T* def) {
 
 // Levels 0..K of the FP32 mass V-cycle as one launch (see mass_bottom.cu): the
 // same steps, coefficients and vectors as the multi-launch recursion below.
-void mass_bottom(Handle& H, int K) {
-  MassBottomArgs A{};
+void fill_mass_bottom(Handle& H, int K, MassBottomArgs& A) {
+  A = MassBottomArgs{};
   A.n_levels = K + 1;
   for (int l = 0; l <= K; ++l) {
     Level& L = H.levels[l];
@@ -612,6 +615,10 @@ void mass_bottom(Handle& H, int K) {
       rhok = rhokp;
     }
   }
+}
+void mass_bottom(Handle& H, int K) {
+  MassBottomArgs A;
+  fill_mass_bottom(H, K, A);
   launch_mass_vcycle_bottom(A, mass_bottom_layout(A), H.st);
   ++H.cell_launches;
 }
@@ -638,9 +645,60 @@ int plan_mass_bottom(const Handle& H) {
   return K;
 }
 
+// the highest level K whose cycle of levels 0..K becomes an explicit matrix
+// (options.dense_mass_cycle_nodes; same qualification as plan_mass_bottom)
+int plan_mass_dense(const Handle& H) {
+  const int max_nodes = std::min(H.opt.dense_mass_cycle_nodes, kMaxDenseBottomNodes);
+  if (H.opt.coarse_solver != GB_GMG_COARSE_CHEBYSHEV || max_nodes <= 0) return -1;
+  const int smem_limit = mass_bottom_reserve();
+  MassBottomArgs A{};
+  int K = -1;
+  for (int l = 0; l < H.n_levels && l < kMaxBottomLevels; ++l) {
+    const Level& L = H.levels[l];
+    const int degree = cheb_params(H, l).degree;
+    if (!L.structured || L.dim != 3 || L.n_p > max_nodes || degree < 1 || degree > kMaxBottomDegree) break;
+    A.n_levels = l + 1;
+    A.lev[l].L.n_cells = (int)L.n_cells;
+    A.lev[l].L.n_p = (int)L.n_p;
+    if (mass_bottom_layout(A) > smem_limit) break;
+    K = l;
+  }
+  return K;
+}
+
+// The FP32 mass cycle of levels 0..K is linear in its defect (Chebyshev steps
+// with fixed coefficients from a zero start, the smoother as the coarse solver),
+// so its matrix is the cycle applied to the unit vectors: one block per column,
+// each running the single-block cycle (batch mode of mass_vcycle_bottom). Built
+// after the eigenvalue estimates and again whenever they or the level tables change.
+void build_mass_dense(Handle& H) {
+  H.mass_dense_top = -1;
+  if (!H.prec_done[1]) return;
+  const int K = plan_mass_dense(H);
+  if (K < 0) {
+    H.mass_dense.release();
+    return;
+  }
+  const int n = (int)H.levels[K].n_p;
+  MassBottomArgs A;
+  fill_mass_bottom(H, K, A);
+  H.mass_dense.alloc((size_t)n * n);
+  A.batch_out = H.mass_dense.p;
+  launch_mass_vcycle_bottom_batch(A, mass_bottom_layout(A), n, H.st);
+  ++H.cell_launches;
+  GB_CUDA(cudaStreamSynchronize(H.st));
+  H.mass_dense_top = K;
+}
+
 template <typename T>
 void vcycle_level(Handle& H, int lev, int block) {
   if constexpr (std::is_same<T, float>::value) {
+    if (block == 1 && lev == H.mass_dense_top) {
+      const Level& L = H.levels[lev];
+      launch_dense_gemv_colmajor((int)L.n_p, H.mass_dense.p, L.f32.defM.p, H.levels[lev].f32.solM.p, H.st);
+      ++H.cell_launches;
+      return;
+    }
     if (block == 1 && lev <= H.mass_bottom_top) {
       mass_bottom(H, lev);
       return;
@@ -1465,6 +1523,7 @@ void gb_gmg_default_options(gb_gmg_options* o) {
   o->force_indexed_layout = 0;
   o->coarse_solver = GB_GMG_COARSE_CHEBYSHEV;
   o->fused_a_min_cells = 0;  // measured slower than the two-pass form (see ablock_fused.cu)
+  o->dense_mass_cycle_nodes = gb::kMaxDenseBottomNodes;
 }
 
 void gb_gmg_default_solve_params(gb_gmg_solve_params* p) {
@@ -1642,6 +1701,7 @@ int gb_gmg_set_viscosity(gb_gmg* g, const double* eta, int n_per_cell, int proje
     H.compressible = compressible;
     H.projection = projection;
     H.visc_done = false;
+    H.mass_dense_top = -1;  // rebuilt by build_preconditioner
     GB_CHECK(eta, 1, "null viscosity");
     gb::device_level_viscosity(H.levels, eta, n_per_cell, projection, s, H.eta_min, H.eta_max, H.st);
     H.visc_n_per_cell = n_per_cell;
@@ -1667,6 +1727,9 @@ int gb_gmg_update_viscosity(gb_gmg* g, const double* eta, int n_per_cell) {
     gb::device_level_viscosity(H.levels, eta, n_per_cell, H.projection, H.s, mn, mx, H.st);
     H.eta_min = mn;
     H.eta_max = mx;
+    // the explicit coarse mass cycle holds the levels' mass matrices (same size:
+    // same buffer, so captured V-cycles stay valid)
+    if (H.mass_dense_top >= 0) gb::build_mass_dense(H);
   })
 }
 
@@ -1818,6 +1881,7 @@ int gb_gmg_build_preconditioner(gb_gmg* g) {
     gb::build_preconditioner_T<float>(H);
     H.mass_bottom_top = gb::plan_mass_bottom(H);
     H.prec_done[1] = true;
+    gb::build_mass_dense(H);
   })
 }
 
@@ -2030,6 +2094,8 @@ int gb_gmg_set_eigenvalues(gb_gmg* g, int level, int block, int precision, const
     e[1] = mm[1];
     *given = true;
     g->h.reset_graphs();
+    // the explicit coarse mass cycle holds these coefficients
+    if (precision == GB_GMG_FP32 && block == 1 && level <= g->h.mass_dense_top) gb::build_mass_dense(g->h);
   })
 }
 

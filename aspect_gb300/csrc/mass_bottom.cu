@@ -95,7 +95,8 @@ __global__ void __launch_bounds__(kBottomThreads) mass_vcycle_bottom(const MassB
   if (threadIdx.x == 0) A = args;
   __syncthreads();
   const int K = A.n_levels - 1;
-  float* sol_out = A.lev[K].sol;
+  const int n_top = A.lev[K].L.n_p;
+  float* sol_out = A.batch_out ? A.batch_out + (size_t)blockIdx.x * n_top : A.lev[K].sol;
   // stage the mass matrices and diagonals of all levels and the top level's defect
   for (int l = 0; l <= K; ++l) {
     const MassBottomLevel& V = A.lev[l];
@@ -105,7 +106,8 @@ __global__ void __launch_bounds__(kBottomThreads) mass_vcycle_bottom(const MassB
     for (int i = threadIdx.x; i < n4; i += kBottomThreads) dst[i] = src[i];
     for (int i = threadIdx.x; i < V.L.n_p; i += kBottomThreads) sm[V.off[1] + i] = V.dinv[i];
   }
-  for (int i = threadIdx.x; i < A.lev[K].L.n_p; i += kBottomThreads) sm[A.lev[K].off[3] + i] = A.lev[K].def[i];
+  for (int i = threadIdx.x; i < n_top; i += kBottomThreads)
+    sm[A.lev[K].off[3] + i] = A.batch_out ? (i == (int)blockIdx.x ? 1.0f : 0.0f) : A.lev[K].def[i];
   __syncthreads();
   if (threadIdx.x == 0) {
     for (int l = 0; l <= K; ++l) {
@@ -186,6 +188,44 @@ int mass_bottom_reserve() {
 
 void launch_mass_vcycle_bottom(const MassBottomArgs& A, int smem_bytes, cudaStream_t s) {
   mass_vcycle_bottom<<<1, kBottomThreads, smem_bytes, s>>>(A);
+}
+
+void launch_mass_vcycle_bottom_batch(const MassBottomArgs& A, int smem_bytes, int n_cols, cudaStream_t s) {
+  if (n_cols <= 0 || !A.batch_out) return;
+  mass_vcycle_bottom<<<n_cols, kBottomThreads, smem_bytes, s>>>(A);
+  GB_CUDA(cudaGetLastError());
+}
+
+namespace {
+// 32 rows per block, the columns split over 16 warps: lane = row, warp = slice of
+// columns; the 16 partial sums of a row are added in slice order
+constexpr int kGemvSlices = 16;
+__global__ void __launch_bounds__(32 * kGemvSlices) dense_gemv_colmajor(int n, const float* __restrict__ B,
+                                                                       const float* __restrict__ x,
+                                                                       float* __restrict__ y) {
+  pdl_wait();
+  __shared__ float part[kGemvSlices][32];
+  const int lane = threadIdx.x & 31, slice = threadIdx.x >> 5;
+  const int row = blockIdx.x * 32 + lane;
+  const int chunk = (n + kGemvSlices - 1) / kGemvSlices;
+  const int j0 = slice * chunk, j1 = min(n, j0 + chunk);
+  float acc = 0.0f;
+  if (row < n)
+    for (int j = j0; j < j1; ++j) acc += B[(size_t)j * n + row] * x[j];
+  part[slice][lane] = acc;
+  __syncthreads();
+  if (slice == 0 && row < n) {
+    float t = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kGemvSlices; ++k) t += part[k][lane];
+    y[row] = t;
+  }
+}
+}  // namespace
+
+void launch_dense_gemv_colmajor(int n, const float* B, const float* x, float* y, cudaStream_t s) {
+  if (n <= 0) return;
+  dense_gemv_colmajor<<<(n + 31) / 32, 32 * kGemvSlices, 0, s>>>(n, B, x, y);
 }
 
 }  // namespace gb

@@ -44,7 +44,17 @@ struct MassBottomLevel {
 struct MassBottomArgs {
   int n_levels;  // levels 0 .. n_levels-1 of the hierarchy
   MassBottomLevel lev[kMaxBottomLevels];
+  // batch mode (non-null): block b runs the cycle on the unit vector e_b as the
+  // top level's defect and writes the result to column b (column-major, n x n,
+  // n = pressure nodes of the top level) instead of the top level's solution
+  float* batch_out;
 };
+
+// The cycle of levels 0..K as an explicit matrix: its columns (batch mode) are
+// computed once per preconditioner build, after which one dense product
+// replaces every launch of those levels. Levels of at most this many pressure
+// nodes qualify (the matrix is n x n floats).
+constexpr int kMaxDenseBottomNodes = 1000;
 
 // Fills lev[l].off for levels 0..n_levels-1 and returns the dynamic shared
 // memory the launch needs, in bytes.
@@ -53,5 +63,9 @@ int mass_bottom_layout(MassBottomArgs& A);
 // attribute the first time; call outside stream capture).
 int mass_bottom_reserve();
 void launch_mass_vcycle_bottom(const MassBottomArgs& A, int smem_bytes, cudaStream_t s);
+// batch mode: n_cols blocks, A.batch_out set
+void launch_mass_vcycle_bottom_batch(const MassBottomArgs& A, int smem_bytes, int n_cols, cudaStream_t s);
+// y = B x for a column-major n x n matrix B (fixed summation order)
+void launch_dense_gemv_colmajor(int n, const float* B, const float* x, float* y, cudaStream_t s);
 
 }  // namespace gb

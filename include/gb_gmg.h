@@ -121,6 +121,12 @@ typedef struct gb_gmg_options {
                                    with at least this many cells (and 16 x 8 | cells in
                                    x, y) run as one fused cell-and-gather pass (0: never,
                                    the default: the two-pass form measured faster)      */
+  int dense_mass_cycle_nodes;   /* FP32 Schur (pressure-mass) V-cycle: the sub-cycle of
+                                   the coarse lattice levels up to the highest one with
+                                   at most this many pressure nodes (<= 1000) is
+                                   computed once per preconditioner build as an explicit
+                                   matrix and applied as one dense product (1000; 0: off,
+                                   every level runs its own launches)                 */
 } gb_gmg_options;
 
 enum gb_gmg_coarse_solver {
