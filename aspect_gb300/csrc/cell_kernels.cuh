@@ -1053,10 +1053,7 @@ __global__ void __launch_bounds__(256) velocity_gather_structured(LevelView<T> L
 // summed in the same order as velocity_gather_structured (z, y, x; the lower
 // cell along a direction first), so the two give bit-identical sums.
 template <typename T, int epi>
-__global__ void __launch_bounds__(256) velocity_gather_lattice3(LevelView<T> L, GatherArgs<T> a) {
-  pdl_wait();
-  const int node = blockIdx.x * blockDim.x + threadIdx.x;
-  if (node >= L.n_nodes) return;
+__device__ __forceinline__ void velocity_lattice_node(const LevelView<T>& L, const GatherArgs<T>& a, int node) {
   const int nxy = L.Nn[0] * L.Nn[1];
   const int gz = node / nxy;
   const int rem = node - gz * nxy;
@@ -1105,6 +1102,13 @@ __global__ void __launch_bounds__(256) velocity_gather_lattice3(LevelView<T> L, 
       }
 #pragma unroll
   for (int c = 0; c < 3; ++c) gather_epilogue<T, epi>(a, (long)c * L.n_nodes + node, sum[c], cons[c]);
+}
+template <typename T, int epi>
+__global__ void __launch_bounds__(256) velocity_gather_lattice3(LevelView<T> L, GatherArgs<T> a) {
+  pdl_wait();
+  const int node = blockIdx.x * blockDim.x + threadIdx.x;
+  if (node >= L.n_nodes) return;
+  velocity_lattice_node<T, epi>(L, a, node);
 }
 
 // Pressure DoFs of a lattice level (never constrained there).

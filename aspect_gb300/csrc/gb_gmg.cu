@@ -29,6 +29,7 @@
 #include "../../include/gb_gmg.h"
 #include "level.cuh"
 #include "mass_bottom.cuh"
+#include "a_bottom.cuh"
 
 namespace gb {
 
@@ -123,6 +124,9 @@ struct Handle {
   // levels 0..mass_dense_top of the FP32 mass V-cycle as one column-major matrix (-1: none)
   int mass_dense_top = -1;
   DevBuf<float> mass_dense;
+  // the same for the FP32 A-block V-cycle
+  int a_dense_top = -1;
+  DevBuf<float> a_dense;
 
   Level& top() { return levels.back(); }
   void reset_graphs() {
@@ -690,9 +694,91 @@ void build_mass_dense(Handle& H) {
   H.mass_dense_top = K;
 }
 
+// The A-block counterpart: levels 0..K of 3D lattices with at most
+// options.dense_a_cycle_dofs velocity DoFs on level K and one viscosity layout
+void fill_a_bottom(Handle& H, int K, ABottomArgs& A) {
+  A = ABottomArgs{};
+  A.n_levels = K + 1;
+  A.eta_per_q = H.levels[0].eta_n > 1;
+  for (int l = 0; l <= K; ++l) {
+    Level& L = H.levels[l];
+    LevelDev<float>& D = L.f32;
+    ABottomLevel& V = A.lev[l];
+    V.L = L.view<float>(H.s, H.compressible);
+    V.dinv = D.dinvA.p;
+    if (l >= 1) {
+      V.pt_rows = (int)L.PuT_rows;
+      V.pt_ptr = L.PuT_ptr.p;
+      V.pt_col = L.PuT_col.p;
+      V.pt_val = D.PuT_val.p;
+      V.p_rows = (int)L.Pu_rows;
+      V.p_ptr = L.Pu_ptr.p;
+      V.p_col = L.Pu_col.p;
+      V.p_val = D.Pu_val.p;
+    }
+    const ChebParams cp = cheb_params(H, l);
+    double theta, delta;
+    chebyshev_bounds<float>(H, l, 0, theta, delta);
+    V.degree = cp.degree;
+    V.inv_theta = (float)(1.0 / theta);
+    double rhok = delta / theta;
+    const double sigma = theta / delta;
+    for (int k = 1; k < cp.degree; ++k) {
+      const double rhokp = 1.0 / (2.0 * sigma - rhok);
+      V.f1[k] = (float)(rhokp * rhok);
+      V.f2[k] = (float)(2.0 * rhokp / delta);
+      rhok = rhokp;
+    }
+  }
+}
+int plan_a_dense(const Handle& H) {
+  const int max_dofs = std::min(H.opt.dense_a_cycle_dofs, kMaxDenseANodes);
+  if (H.opt.coarse_solver != GB_GMG_COARSE_CHEBYSHEV || max_dofs <= 0) return -1;
+  const int smem_limit = a_bottom_reserve();
+  ABottomArgs A{};
+  int K = -1;
+  for (int l = 0; l < H.n_levels && l < kMaxABottomLevels; ++l) {
+    const Level& L = H.levels[l];
+    const int degree = cheb_params(H, l).degree;
+    if (!L.structured || L.dim != 3 || L.n_u > max_dofs || degree < 1 || degree > kMaxBottomDegree ||
+        (L.eta_n > 1) != (H.levels[0].eta_n > 1))
+      break;
+    A.n_levels = l + 1;
+    A.lev[l].L.n_cells = (int)L.n_cells;
+    A.lev[l].L.n_u = (int)L.n_u;
+    if (a_bottom_layout(A) > smem_limit) break;
+    K = l;
+  }
+  return K;
+}
+void build_a_dense(Handle& H) {
+  H.a_dense_top = -1;
+  if (!H.prec_done[1]) return;
+  const int K = plan_a_dense(H);
+  if (K < 0) {
+    H.a_dense.release();
+    return;
+  }
+  const int n = (int)H.levels[K].n_u;
+  ABottomArgs A;
+  fill_a_bottom(H, K, A);
+  H.a_dense.alloc((size_t)n * n);
+  A.batch_out = H.a_dense.p;
+  launch_a_vcycle_bottom_batch(A, a_bottom_layout(A), n, H.st);
+  ++H.cell_launches;
+  GB_CUDA(cudaStreamSynchronize(H.st));
+  H.a_dense_top = K;
+}
+
 template <typename T>
 void vcycle_level(Handle& H, int lev, int block) {
   if constexpr (std::is_same<T, float>::value) {
+    if (block == 0 && lev == H.a_dense_top) {
+      const Level& L = H.levels[lev];
+      launch_dense_gemv_colmajor((int)L.n_u, H.a_dense.p, L.f32.defA.p, H.levels[lev].f32.solA.p, H.st);
+      ++H.cell_launches;
+      return;
+    }
     if (block == 1 && lev == H.mass_dense_top) {
       const Level& L = H.levels[lev];
       launch_dense_gemv_colmajor((int)L.n_p, H.mass_dense.p, L.f32.defM.p, H.levels[lev].f32.solM.p, H.st);
@@ -1524,6 +1610,7 @@ void gb_gmg_default_options(gb_gmg_options* o) {
   o->coarse_solver = GB_GMG_COARSE_CHEBYSHEV;
   o->fused_a_min_cells = 0;  // measured slower than the two-pass form (see ablock_fused.cu)
   o->dense_mass_cycle_nodes = gb::kMaxDenseBottomNodes;
+  o->dense_a_cycle_dofs = gb::kMaxDenseANodes;
 }
 
 void gb_gmg_default_solve_params(gb_gmg_solve_params* p) {
@@ -1702,6 +1789,7 @@ int gb_gmg_set_viscosity(gb_gmg* g, const double* eta, int n_per_cell, int proje
     H.projection = projection;
     H.visc_done = false;
     H.mass_dense_top = -1;  // rebuilt by build_preconditioner
+    H.a_dense_top = -1;
     GB_CHECK(eta, 1, "null viscosity");
     gb::device_level_viscosity(H.levels, eta, n_per_cell, projection, s, H.eta_min, H.eta_max, H.st);
     H.visc_n_per_cell = n_per_cell;
@@ -1730,6 +1818,7 @@ int gb_gmg_update_viscosity(gb_gmg* g, const double* eta, int n_per_cell) {
     // the explicit coarse mass cycle holds the levels' mass matrices (same size:
     // same buffer, so captured V-cycles stay valid)
     if (H.mass_dense_top >= 0) gb::build_mass_dense(H);
+    if (H.a_dense_top >= 0) gb::build_a_dense(H);
   })
 }
 
@@ -1882,6 +1971,7 @@ int gb_gmg_build_preconditioner(gb_gmg* g) {
     H.mass_bottom_top = gb::plan_mass_bottom(H);
     H.prec_done[1] = true;
     gb::build_mass_dense(H);
+    gb::build_a_dense(H);
   })
 }
 
@@ -2096,6 +2186,7 @@ int gb_gmg_set_eigenvalues(gb_gmg* g, int level, int block, int precision, const
     g->h.reset_graphs();
     // the explicit coarse mass cycle holds these coefficients
     if (precision == GB_GMG_FP32 && block == 1 && level <= g->h.mass_dense_top) gb::build_mass_dense(g->h);
+    if (precision == GB_GMG_FP32 && block == 0 && level <= g->h.a_dense_top) gb::build_a_dense(g->h);
   })
 }
 

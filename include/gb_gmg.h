@@ -127,6 +127,9 @@ typedef struct gb_gmg_options {
                                    computed once per preconditioner build as an explicit
                                    matrix and applied as one dense product (1000; 0: off,
                                    every level runs its own launches)                 */
+  int dense_a_cycle_dofs;       /* the same for the FP32 A-block V-cycle: lattice levels
+                                   up to the highest one with at most this many velocity
+                                   DoFs (<= 2200; 2200; 0: off)                        */
 } gb_gmg_options;
 
 enum gb_gmg_coarse_solver {
