@@ -1031,32 +1031,7 @@ void ensure_krylov(Handle& H, int restart) {
   H.restart_alloc = restart;
 }
 
-// Device-side bookkeeping of classical Gram-Schmidt for Arnoldi step j.
-// pass 0: h[0..j] = dots, coef = -dots, arn[1] = sqrt(dots[j+1]) (|w| before);
-// pass 1 (only while *need2): h += dots, coef = -dots.
-__global__ void k_cgs_coef(int j, int pass, const double* __restrict__ dots, double* __restrict__ h,
-                           double* __restrict__ coef, double* __restrict__ arn, const int* __restrict__ need2) {
-  pdl_wait();
-  if (pass == 1 && *need2 == 0) return;
-  for (int i = threadIdx.x; i <= j; i += blockDim.x) {
-    const double v = dots[i];
-    h[i] = pass == 0 ? v : h[i] + v;
-    coef[i] = -v;
-  }
-  if (pass == 0 && threadIdx.x == 0) arn[1] = sqrt(dots[j + 1]);
-}
-// after w -= V coef and arn[0] = <w, w>: h[j+1] = |w| and arn[2] = 1 / |w| (1
-// when |w| = 0); pass 0 decides whether the second pass runs (|w| <= 0.7 |w before|)
-__global__ void k_cgs_norm(int j, int pass, double* __restrict__ h, double* __restrict__ arn,
-                           int* __restrict__ need2) {
-  pdl_wait();
-  if (pass == 1 && *need2 == 0) return;
-  const double nw = sqrt(arn[0]);
-  h[j + 1] = nw;
-  arn[2] = 1.0 / (nw > 0 ? nw : 1.0);
-  if (pass == 0) *need2 = nw > 0.7 * arn[1] ? 0 : 1;
-}
-// next basis vector v = w / h[j+1] (the reciprocal is formed once, in k_cgs_norm)
+// next basis vector v = w / h[j+1] (the reciprocal is formed once, in k_cgs_update)
 __global__ void k_next_basis(long n, const double* __restrict__ arn, const double* __restrict__ w,
                              double* __restrict__ v) {
   pdl_wait();
@@ -1111,17 +1086,11 @@ int gmres(Handle& H, double* x, const double* b, double tol, int maxit, int rest
       int* need2 = H.arn_flag.p;
       double* vnext = V + (size_t)(j + 1) * n;
       v_multidot(n, w, V, n, j + 1, true, H.dots_d.p, H.partial.p, H.st);
-      k_cgs_coef<<<1, 128, 0, H.st>>>(j, 0, H.dots_d.p, hcol, H.coef_d.p, arn, need2);
-      v_multiaxpy(n, j + 1, H.coef_d.p, V, n, w, H.st);
-      v_dot<double>(n, w, w, arn, H.partial.p, H.st);
-      k_cgs_norm<<<1, 1, 0, H.st>>>(j, 0, hcol, arn, need2);
+      v_cgs_update(n, j, 0, H.dots_d.p, V, n, w, hcol, arn, need2, H.partial.p, H.st);
       v_multidot(n, w, V, n, j + 1, false, H.dots_d.p, H.partial.p, H.st, need2);
-      k_cgs_coef<<<1, 128, 0, H.st>>>(j, 1, H.dots_d.p, hcol, H.coef_d.p, arn, need2);
-      v_multiaxpy(n, j + 1, H.coef_d.p, V, n, w, H.st, need2);
-      v_dot<double>(n, w, w, arn, H.partial.p, H.st, need2);
-      k_cgs_norm<<<1, 1, 0, H.st>>>(j, 1, hcol, arn, need2);
+      v_cgs_update(n, j, 1, H.dots_d.p, V, n, w, hcol, arn, need2, H.partial.p, H.st);
       k_next_basis<<<ceil_div(n, 256), 256, 0, H.st>>>(n, arn, w, vnext);
-      VecCounter::launches() += 5;
+      VecCounter::launches() += 1;
       GB_CUDA(cudaMemcpyAsync(H.dots_h, hcol, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, H.st));
       GB_CUDA(cudaStreamSynchronize(H.st));
       std::vector<double> h(H.dots_h, H.dots_h + j + 2);

@@ -245,12 +245,13 @@ __device__ __forceinline__ bool arrive_last(unsigned* counter) {
   if (last) __threadfence();
   return last;
 }
-__device__ __forceinline__ void finish_partials(const double* part, int nk, double* out, unsigned* counter) {
+__device__ __forceinline__ void finish_partials(const double* part, int nk, double* out, unsigned* counter,
+                                                int nb = kDotBlocks) {
   __shared__ double sh[kDotThreads / 32][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int j = wid; j < nk; j += kDotThreads / 32) {
     double t = 0;
-    for (int b = lane; b < kDotBlocks; b += 32) t += __ldcg(part + (size_t)j * kDotBlocks + b);
+    for (int b = lane; b < nb; b += 32) t += __ldcg(part + (size_t)j * nb + b);
     sh[wid][lane] = t;
     __syncwarp();
     if (lane == 0) {
@@ -263,7 +264,12 @@ __device__ __forceinline__ void finish_partials(const double* part, int nk, doub
   if (threadIdx.x == 0) *counter = 0u;
 }
 
-// blockIdx.y = chunk of kDotChunk vectors; the chunk that ends at k also forms <w, w>
+// blockIdx.y = chunk of kDotChunk vectors; the chunk that ends at k also forms
+// <w, w>. gridDim.x blocks per chunk (chosen so that all chunks run in about
+// one wave); each thread takes two elements per step, so eighteen independent
+// loads are in flight per thread. FP64 BLAS-1 on this GPU is bound by the
+// FP64 pipe (one FMA per basis entry), not by HBM, so keeping it fed is what
+// matters.
 __global__ void __launch_bounds__(kDotThreads) k_multidot(long n, const double* __restrict__ w,
                                                           const double* __restrict__ V, long ld, int k,
                                                           int with_norm, double* __restrict__ out,
@@ -271,6 +277,7 @@ __global__ void __launch_bounds__(kDotThreads) k_multidot(long n, const double* 
                                                           const int* __restrict__ active) {
   pdl_wait();
   if (active && *active == 0) return;
+  const int nb = gridDim.x;
   const int chunk = blockIdx.y;
   const int j0 = chunk * kDotChunk;
   const int kk = k - j0 < kDotChunk ? k - j0 : kDotChunk;
@@ -279,16 +286,46 @@ __global__ void __launch_bounds__(kDotThreads) k_multidot(long n, const double* 
   double acc[kDotChunk + 1];
 #pragma unroll
   for (int j = 0; j <= kDotChunk; ++j) acc[j] = 0;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+  const long stride = (long)nb * blockDim.x;
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  for (; i + stride < n; i += 2 * stride) {
+    const double wa = w[i], wb = w[i + stride];
+    double va[kDotChunk], vb[kDotChunk];
+#pragma unroll
+    for (int j = 0; j < kDotChunk; ++j)
+      if (j < kk) {
+        va[j] = Vc[j * ld + i];
+        vb[j] = Vc[j * ld + i + stride];
+      }
+#pragma unroll
+    for (int j = 0; j < kDotChunk; ++j)
+      if (j < kk) {
+        acc[j] += wa * va[j];
+        acc[j] += wb * vb[j];
+      }
+    if (norm) {
+      acc[kDotChunk] += wa * wa;
+      acc[kDotChunk] += wb * wb;
+    }
+  }
+  if (i < n) {
     const double wi = w[i];
 #pragma unroll
     for (int j = 0; j < kDotChunk; ++j)
       if (j < kk) acc[j] += wi * Vc[j * ld + i];
     if (norm) acc[kDotChunk] += wi * wi;
   }
-  double* part = partial + (size_t)chunk * (kDotChunk + 1) * kDotBlocks;
-  block_reduce_store<kDotChunk + 1>(acc, kk + norm, part, kDotBlocks, norm ? kk : -1);
-  if (arrive_last(counters + chunk)) finish_partials(part, kk + norm, out + j0, counters + chunk);
+  double* part = partial + (size_t)chunk * (kDotChunk + 1) * nb;
+  block_reduce_store<kDotChunk + 1>(acc, kk + norm, part, nb, norm ? kk : -1);
+  if (arrive_last(counters + chunk)) finish_partials(part, kk + norm, out + j0, counters + chunk, nb);
+}
+
+// blocks per chunk: about three resident blocks per SM over all chunks
+int multidot_blocks(int chunks) {
+  int nb = 3 * kDotBlocks / (chunks > 0 ? chunks : 1);
+  if (nb > kDotBlocks) nb = kDotBlocks;
+  if (nb < 32) nb = 32;
+  return nb;
 }
 
 void v_multidot(long n, const double* w, const double* V, long ld, int k, bool with_norm, double* out_dev,
@@ -305,10 +342,68 @@ void v_multidot(long n, const double* w, const double* V, long ld, int k, bool w
     const int kl = k - done < per_launch ? k - done : per_launch;
     const int norm = (with_norm && done + kl == k) ? 1 : 0;
     const int chunks = (kl + kDotChunk - 1) / kDotChunk;
-    k_multidot<<<dim3(kDotBlocks, chunks), kDotThreads, 0, s>>>(n, w, V + (size_t)done * ld, ld, kl, norm,
-                                                                out_dev + done, partial, counters, active);
+    k_multidot<<<dim3(multidot_blocks(chunks), chunks), kDotThreads, 0, s>>>(n, w, V + (size_t)done * ld, ld, kl,
+                                                                             norm, out_dev + done, partial,
+                                                                             counters, active);
     VecCounter::launches() += 1;
   }
+}
+
+// One classical Gram-Schmidt pass of Arnoldi step j after its multi-dot
+// (dots[0..j] = V^T w, and for pass 0 dots[j+1] = <w, w> before): w -= V dots
+// with <w, w> after formed in the same sweep (fixed-grid reduction); the block
+// that finishes the reduction also does the step's bookkeeping:
+//   pass 0: h[0..j] = dots, arn[1] = |w before|; pass 1: h[0..j] += dots;
+//   h[j+1] = |w| and arn[2] = 1 / |w| (1 when |w| = 0);
+//   pass 0: *need2 = 1 when |w| <= 0.7 |w before| (the second pass runs).
+// Pass 1 does nothing when *need2 == 0.
+constexpr int kCgsBlocks = 3 * kDotBlocks;
+__global__ void __launch_bounds__(kDotThreads) k_cgs_update(long n, int j, int pass, const double* __restrict__ dots,
+                                                            const double* __restrict__ V, long ld,
+                                                            double* __restrict__ w, double* __restrict__ h,
+                                                            double* __restrict__ arn, int* __restrict__ need2,
+                                                            double* __restrict__ partial, unsigned* counter) {
+  pdl_wait();
+  if (pass == 1 && *need2 == 0) return;
+  const int k = j + 1;
+  constexpr int kCached = 256;
+  __shared__ double c[kCached];
+  for (int i = threadIdx.x; i < k && i < kCached; i += blockDim.x) c[i] = -dots[i];
+  __syncthreads();
+  double acc[1] = {0};
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    double t = w[i];
+    int q = 0;
+    for (; q + 8 <= k; q += 8) {
+      double v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = V[(size_t)(q + u) * ld + i];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) t += (q + u < kCached ? c[q + u] : -dots[q + u]) * v[u];
+    }
+    for (; q < k; ++q) t += (q < kCached ? c[q] : -dots[q]) * V[(size_t)q * ld + i];
+    w[i] = t;
+    acc[0] += t * t;
+  }
+  block_reduce_store<1>(acc, 1, partial, gridDim.x);
+  if (!arrive_last(counter)) return;
+  finish_partials(partial, 1, arn, counter, gridDim.x);  // arn[0] = <w, w>
+  for (int i = threadIdx.x; i < k; i += blockDim.x) h[i] = pass == 0 ? dots[i] : h[i] + dots[i];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (pass == 0) arn[1] = sqrt(dots[k]);
+    const double nw = sqrt(arn[0]);
+    h[k] = nw;
+    arn[2] = 1.0 / (nw > 0 ? nw : 1.0);
+    if (pass == 0) *need2 = nw > 0.7 * arn[1] ? 0 : 1;
+  }
+}
+
+void v_cgs_update(long n, int j, int pass, const double* dots, const double* V, long ld, double* w, double* h,
+                  double* arn, int* need2, double* partial, cudaStream_t s) {
+  unsigned* counter = reinterpret_cast<unsigned*>(partial + kDotPartialDoubles) + kDotMaxChunks;
+  k_cgs_update<<<kCgsBlocks, kDotThreads, 0, s>>>(n, j, pass, dots, V, ld, w, h, arn, need2, partial, counter);
+  VecCounter::launches() += 1;
 }
 
 template <typename T>
@@ -330,13 +425,31 @@ void v_dot(long n, const T* a, const T* b, double* out_dev, double* partial, cud
   VecCounter::launches() += 1;
 }
 
-__global__ void k_multiaxpy(long n, int k, const double* __restrict__ coef, const double* __restrict__ V, long ld,
-                            double* __restrict__ w, const int* __restrict__ active) {
+// w += V coef. The basis entries of a row are loaded eight at a time before
+// they are summed (in order j = 0, 1, ...), so eight independent loads per
+// thread are in flight instead of one dependent load per step; the sums are
+// the same as the one-at-a-time loop's.
+constexpr int kAxpyBatch = 8;
+__global__ void __launch_bounds__(kThreads) k_multiaxpy(long n, int k, const double* __restrict__ coef,
+                                                        const double* __restrict__ V, long ld,
+                                                        double* __restrict__ w, const int* __restrict__ active) {
   pdl_wait();
   if (active && *active == 0) return;
+  constexpr int kCached = 256;
+  __shared__ double c[kCached];
+  for (int j = threadIdx.x; j < k && j < kCached; j += blockDim.x) c[j] = coef[j];
+  __syncthreads();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     double t = w[i];
-    for (int j = 0; j < k; ++j) t += coef[j] * V[j * ld + i];
+    int j = 0;
+    for (; j + kAxpyBatch <= k; j += kAxpyBatch) {
+      double v[kAxpyBatch];
+#pragma unroll
+      for (int u = 0; u < kAxpyBatch; ++u) v[u] = V[(size_t)(j + u) * ld + i];
+#pragma unroll
+      for (int u = 0; u < kAxpyBatch; ++u) t += (j + u < kCached ? c[j + u] : coef[j + u]) * v[u];
+    }
+    for (; j < k; ++j) t += (j < kCached ? c[j] : coef[j]) * V[(size_t)j * ld + i];
     w[i] = t;
   }
 }

@@ -67,6 +67,9 @@ void v_spmv_set(long rows, long n, const int* ptr, const int* col, const T* val,
 // partial: the reduction workspace (kDotWorkspaceDoubles, zeroed once)
 void v_multidot(long n, const double* w, const double* V, long ld, int k, bool with_norm, double* out_dev,
                 double* partial, cudaStream_t s, const int* active = nullptr);
+// one classical Gram-Schmidt pass of an Arnoldi step after its multi-dot (see vec.cu)
+void v_cgs_update(long n, int j, int pass, const double* dots, const double* V, long ld, double* w, double* h,
+                  double* arn, int* need2, double* partial, cudaStream_t s);
 template <typename T>
 void v_dot(long n, const T* a, const T* b, double* out_dev, double* partial, cudaStream_t s,
            const int* active = nullptr);
