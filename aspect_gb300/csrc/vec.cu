@@ -214,20 +214,30 @@ void v_spmv_set(long rows, long n, const int* ptr, const int* col, const T* val,
 template <int K>
 __device__ __forceinline__ void block_reduce_store(double (&acc)[K], int nk, double* partial, int slot_stride,
                                                    int moved = -1) {
-  __shared__ double sh[K][kDotThreads / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  // Through shared memory rather than a shuffle tree per value: on this GPU the
+  // FP64 additions are the cost, and a tree does five warp-wide additions per
+  // value in every warp; here 8 segments of 32 threads are summed by nk x 8
+  // threads, then each value's 8 segment sums by one thread (fixed order).
+  __shared__ double sh[K][kDotThreads];
+  __shared__ double seg[K][kDotThreads / 32];
 #pragma unroll
-  for (int j = 0; j < K; ++j) {
-    double v = acc[j];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) sh[j][wid] = v;
+  for (int j = 0; j < K; ++j) sh[j][threadIdx.x] = acc[j];
+  __syncthreads();
+  constexpr int nseg = kDotThreads / 32;
+  if ((int)threadIdx.x < nk * nseg) {
+    const int o = threadIdx.x / nseg, sg = threadIdx.x % nseg;
+    const int src = o == moved ? K - 1 : o;
+    double t = 0;
+#pragma unroll 8
+    for (int l = 0; l < 32; ++l) t += sh[src][sg * 32 + l];
+    seg[src][sg] = t;
   }
   __syncthreads();
-  if (threadIdx.x < nk) {
+  if ((int)threadIdx.x < nk) {
     const int src = (int)threadIdx.x == moved ? K - 1 : (int)threadIdx.x;
     double t = 0;
-    for (int w = 0; w < kDotThreads / 32; ++w) t += sh[src][w];
+#pragma unroll
+    for (int w = 0; w < nseg; ++w) t += seg[src][w];
     partial[threadIdx.x * slot_stride + blockIdx.x] = t;
   }
 }
@@ -250,8 +260,20 @@ __device__ __forceinline__ void finish_partials(const double* part, int nk, doub
   __shared__ double sh[kDotThreads / 32][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int j = wid; j < nk; j += kDotThreads / 32) {
+    // lane l adds blocks l, l + 32, ... in that order; eight loads are issued
+    // before they are added, so the finishing block does not wait on one load
+    // at a time
     double t = 0;
-    for (int b = lane; b < nb; b += 32) t += __ldcg(part + (size_t)j * nb + b);
+    const double* pj = part + (size_t)j * nb;
+    int b = lane;
+    for (; b + 7 * 32 < nb; b += 8 * 32) {
+      double v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = __ldcg(pj + b + u * 32);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) t += v[u];
+    }
+    for (; b < nb; b += 32) t += __ldcg(pj + b);
     sh[wid][lane] = t;
     __syncwarp();
     if (lane == 0) {
@@ -270,7 +292,7 @@ __device__ __forceinline__ void finish_partials(const double* part, int nk, doub
 // loads are in flight per thread. FP64 BLAS-1 on this GPU is bound by the
 // FP64 pipe (one FMA per basis entry), not by HBM, so keeping it fed is what
 // matters.
-__global__ void __launch_bounds__(kDotThreads) k_multidot(long n, const double* __restrict__ w,
+__global__ void __launch_bounds__(kDotThreads, 3) k_multidot(long n, const double* __restrict__ w,
                                                           const double* __restrict__ V, long ld, int k,
                                                           int with_norm, double* __restrict__ out,
                                                           double* __restrict__ partial, unsigned* counters,
@@ -320,11 +342,14 @@ __global__ void __launch_bounds__(kDotThreads) k_multidot(long n, const double* 
   if (arrive_last(counters + chunk)) finish_partials(part, kk + norm, out + j0, counters + chunk, nb);
 }
 
-// blocks per chunk: about three resident blocks per SM over all chunks
+// Blocks per chunk: all chunks together about 3 x kDotBlocks blocks (three
+// resident per SM at 70 registers), at most kDotBlocks per chunk. FP64
+// arithmetic (one FMA per basis entry) bounds the multi-dot on this GPU, so the
+// grid aims at an even share of it per SM.
 int multidot_blocks(int chunks) {
   int nb = 3 * kDotBlocks / (chunks > 0 ? chunks : 1);
   if (nb > kDotBlocks) nb = kDotBlocks;
-  if (nb < 32) nb = 32;
+  if (nb < 1) nb = 1;
   return nb;
 }
 
@@ -356,8 +381,11 @@ void v_multidot(long n, const double* w, const double* V, long ld, int k, bool w
 //   pass 0: h[0..j] = dots, arn[1] = |w before|; pass 1: h[0..j] += dots;
 //   h[j+1] = |w| and arn[2] = 1 / |w| (1 when |w| = 0);
 //   pass 0: *need2 = 1 when |w| <= 0.7 |w before| (the second pass runs).
-// Pass 1 does nothing when *need2 == 0.
-constexpr int kCgsBlocks = 3 * kDotBlocks;
+// Pass 1 does nothing when *need2 == 0. kCgsPerThread elements per thread in
+// full warps (a partly filled warp costs the FP64 pipe as much as a full one);
+// the coefficients are read from shared memory and subtracted (no negated copy).
+constexpr int kCgsPerThread = 4;
+constexpr int kCgsCached = 1024;
 __global__ void __launch_bounds__(kDotThreads) k_cgs_update(long n, int j, int pass, const double* __restrict__ dots,
                                                             const double* __restrict__ V, long ld,
                                                             double* __restrict__ w, double* __restrict__ h,
@@ -366,22 +394,24 @@ __global__ void __launch_bounds__(kDotThreads) k_cgs_update(long n, int j, int p
   pdl_wait();
   if (pass == 1 && *need2 == 0) return;
   const int k = j + 1;
-  constexpr int kCached = 256;
-  __shared__ double c[kCached];
-  for (int i = threadIdx.x; i < k && i < kCached; i += blockDim.x) c[i] = -dots[i];
+  const int kc = k < kCgsCached ? k : kCgsCached;
+  __shared__ double c[kCgsCached];
+  for (int i = threadIdx.x; i < kc; i += blockDim.x) c[i] = dots[i];
   __syncthreads();
   double acc[1] = {0};
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += stride) {
     double t = w[i];
     int q = 0;
-    for (; q + 8 <= k; q += 8) {
+    for (; q + 8 <= kc; q += 8) {
       double v[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) v[u] = V[(size_t)(q + u) * ld + i];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) t += (q + u < kCached ? c[q + u] : -dots[q + u]) * v[u];
+      for (int u = 0; u < 8; ++u) t -= c[q + u] * v[u];
     }
-    for (; q < k; ++q) t += (q < kCached ? c[q] : -dots[q]) * V[(size_t)q * ld + i];
+    for (; q < kc; ++q) t -= c[q] * V[(size_t)q * ld + i];
+    for (; q < k; ++q) t -= dots[q] * V[(size_t)q * ld + i];
     w[i] = t;
     acc[0] += t * t;
   }
@@ -402,7 +432,11 @@ __global__ void __launch_bounds__(kDotThreads) k_cgs_update(long n, int j, int p
 void v_cgs_update(long n, int j, int pass, const double* dots, const double* V, long ld, double* w, double* h,
                   double* arn, int* need2, double* partial, cudaStream_t s) {
   unsigned* counter = reinterpret_cast<unsigned*>(partial + kDotPartialDoubles) + kDotMaxChunks;
-  k_cgs_update<<<kCgsBlocks, kDotThreads, 0, s>>>(n, j, pass, dots, V, ld, w, h, arn, need2, partial, counter);
+  long nb = (n + (long)kDotThreads * kCgsPerThread - 1) / ((long)kDotThreads * kCgsPerThread);
+  const long max_nb = kDotPartialDoubles;  // one partial per block
+  if (nb > max_nb) nb = max_nb;
+  if (nb < 1) nb = 1;
+  k_cgs_update<<<(int)nb, kDotThreads, 0, s>>>(n, j, pass, dots, V, ld, w, h, arn, need2, partial, counter);
   VecCounter::launches() += 1;
 }
 
