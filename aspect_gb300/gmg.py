@@ -385,7 +385,8 @@ class StokesMatrixFreeGPU:
 
 def from_problem(problem, options: dict | None = None, build: bool = True) -> StokesMatrixFreeGPU:
     """Set up a solver for a :class:`aspect_gb300.problems.StokesProblem`."""
-    s = StokesMatrixFreeGPU(problem.levels[0].dim, len(problem.levels), options)
+    s = StokesMatrixFreeGPU(problem.levels[0].dim, len(problem.levels), options,
+                            degree=getattr(problem.levels[0], "degree", 2))
     s.setup_dofs(problem.levels)
     s.assemble(problem.eta, problem.projection, problem.pressure_scaling)
     if build:

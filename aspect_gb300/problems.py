@@ -258,17 +258,17 @@ def sinker_density(x: np.ndarray, centres: np.ndarray, radius: float = 0.075) ->
 
 
 def sinkers_3d(n: int = 32, seed: int = BASE_SEED + 2, projection: int = 1,
-               n_coarse: int = 1) -> StokesProblem:
+               n_coarse: int = 1, degree: int = 2) -> StokesProblem:
     """3D unit cube, n^3 Q2-Q1 cells, 8 smooth sinkers (centres seeded uniform in
     [0.2, 0.8]^3), eta = 1e-6 + (1-1e-6) prod_i(...) (1e6 contrast), rho = 1
     inside r = 0.075, g = -z,
     free slip. ``projection`` = 1 uses ASPECT's default averaging for GMG
     (project to Q1 only viscosity: per-quadrature-point viscosity); 0 uses the
-    harmonic cell average."""
-    levels = box_hierarchy(3, n, n_coarse=n_coarse)
+    harmonic cell average. ``degree`` 3: Q3-Q2 elements, QGauss(4)."""
+    levels = box_hierarchy(3, n, n_coarse=n_coarse, degree=degree)
     fine = levels[-1]
     centres = sinker_centres(seed)
-    xq, jxw = q_points_real(fine)
+    xq, jxw = q_points_real(fine, degree + 1)
     eta_q = sinker_viscosity(xq, centres)
     eta = eta_q if projection == 1 else harmonic_average(eta_q)
     rho = sinker_density(xq, centres)
@@ -277,8 +277,8 @@ def sinkers_3d(n: int = 32, seed: int = BASE_SEED + 2, projection: int = 1,
     rhs = assemble_rhs(fine, force)
     mid = fine.map_points(np.full((1, 3), 0.5))[:, 0, :]
     s = pressure_scaling(fine, sinker_viscosity(mid, centres), 0.01)
-    return StokesProblem(f"sinkers_{n}^3", levels, eta, projection, s, rhs, 2,
-                         extra=dict(centres=centres, seed=seed))
+    name = f"sinkers_{n}^3" + ("" if degree == 2 else f"_Q{degree}Q{degree - 1}")
+    return StokesProblem(name, levels, eta, projection, s, rhs, 2, extra=dict(centres=centres, seed=seed))
 
 
 def adaptive_sphere(base_depth: int = 4, n_adaptive: int = 2, radius: float = 0.2,

@@ -600,6 +600,19 @@ def _config_line(name):
         return _solve_pair(problems.solcx(6, density_sign=1.0))
     if name == "sphere16":
         return _solve_pair(problems.adaptive_sphere(4, 2))
+    if name == "sinkers16q3":
+        # velocity degree 3 (Q3-Q2, QGauss(4)) on the sinker workload at 16^3 cells
+        # (the pressure space of the 32^3 Q2-Q1 workload); operator timings beside
+        P = problems.sinkers_3d(16, degree=3)
+        line = _solve_pair(P, oracle_residual=True)
+        g = gmg.from_problem(P)
+        ops = {"stokes_vmult_fp64": g.time_operation(gmg.TIME_STOKES_VMULT, gmg.FP64, 20),
+               "stokes_vmult_fp32": g.time_operation(gmg.TIME_STOKES_VMULT, gmg.FP32, 20),
+               "A_vmult_fp32": g.time_operation(gmg.TIME_A_VMULT, gmg.FP32, 20)}
+        n = P.fine.n_u + P.fine.n_p
+        line["operator_seconds"] = ops
+        line["operator_gdofs"] = {k: (n if k.startswith("stokes") else P.fine.n_u) / v / 1e9 for k, v in ops.items()}
+        return line
     if name in ("shell3", "shell3a"):
         # refinement 3, and for shell3a one adaptive level on the temperature gradient
         t0 = time.perf_counter()
@@ -654,7 +667,7 @@ def main():
     ap.add_argument("--profile-op", default=None, choices=sorted(PROFILE_OPS))
     ap.add_argument("--sweep", default=None, help="comma-separated cells per direction, e.g. 32,64")
     ap.add_argument("--configs", default=None,
-                    help="comma-separated: solcx64,sphere16,adjoint32,shell3,shell3a")
+                    help="comma-separated: solcx64,sphere16,sinkers16q3,adjoint32,shell3,shell3a")
     args = ap.parse_args()
     if args.configs:
         run_configs(args.configs.split(","))
