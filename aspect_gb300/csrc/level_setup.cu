@@ -543,7 +543,14 @@ void setup_transfer(Level& F, const Level& C) {
     const HostCons& CC = block == 0 ? C.cu : C.cp;
     const std::vector<int>& fperm = block == 0 ? F.perm_u : F.perm_p;
     const std::vector<int>& cperm = block == 0 ? C.perm_u : C.perm_p;
-    std::vector<std::map<int, double>> rows(nf);
+    // each fine DoF's entries are appended once, contiguously (the DoF is
+    // handled when first met), then sorted by internal column and merged below
+    std::vector<long> seg_begin(nf, -1);
+    std::vector<int> seg_len(nf, 0);
+    std::vector<int> ecol;
+    std::vector<double> eval;
+    ecol.reserve((size_t)nf * 8);
+    eval.reserve((size_t)nf * 8);
     std::vector<char> done(nf, 0);
     for (long fc = 0; fc < F.n_cells; ++fc) {
       const int pc = F.parent[fc], ch = F.child[fc];
@@ -567,26 +574,47 @@ void setup_transfer(Level& F, const Level& C) {
           const int gf = block == 0 ? F.cdu[fc * nu + comp * nl + n] : F.cdp[fc * np + n];
           if (FC.constrained(gf) || done[gf]) continue;
           done[gf] = 1;
+          seg_begin[gf] = (long)ecol.size();
           for (int m = 0; m < nl; ++m) {
             if (std::fabs(phi[m]) < 1e-14) continue;
             const int gc = block == 0 ? C.cdu[(long)pc * nu + comp * nl + m] : C.cdp[(long)pc * np + m];
             Expansion e = expand(CC, gc);
-            for (int k = 0; k < e.n; ++k) rows[gf][e.g[k]] += phi[m] * e.w[k];
+            for (int k = 0; k < e.n; ++k) {
+              ecol.push_back(e.g[k]);
+              eval.push_back(phi[m] * e.w[k]);
+            }
           }
+          seg_len[gf] = (int)((long)ecol.size() - seg_begin[gf]);
         }
       }
     }
-    // internal numbering
-    std::vector<std::map<int, double>> irows(nf);
-    for (long g = 0; g < nf; ++g)
-      for (auto& kv : rows[g]) irows[fperm[g]][cperm[kv.first]] += kv.second;
+    // internal numbering: rows in internal order, each row's entries sorted by
+    // internal column (a stable sort, so repeated columns are summed in the
+    // order they were generated), entries of magnitude <= 1e-14 dropped
+    std::vector<long> caller_of(nf);
+    for (long g = 0; g < nf; ++g) caller_of[fperm[g]] = g;
     Csr P;
+    P.col.reserve(ecol.size());
+    P.val.reserve(ecol.size());
+    std::vector<std::pair<int, double>> row;
     for (long r = 0; r < nf; ++r) {
-      for (auto& kv : irows[r])
-        if (std::fabs(kv.second) > 1e-14) {
-          P.col.push_back(kv.first);
-          P.val.push_back(kv.second);
+      const long g = caller_of[r];
+      if (seg_begin[g] >= 0) {
+        row.clear();
+        for (long q = seg_begin[g]; q < seg_begin[g] + seg_len[g]; ++q) row.push_back({cperm[ecol[q]], eval[q]});
+        std::stable_sort(row.begin(), row.end(),
+                         [](const std::pair<int, double>& a, const std::pair<int, double>& b) { return a.first < b.first; });
+        for (size_t q = 0; q < row.size();) {
+          double v = 0;
+          size_t q2 = q;
+          for (; q2 < row.size() && row[q2].first == row[q].first; ++q2) v += row[q2].second;
+          if (std::fabs(v) > 1e-14) {
+            P.col.push_back(row[q].first);
+            P.val.push_back(v);
+          }
+          q = q2;
         }
+      }
       P.ptr.push_back((int)P.col.size());
     }
     Csr PT = P.transpose(block == 0 ? C.n_u : C.n_p);
