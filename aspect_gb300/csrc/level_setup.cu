@@ -556,6 +556,13 @@ void setup_transfer(Level& F, const Level& C) {
       const int pc = F.parent[fc], ch = F.child[fc];
       GB_CHECK(pc >= 0 && pc < C.n_cells, 1, "parent index out of range");
       for (int n = 0; n < nl; ++n) {
+        // a node shared with an earlier cell is done for every component
+        bool any = false;
+        for (int comp = 0; comp < ncomp && !any; ++comp) {
+          const int gf = block == 0 ? F.cdu[fc * nu + comp * nl + n] : F.cdp[fc * np + n];
+          any = !FC.constrained(gf) && !done[gf];
+        }
+        if (!any) continue;
         double xi[3];
         for (int e = 0; e < d; ++e) {
           const int idx = (e == 0 ? n : e == 1 ? n / n1 : n / (n1 * n1)) % n1;
@@ -578,6 +585,11 @@ void setup_transfer(Level& F, const Level& C) {
           for (int m = 0; m < nl; ++m) {
             if (std::fabs(phi[m]) < 1e-14) continue;
             const int gc = block == 0 ? C.cdu[(long)pc * nu + comp * nl + m] : C.cdp[(long)pc * np + m];
+            if (!CC.constrained(gc)) {  // the common case: the DoF itself, weight 1
+              ecol.push_back(gc);
+              eval.push_back(phi[m] * 1.0);
+              continue;
+            }
             Expansion e = expand(CC, gc);
             for (int k = 0; k < e.n; ++k) {
               ecol.push_back(e.g[k]);
@@ -602,8 +614,13 @@ void setup_transfer(Level& F, const Level& C) {
       if (seg_begin[g] >= 0) {
         row.clear();
         for (long q = seg_begin[g]; q < seg_begin[g] + seg_len[g]; ++q) row.push_back({cperm[ecol[q]], eval[q]});
-        std::stable_sort(row.begin(), row.end(),
-                         [](const std::pair<int, double>& a, const std::pair<int, double>& b) { return a.first < b.first; });
+        // stable insertion sort (rows hold a few dozen entries)
+        for (size_t q = 1; q < row.size(); ++q) {
+          const std::pair<int, double> x = row[q];
+          size_t z = q;
+          for (; z > 0 && row[z - 1].first > x.first; --z) row[z] = row[z - 1];
+          row[z] = x;
+        }
         for (size_t q = 0; q < row.size();) {
           double v = 0;
           size_t q2 = q;
