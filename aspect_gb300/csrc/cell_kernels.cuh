@@ -299,7 +299,7 @@ __device__ __forceinline__ void velocity_cell_op(const LevelView<T>& L, int cell
     if (need_u) {
       if constexpr (dim == 3) {
         const int k1 = (comp + 1) % 3, k2 = (comp + 2) % 3;
-        // round 1: receive d_comp u_{comp+1}; round 2: receive d_comp u_{comp+2}
+        // first exchange: receive d_comp u_{comp+1}; second: receive d_comp u_{comp+2}
         const T send1 = sel3(g[0], g[1], g[2], k2);
         const T send2 = sel3(g[0], g[1], g[2], k1);
         const T r1 = __shfl_sync(full, send1, l1);
