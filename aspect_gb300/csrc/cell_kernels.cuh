@@ -56,6 +56,8 @@ struct LevelView {
   const T* gtab;        // [n_cells][nq][dim*dim+1]: invJ (dxi_d/dx_e at [d*dim+e]), JxW/w_q
   const T* eta;         // [n_cells][eta_n]
   int eta_n;
+  const T* Mp;          // per-cell pressure mass matrices of the level table ([cell][np][np], internal
+                        // order), or null: the mass cell pass integrates at the quadrature points
   T s;                  // pressure scaling
   int compressible;
 };
@@ -930,6 +932,27 @@ __global__ void __launch_bounds__(kSmallCellThreads) lattice_cell_kernel_small(L
   if (act) Eu[(size_t)(c * 27 + n) * L.n_cells + cell] = A[cur][t];
 }
 
+// (generic loads: the rows may live in global or in shared memory)
+template <typename T, int np>
+__device__ __forceinline__ void load_row(const T* __restrict__ row, T (&r)[np]) {
+  if constexpr (sizeof(T) == 4 && np % 4 == 0) {
+#pragma unroll
+    for (int j = 0; j < np; j += 4) {
+      const float4 v = *reinterpret_cast<const float4*>(row + j);
+      r[j] = v.x; r[j + 1] = v.y; r[j + 2] = v.z; r[j + 3] = v.w;
+    }
+  } else if constexpr (sizeof(T) == 8 && np % 2 == 0) {
+#pragma unroll
+    for (int j = 0; j < np; j += 2) {
+      const double2 v = *reinterpret_cast<const double2*>(row + j);
+      r[j] = v.x; r[j + 1] = v.y;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < np; ++j) r[j] = row[j];
+  }
+}
+
 template <typename T, int dim>
 __global__ void __launch_bounds__(128) mass_cell_kernel(LevelView<T> L, const T* __restrict__ src_p,
                                                          T* __restrict__ Ep) {
@@ -944,13 +967,26 @@ __global__ void __launch_bounds__(128) mass_cell_kernel(LevelView<T> L, const T*
   for (int n = 0; n < np; ++n)
     P[n] = L.structured ? src_p[sc.pnode0 + structured_pnode_offset<dim>(L.Np, n)]
                         : gather_general(src_p, L.cdp[(size_t)cell * np + n], L.plptr, L.plcol, L.plw);
-  T box[4] = {T(0), T(0), T(0), T(0)};
-  if (L.geom == GEOM_BOX)
+  if (L.Mp) {  // the cell's matrix of the level table: np x np multiply-adds, no geometry reads
+    const T* __restrict__ M = L.Mp + (size_t)cell * np * np;
 #pragma unroll
-    for (int d = 0; d <= dim; ++d) box[d] = L.gbox[(size_t)cell * (dim + 1) + d];
-  const T eta_cell = L.eta_n == 1 ? L.eta[cell] : T(1);
-  const T* eta_q = L.eta_n == 1 ? nullptr : L.eta + (size_t)cell * L.eta_n;
-  mass_cell_op<T, dim>(L, cell, P, YP, box, eta_cell, eta_q);
+    for (int i = 0; i < np; ++i) {
+      T r[np];
+      load_row<T, np>(M + i * np, r);
+      T t = T(0);
+#pragma unroll
+      for (int j = 0; j < np; ++j) t += r[j] * P[j];
+      YP[i] = t;
+    }
+  } else {
+    T box[4] = {T(0), T(0), T(0), T(0)};
+    if (L.geom == GEOM_BOX)
+#pragma unroll
+      for (int d = 0; d <= dim; ++d) box[d] = L.gbox[(size_t)cell * (dim + 1) + d];
+    const T eta_cell = L.eta_n == 1 ? L.eta[cell] : T(1);
+    const T* eta_q = L.eta_n == 1 ? nullptr : L.eta + (size_t)cell * L.eta_n;
+    mass_cell_op<T, dim>(L, cell, P, YP, box, eta_cell, eta_q);
+  }
 #pragma unroll
   for (int n = 0; n < np; ++n) Ep[(size_t)cell * np + n] = YP[n];
 }
@@ -1151,27 +1187,6 @@ __global__ void __launch_bounds__(256) pressure_gather_structured(LevelView<T> L
 // nodes, so a Chebyshev step writes its new iterate to a separate vector
 // (EPI_CHEB_OUT).
 constexpr int kMassLatticeThreads = 256;
-
-// (generic loads: the rows may live in global or in shared memory)
-template <typename T, int np>
-__device__ __forceinline__ void load_row(const T* __restrict__ row, T (&r)[np]) {
-  if constexpr (sizeof(T) == 4 && np % 4 == 0) {
-#pragma unroll
-    for (int j = 0; j < np; j += 4) {
-      const float4 v = *reinterpret_cast<const float4*>(row + j);
-      r[j] = v.x; r[j + 1] = v.y; r[j + 2] = v.z; r[j + 3] = v.w;
-    }
-  } else if constexpr (sizeof(T) == 8 && np % 2 == 0) {
-#pragma unroll
-    for (int j = 0; j < np; j += 2) {
-      const double2 v = *reinterpret_cast<const double2*>(row + j);
-      r[j] = v.x; r[j + 1] = v.y;
-    }
-  } else {
-#pragma unroll
-    for (int j = 0; j < np; ++j) r[j] = row[j];
-  }
-}
 
 // Task t = (node t / 2^dim, cell slot t % 2^dim). All 32 lanes of a warp must
 // call it together (the lanes of a node are summed with shuffles); tasks past

@@ -181,6 +181,32 @@ __global__ void k_mass_matrices(long n_cells, int eta_n, const double* __restric
   }
 }
 
+// per-cell pressure mass matrices of an indexed level (internal cell order):
+// JxW from the level's box table (|det J|) or per-point geometry table
+template <int dim>
+__global__ void k_mass_matrices_general(long n_cells, int eta_n, const double* __restrict__ eta, double s2,
+                                        int geom, const double* __restrict__ gbox, const double* __restrict__ gtab,
+                                        double* __restrict__ m64, float* __restrict__ m32) {
+  constexpr int nq = fe::pow3(dim), np = fe::pow2(dim);
+  const long ic = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (ic >= n_cells) return;
+  double m[np * np];
+  for (int k = 0; k < np * np; ++k) m[k] = 0;
+  for (int q = 0; q < nq; ++q) {
+    double wq = fe::Wv(q % 3) * fe::Wv((q / 3) % 3);
+    if (dim == 3) wq *= fe::Wv(q / 9);
+    const double det = geom == GEOM_TABLE ? gtab[(ic * nq + q) * (dim * dim + 1) + dim * dim]
+                                          : gbox[ic * (dim + 1) + dim];
+    const double f = s2 / eta[ic * eta_n + (eta_n == 1 ? 0 : q)] * det * wq;
+    for (int i = 0; i < np; ++i)
+      for (int j = 0; j < np; ++j) m[i * np + j] += f * psi1<dim>(q, i) * psi1<dim>(q, j);
+  }
+  for (int k = 0; k < np * np; ++k) {
+    m64[ic * np * np + k] = m[k];
+    m32[ic * np * np + k] = (float)m[k];
+  }
+}
+
 // Body-force right-hand side of one finest cell and velocity component:
 // V[n] = sum_q JxW_q f_comp(q) phi_n(q) (source/simulator/assemblers/stokes.cc:
 // 285-400, the rho g . phi_u term), by the transposed interpolation of the
@@ -370,6 +396,20 @@ void device_level_viscosity(std::vector<Level>& levels, const double* eta_in, in
     } else {
       L.f64.eta_active.release();
       L.f32.eta_active.release();
+    }
+    if (!L.structured && L.degree == 2) {
+      // indexed levels: the same matrices from the level's JxW (the mass cell
+      // pass then reads them instead of the per-point geometry)
+      const int np = d == 3 ? 8 : 4;
+      const LevelView<double> v = L.view<double>(s, 0);
+      L.f64.Mp.alloc((size_t)L.n_cells * np * np);
+      L.f32.Mp.alloc((size_t)L.n_cells * np * np);
+      if (d == 3)
+        k_mass_matrices_general<3><<<grid(L.n_cells), kCoefThreads, 0, st>>>(
+            L.n_cells, L.eta_n, L.f64.eta.p, s * s, v.geom, v.gbox, v.gtab, L.f64.Mp.p, L.f32.Mp.p);
+      else
+        k_mass_matrices_general<2><<<grid(L.n_cells), kCoefThreads, 0, st>>>(
+            L.n_cells, L.eta_n, L.f64.eta.p, s * s, v.geom, v.gbox, v.gtab, L.f64.Mp.p, L.f32.Mp.p);
     }
     if (L.structured) {
       const int np = d == 3 ? 8 : 4;

@@ -55,7 +55,7 @@ struct LevelDev {
   DevBuf<T> dinvA, dinvM;
   DevBuf<T> gu_w, gp_w;  // gather weights (general levels)
   DevBuf<T> Eu, Ep;      // per-cell contributions of pass 1
-  DevBuf<T> Mp;          // lattice levels: per-cell pressure mass matrices [cell][np][np]
+  DevBuf<T> Mp;          // per-cell pressure mass matrices of the level table [cell][np][np] (velocity degree 2)
   DevBuf<T> Fa;          // fused A-block operator (FP32): per-tile partial sums of face nodes
   DevBuf<T> eta_active;  // finest level without averaging: per-point table of the outer operators
   // V-cycle work vectors (A block: n_u, Schur block: n_p)
@@ -140,6 +140,7 @@ struct Level {
     if (eta_active_n > 0) {
       v.eta = dev<T>().eta_active.p;
       v.eta_n = eta_active_n;
+      v.Mp = nullptr;  // the per-cell mass matrices belong to the level table
     }
     return v;
   }

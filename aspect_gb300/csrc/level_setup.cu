@@ -685,6 +685,7 @@ LevelView<T> Level::view(double s, int compressible) {
   v.gtab = D.gtab.p;
   v.eta = D.eta.p;
   v.eta_n = eta_n;
+  v.Mp = D.Mp.p;
   v.s = (T)s;
   v.compressible = compressible;
   return v;
