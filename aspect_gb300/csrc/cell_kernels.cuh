@@ -214,9 +214,11 @@ struct QGeom {
   T jxw;
 };
 
-template <typename T, int dim, int q>
+// GK >= 0: the level's geometry kind known at compile time (GeomKind)
+template <typename T, int dim, int q, int GK = -1>
 __device__ __forceinline__ void qgeom(const LevelView<T>& L, int cell, const T* box, QGeom<T, dim>& g) {
-  if (L.geom == GEOM_TABLE) {
+  const int geom = GK >= 0 ? GK : L.geom;
+  if (geom == GEOM_TABLE) {
     const T* t = L.gtab + ((size_t)cell * Shape<dim>::nq + q) * (dim * dim + 1);
 #pragma unroll
     for (int d = 0; d < dim; ++d)
@@ -238,10 +240,11 @@ __device__ __forceinline__ void qgeom(const LevelView<T>& L, int cell, const T* 
 //   P: nodal pressure values (OPK_STOKES / OPK_BT)
 // Output: V (nodal velocity-test contributions, this component),
 //         YP (partial pressure-test contributions of this component; STOKES)
-template <typename T, int dim, int op>
+template <typename T, int dim, int op, int GK = -1>
 __device__ __forceinline__ void velocity_cell_op(const LevelView<T>& L, int cell, int comp, unsigned lane_base,
                                                  T* U, const T* P, T* V, T* YP, const T* box, T eta_cell,
                                                  const T* __restrict__ eta_q) {
+  const int geom = GK >= 0 ? GK : L.geom;
   constexpr int nv = Shape<dim>::nv, np = Shape<dim>::np;
   constexpr bool need_u = (op == OPK_STOKES || op == OPK_A);
   constexpr bool need_p = (op == OPK_STOKES || op == OPK_BT);
@@ -259,14 +262,14 @@ __device__ __forceinline__ void velocity_cell_op(const LevelView<T>& L, int cell
   static_for<nv>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
     QGeom<T, dim> G;
-    if (L.geom == GEOM_CART) {
+    if (geom == GEOM_CART) {
 #pragma unroll
       for (int d = 0; d < dim; ++d)
 #pragma unroll
         for (int e = 0; e < dim; ++e) G.iJ[d][e] = d == e ? L.inv_h[d] : T(0);
       G.jxw = L.det * T(qweight<dim, q>());
     } else {
-      qgeom<T, dim, q>(L, cell, box, G);
+      qgeom<T, dim, q, GK>(L, cell, box, G);
     }
     const T eta = eta_q ? eta_q[q] : eta_cell;
     // real-space gradient row of this component: g[e] = d u_comp / d x_e
@@ -276,7 +279,7 @@ __device__ __forceinline__ void velocity_cell_op(const LevelView<T>& L, int cell
       gr[0] = colloc_d<T, dim, q, 0>(U);
       gr[1] = colloc_d<T, dim, q, 1>(U);
       if constexpr (dim == 3) gr[2] = colloc_d<T, dim, q, 2>(U);
-      if (L.geom == GEOM_TABLE) {
+      if (geom == GEOM_TABLE) {
 #pragma unroll
         for (int e = 0; e < dim; ++e) {
           T t = T(0);
@@ -344,7 +347,7 @@ __device__ __forceinline__ void velocity_cell_op(const LevelView<T>& L, int cell
     }
     // reference-direction flux R[d] = JxW sum_e F[e] invJ[d][e]
     T R[3];
-    if (L.geom == GEOM_TABLE) {
+    if (geom == GEOM_TABLE) {
 #pragma unroll
       for (int d = 0; d < dim; ++d) {
         T t = T(0);
@@ -394,7 +397,7 @@ __device__ __forceinline__ void structured_cell_lex(const LevelView<T>& L, int c
   sc.pnode0 = (sc.k * L.Np[1] + sc.j) * L.Np[0] + sc.i;
 }
 
-template <typename T, int dim, int op>
+template <typename T, int dim, int op, int GK = -1>
 __global__ void __launch_bounds__(128) velocity_cell_kernel(LevelView<T> L, const T* __restrict__ src_u,
                                                              const T* __restrict__ src_p, T* __restrict__ Eu,
                                                              T* __restrict__ Ep) {
@@ -417,7 +420,7 @@ __global__ void __launch_bounds__(128) velocity_cell_kernel(LevelView<T> L, cons
 
   T U[nv], V[nv], P[np], YP[np];
   T box[4] = {T(0), T(0), T(0), T(0)};
-  if (L.geom == GEOM_BOX && active)
+  if ((GK >= 0 ? GK : L.geom) == GEOM_BOX && active)
 #pragma unroll
     for (int d = 0; d <= dim; ++d) box[d] = L.gbox[(size_t)cell * (dim + 1) + d];
   if (need_u) {
@@ -452,7 +455,7 @@ __global__ void __launch_bounds__(128) velocity_cell_kernel(LevelView<T> L, cons
     if (L.eta_n == 1) eta_cell = L.eta[cell];
     else eta_q = L.eta + (size_t)cell * L.eta_n;
   }
-  velocity_cell_op<T, dim, op>(L, cell, comp, lane_base, U, P, V, YP, box, eta_cell, eta_q);
+  velocity_cell_op<T, dim, op, GK>(L, cell, comp, lane_base, U, P, V, YP, box, eta_cell, eta_q);
   if (active) {
     T* e = Eu + ((size_t)cell * dim + comp) * nv;
 #pragma unroll

@@ -25,6 +25,20 @@ void cell_pass_dim(const LevelView<GB_T>& L, int op, const GB_T* su, const GB_T*
     return;
   }
   const int g = cell_grid<dim>(L.n_cells);
+  // indexed levels: the geometry kind as a template argument (one code path per
+  // point instead of three, a smaller kernel for the instruction cache)
+  if (L.geom == GEOM_TABLE) {
+    if (op == OPK_STOKES) velocity_cell_kernel<GB_T, dim, OPK_STOKES, GEOM_TABLE><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
+    else if (op == OPK_A) velocity_cell_kernel<GB_T, dim, OPK_A, GEOM_TABLE><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
+    else velocity_cell_kernel<GB_T, dim, OPK_BT, GEOM_TABLE><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
+    return;
+  }
+  if (L.geom == GEOM_BOX) {
+    if (op == OPK_STOKES) velocity_cell_kernel<GB_T, dim, OPK_STOKES, GEOM_BOX><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
+    else if (op == OPK_A) velocity_cell_kernel<GB_T, dim, OPK_A, GEOM_BOX><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
+    else velocity_cell_kernel<GB_T, dim, OPK_BT, GEOM_BOX><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
+    return;
+  }
   if (op == OPK_STOKES) velocity_cell_kernel<GB_T, dim, OPK_STOKES><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
   else if (op == OPK_A) velocity_cell_kernel<GB_T, dim, OPK_A><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
   else velocity_cell_kernel<GB_T, dim, OPK_BT><<<g, kCellThreads, 0, s>>>(L, su, sp, Eu, Ep);
