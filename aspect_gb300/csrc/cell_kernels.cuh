@@ -397,8 +397,13 @@ __device__ __forceinline__ void structured_cell_lex(const LevelView<T>& L, int c
   sc.pnode0 = (sc.k * L.Np[1] + sc.j) * L.Np[0] + sc.i;
 }
 
+// Per-point geometry tables (GK = GEOM_TABLE): at most 96 registers, five
+// blocks per SM. The kernel waits on global loads (cell DoF codes, values,
+// geometry), so the extra resident warps pay for the few spilled registers
+// (measured on the shell: FP32 A cell pass 95 -> 91 us, FP32 Stokes 194 -> 170 us;
+// on box-geometry levels the same cap measured slower, so they keep the default).
 template <typename T, int dim, int op, int GK = -1>
-__global__ void __launch_bounds__(128) velocity_cell_kernel(LevelView<T> L, const T* __restrict__ src_u,
+__global__ void __launch_bounds__(128, (GK == GEOM_TABLE ? 5 : 1)) velocity_cell_kernel(LevelView<T> L, const T* __restrict__ src_u,
                                                              const T* __restrict__ src_p, T* __restrict__ Eu,
                                                              T* __restrict__ Ep) {
   pdl_wait();
