@@ -121,9 +121,11 @@ struct Handle {
   bool coarse_ready = false;
   // levels 0..mass_bottom_top of the FP32 mass V-cycle run in one single-block launch (-1: none)
   int mass_bottom_top = -1;
-  // levels 0..mass_dense_top of the FP32 mass V-cycle as one column-major matrix (-1: none)
-  int mass_dense_top = -1;
-  DevBuf<float> mass_dense;
+  // levels 0..mass_dense_top of the FP32 mass V-cycle as one column-major matrix (-1: none):
+  // mass_dense for the levels the single-block cycle covers (top mass_dense_base),
+  // mass_dense2 when the lattice level above them is included (built from mass_dense)
+  int mass_dense_top = -1, mass_dense_base = -1;
+  DevBuf<float> mass_dense, mass_dense2;
   // the same for the FP32 A-block V-cycle
   int a_dense_top = -1;
   DevBuf<float> a_dense;
@@ -675,12 +677,14 @@ int plan_mass_dense(const Handle& H) {
 // so its matrix is the cycle applied to the unit vectors: one block per column,
 // each running the single-block cycle (batch mode of mass_vcycle_bottom). Built
 // after the eigenvalue estimates and again whenever they or the level tables change.
+void build_mass_dense_next(Handle& H);
 void build_mass_dense(Handle& H) {
-  H.mass_dense_top = -1;
+  H.mass_dense_top = H.mass_dense_base = -1;
   if (!H.prec_done[1]) return;
   const int K = plan_mass_dense(H);
   if (K < 0) {
     H.mass_dense.release();
+    H.mass_dense2.release();
     return;
   }
   const int n = (int)H.levels[K].n_p;
@@ -691,7 +695,11 @@ void build_mass_dense(Handle& H) {
   launch_mass_vcycle_bottom_batch(A, mass_bottom_layout(A), n, H.st);
   ++H.cell_launches;
   GB_CUDA(cudaStreamSynchronize(H.st));
-  H.mass_dense_top = K;
+  H.mass_dense_top = H.mass_dense_base = K;
+  build_mass_dense_next(H);
+}
+const float* mass_dense_matrix(const Handle& H) {
+  return H.mass_dense_top > H.mass_dense_base ? H.mass_dense2.p : H.mass_dense.p;
 }
 
 // The A-block counterpart: levels 0..K of 3D lattices with at most
@@ -781,7 +789,7 @@ void vcycle_level(Handle& H, int lev, int block) {
     }
     if (block == 1 && lev == H.mass_dense_top) {
       const Level& L = H.levels[lev];
-      launch_dense_gemv_colmajor((int)L.n_p, H.mass_dense.p, L.f32.defM.p, H.levels[lev].f32.solM.p, H.st);
+      launch_dense_gemv_colmajor((int)L.n_p, mass_dense_matrix(H), L.f32.defM.p, H.levels[lev].f32.solM.p, H.st);
       ++H.cell_launches;
       return;
     }
@@ -1351,6 +1359,99 @@ __global__ void k_scale_columns(long n, const double* V, const double* sc, doubl
     if ((x) != CUBLAS_STATUS_SUCCESS) throw ::gb::Error(3, "cuBLAS error in " #x);         \
   } while (0)
 
+// The FP32 mass cycle of levels 0..K+1 as a matrix, from that of levels 0..K
+// (mass_dense): the multi-launch steps of level K+1 -- Chebyshev pre-smoothing
+// from a zero start, the residual, the restriction, the coarse product, the
+// prolongation, the post-smoothing -- each run once over all n unit vectors of
+// level K+1 as n columns (batched kernels, the coarse product one SGEMM),
+// with the coefficients and vectors of the multi-launch cycle.
+void build_mass_dense_next(Handle& H) {
+  const int K = H.mass_dense_base;
+  const int max_nodes = std::min(H.opt.dense_mass_cycle_nodes, kMaxDenseNextNodes);
+  if (K < 0 || K + 1 >= H.n_levels) {
+    H.mass_dense2.release();
+    return;
+  }
+  Level& L = H.levels[K + 1];
+  if (!L.structured || L.dim != 3 || L.n_p > max_nodes) {
+    H.mass_dense2.release();
+    return;
+  }
+  const int n = (int)L.n_p, m = n, nc = (int)H.levels[K].n_p;
+  LevelDev<float>& D = L.f32;
+  const LevelView<float> v = L.view<float>(H.s, H.compressible);
+  const size_t nm = (size_t)n * m;
+  DevBuf<float> X, T, Dd, B, CD, CS;
+  X.alloc(nm);
+  T.alloc(nm);
+  Dd.alloc(nm);
+  B.alloc(nm);
+  CD.alloc((size_t)nc * m);
+  CS.alloc((size_t)nc * m);
+  launch_unit_columns(n, m, B.p, H.st);
+  const ChebParams cp = cheb_params(H, K + 1);
+  double theta, delta;
+  chebyshev_bounds<float>(H, K + 1, 1, theta, delta);
+  auto cheb = [&](bool zero_start) {
+    float* cur = X.p;
+    auto step = [&](double f1, double f2) {
+      float* nxt = cur == X.p ? T.p : X.p;
+      GatherArgs<float> a{};
+      a.x = cur;
+      a.y = nxt;
+      a.b = B.p;
+      a.dinv = D.dinvM.p;
+      a.d = Dd.p;
+      a.f1 = (float)f1;
+      a.f2 = (float)f2;
+      launch_mass_lattice_batched(v, D.Mp.p, EPI_CHEB_OUT, a, m, H.st);
+      cur = nxt;
+    };
+    if (zero_start) launch_cheb_first_batched(n, m, B.p, D.dinvM.p, (float)(1.0 / theta), Dd.p, X.p, H.st);
+    else step(0.0, 1.0 / theta);
+    double rhok = delta / theta;
+    const double sigma = theta / delta;
+    for (int k = 1; k < cp.degree; ++k) {
+      const double rhokp = 1.0 / (2.0 * sigma - rhok);
+      const double f1 = rhokp * rhok, f2 = 2.0 * rhokp / delta;
+      rhok = rhokp;
+      step(f1, f2);
+    }
+    if (cur != X.p) launch_copy_batched(n, m, cur, X.p, H.st);
+  };
+  const int steps = smoothing_steps(H, 1);
+  cheb(true);
+  for (int k = 1; k < steps; ++k) cheb(false);
+  {
+    GatherArgs<float> a{};
+    a.x = X.p;
+    a.b = B.p;
+    a.y = T.p;
+    launch_mass_lattice_batched(v, D.Mp.p, EPI_RESID, a, m, H.st);
+  }
+  launch_spmv_batched((int)L.PpT_rows, L.PpT_ptr.p, L.PpT_col.p, D.PpT_val.p, T.p, n, CD.p, nc, m, false, H.st);
+  {
+    cublasHandle_t blas = nullptr;
+    GB_CUBLAS(cublasCreate(&blas));
+    const float one = 1.0f, zero = 0.0f;
+    const cublasStatus_t st1 = cublasSetStream(blas, H.st);
+    const cublasStatus_t st2 = st1 != CUBLAS_STATUS_SUCCESS
+                                   ? st1
+                                   : cublasSgemm(blas, CUBLAS_OP_N, CUBLAS_OP_N, nc, m, nc, &one, H.mass_dense.p, nc,
+                                                 CD.p, nc, &zero, CS.p, nc);
+    GB_CUDA(cudaStreamSynchronize(H.st));
+    cublasDestroy(blas);
+    GB_CUBLAS(st2);
+  }
+  launch_spmv_batched((int)L.Pp_rows, L.Pp_ptr.p, L.Pp_col.p, D.Pp_val.p, CS.p, nc, X.p, n, m, true, H.st);
+  for (int k = 0; k < steps; ++k) cheb(false);
+  H.mass_dense2.alloc(nm);  // same size on a rebuild: same address for captured V-cycles
+  GB_CUDA(cudaMemcpyAsync(H.mass_dense2.p, X.p, nm * sizeof(float), cudaMemcpyDeviceToDevice, H.st));
+  GB_CUDA(cudaStreamSynchronize(H.st));
+  H.cell_launches += 8 * (long long)cp.degree + 8;
+  H.mass_dense_top = K + 1;
+}
+
 // Dense FP64 pseudo-inverses of the level-0 A and mass matrices: the matrices are
 // assembled column by column from the FP64 level operator, eigendecomposed once
 // (cuSOLVER syevd), and eigenvalues below 1e-10 lambda_max (null spaces) dropped.
@@ -1578,7 +1679,7 @@ void gb_gmg_default_options(gb_gmg_options* o) {
   o->force_indexed_layout = 0;
   o->coarse_solver = GB_GMG_COARSE_CHEBYSHEV;
   o->fused_a_min_cells = 0;  // measured slower than the two-pass form (see ablock_fused.cu)
-  o->dense_mass_cycle_nodes = gb::kMaxDenseBottomNodes;
+  o->dense_mass_cycle_nodes = gb::kMaxDenseNextNodes;
   o->dense_a_cycle_dofs = gb::kMaxDenseANodes;
 }
 

@@ -223,6 +223,78 @@ __global__ void __launch_bounds__(32 * kGemvSlices) dense_gemv_colmajor(int n, c
 }
 }  // namespace
 
+namespace {
+template <int epi>
+__global__ void __launch_bounds__(kMassLatticeThreads) k_mass_lattice_batched(LevelView<float> L,
+                                                                              const float* __restrict__ Mc,
+                                                                              GatherArgs<float> a) {
+  const size_t off = (size_t)blockIdx.y * L.n_p;
+  a.x += off;
+  if (a.y) a.y += off;
+  if (a.b) a.b += off;
+  if (a.d) a.d += off;
+  mass_lattice_task<float, 3, epi>(L, Mc, a, blockIdx.x * (long)blockDim.x + threadIdx.x);
+}
+__global__ void k_cheb_first_batched(long n, long total, const float* __restrict__ b, const float* __restrict__ dinv,
+                                     float f2, float* __restrict__ d, float* __restrict__ x) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const float v = f2 * dinv[i % n] * b[i];
+    d[i] = v;
+    x[i] = v;
+  }
+}
+__global__ void k_copy_batched(long total, const float* __restrict__ x, float* __restrict__ y) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) y[i] = x[i];
+}
+__global__ void k_unit_columns(long n, long total, float* __restrict__ x) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x)
+    x[i] = (i % n) == (i / n) ? 1.0f : 0.0f;
+}
+__global__ void k_spmv_batched(int rows, const int* __restrict__ ptr, const int* __restrict__ col,
+                               const float* __restrict__ val, const float* __restrict__ x, long nx,
+                               float* __restrict__ y, long ny, int add) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  const float* xc = x + (size_t)blockIdx.y * nx;
+  float t = 0.0f;
+  for (int k = ptr[r]; k < ptr[r + 1]; ++k) t += val[k] * xc[col[k]];
+  float* yc = y + (size_t)blockIdx.y * ny;
+  yc[r] = add ? yc[r] + t : t;
+}
+int flat_grid(long total) {
+  long b = (total + 255) / 256;
+  if (b > 152L * 32) b = 152L * 32;
+  return (int)(b < 1 ? 1 : b);
+}
+}  // namespace
+
+void launch_mass_lattice_batched(const LevelView<float>& L, const float* Mc, int epi, const GatherArgs<float>& a,
+                                 int m, cudaStream_t s) {
+  const long tasks = (long)L.n_p * 8;
+  const dim3 g((unsigned)((tasks + kMassLatticeThreads - 1) / kMassLatticeThreads), (unsigned)m);
+  if (epi == EPI_RESID) k_mass_lattice_batched<EPI_RESID><<<g, kMassLatticeThreads, 0, s>>>(L, Mc, a);
+  else k_mass_lattice_batched<EPI_CHEB_OUT><<<g, kMassLatticeThreads, 0, s>>>(L, Mc, a);
+  GB_CUDA(cudaGetLastError());
+}
+void launch_cheb_first_batched(long n, int m, const float* b, const float* dinv, float f2, float* d, float* x,
+                               cudaStream_t s) {
+  const long total = n * m;
+  k_cheb_first_batched<<<flat_grid(total), 256, 0, s>>>(n, total, b, dinv, f2, d, x);
+}
+void launch_copy_batched(long n, int m, const float* x, float* y, cudaStream_t s) {
+  k_copy_batched<<<flat_grid(n * m), 256, 0, s>>>(n * m, x, y);
+}
+void launch_unit_columns(long n, int m, float* x, cudaStream_t s) {
+  k_unit_columns<<<flat_grid(n * m), 256, 0, s>>>(n, n * m, x);
+}
+void launch_spmv_batched(int rows, const int* ptr, const int* col, const float* val, const float* x, long nx,
+                         float* y, long ny, int m, bool add, cudaStream_t s) {
+  if (rows <= 0 || m <= 0) return;
+  const dim3 g((unsigned)((rows + 255) / 256), (unsigned)m);
+  k_spmv_batched<<<g, 256, 0, s>>>(rows, ptr, col, val, x, nx, y, ny, add ? 1 : 0);
+  GB_CUDA(cudaGetLastError());
+}
+
 void launch_dense_gemv_colmajor(int n, const float* B, const float* x, float* y, cudaStream_t s) {
   if (n <= 0) return;
   dense_gemv_colmajor<<<(n + 31) / 32, 32 * kGemvSlices, 0, s>>>(n, B, x, y);

@@ -55,6 +55,9 @@ struct MassBottomArgs {
 // replaces every launch of those levels. Levels of at most this many pressure
 // nodes qualify (the matrix is n x n floats).
 constexpr int kMaxDenseBottomNodes = 1000;
+// The lattice level above those (at most this many pressure nodes, the matrix
+// n x n floats) is built from theirs by the batched steps below.
+constexpr int kMaxDenseNextNodes = 6000;
 
 // Fills lev[l].off for levels 0..n_levels-1 and returns the dynamic shared
 // memory the launch needs, in bytes.
@@ -67,5 +70,24 @@ void launch_mass_vcycle_bottom(const MassBottomArgs& A, int smem_bytes, cudaStre
 void launch_mass_vcycle_bottom_batch(const MassBottomArgs& A, int smem_bytes, int n_cols, cudaStream_t s);
 // y = B x for a column-major n x n matrix B (fixed summation order)
 void launch_dense_gemv_colmajor(int n, const float* B, const float* x, float* y, cudaStream_t s);
+
+// Batched forms of one lattice level's FP32 mass-cycle steps, over m column
+// vectors of length n stored one after another (column c at c * n): used to
+// apply the cycle of levels 0..K+1 to all unit vectors of level K+1 at once.
+// mass operator with epilogue EPI_CHEB_OUT or EPI_RESID; a's vectors (x, y, b,
+// d) are the first columns, dinv is shared
+void launch_mass_lattice_batched(const LevelView<float>& L, const float* Mc, int epi, const GatherArgs<float>& a,
+                                 int m, cudaStream_t s);
+// d = f2 dinv b; x = d (the first Chebyshev step from a zero start)
+void launch_cheb_first_batched(long n, int m, const float* b, const float* dinv, float f2, float* d, float* x,
+                               cudaStream_t s);
+// y[:, c] = x[:, c]
+void launch_copy_batched(long n, int m, const float* x, float* y, cudaStream_t s);
+// columns of the identity: x[i + c n] = (i == c)
+void launch_unit_columns(long n, int m, float* x, cudaStream_t s);
+// CSR product per column: y[:, c] = A x[:, c] (add = 0) or y[:, c] += A x[:, c];
+// x columns of length nx, y columns of length ny (rows of A <= ny; rows past it untouched)
+void launch_spmv_batched(int rows, const int* ptr, const int* col, const float* val, const float* x, long nx,
+                         float* y, long ny, int m, bool add, cudaStream_t s);
 
 }  // namespace gb

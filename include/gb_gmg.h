@@ -123,9 +123,9 @@ typedef struct gb_gmg_options {
                                    the default: the two-pass form measured faster)      */
   int dense_mass_cycle_nodes;   /* FP32 Schur (pressure-mass) V-cycle: the sub-cycle of
                                    the coarse lattice levels up to the highest one with
-                                   at most this many pressure nodes (<= 1000) is
+                                   at most this many pressure nodes (<= 6000) is
                                    computed once per preconditioner build as an explicit
-                                   matrix and applied as one dense product (1000; 0: off,
+                                   matrix and applied as one dense product (6000; 0: off,
                                    every level runs its own launches)                 */
   int dense_a_cycle_dofs;       /* the same for the FP32 A-block V-cycle: lattice levels
                                    up to the highest one with at most this many velocity
