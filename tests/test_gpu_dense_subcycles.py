@@ -58,6 +58,18 @@ def test_dense_subcycles_follow_eigenvalue_and_viscosity_changes():
         assert rel_err(on.vcycle(block, r, gmg.FP32), off.vcycle(block, r, gmg.FP32)) < 1e-5, block
 
 
+def test_next_level_dense_subcycle():
+    """dense_mass_cycle_nodes = 6000: the Schur sub-cycle matrix of the 16^3 level,
+    built from the 8^3 level's by the batched steps, against the multi-launch cycle
+    (32^3 hierarchy: the 16^3 level is below the top)."""
+    P = problems.sinkers_3d(32, projection=1)
+    wide = gmg.from_problem(P, {"dense_mass_cycle_nodes": 6000})
+    off = gmg.from_problem(P, OFF)
+    f = P.fine
+    r = np.random.default_rng(8).normal(size=f.n_p)
+    assert rel_err(wide.vcycle(1, r, gmg.FP32), off.vcycle(1, r, gmg.FP32)) < 1e-5
+
+
 def test_mixed_solve_with_and_without_dense_subcycles():
     P, on, off = _pair(16, 1)
     f = P.fine
