@@ -107,6 +107,11 @@ struct Handle {
   int idr_s_alloc = 0;
   DevBuf<double> hcol_d, arn_d;  // Arnoldi column and scalars (|w|^2, |w| before, 1/|w|) on the device
   DevBuf<int> arn_flag;          // 1: the step needs its second Gram-Schmidt pass
+  // float-pair copy of the Krylov basis V (column stride lds) and the scale
+  // exponents of the Arnoldi steps (double-buffered: step j reads [j & 1])
+  DevBuf<float2> Vs;
+  long lds = 0;
+  DevBuf<int> gs_shift;
   DevBuf<double> cg_r, cg_z, cg_p, cg_q, cg_x;
   DevBuf<float> f32_a, f32_b;
   int restart_alloc = -1;
@@ -1026,6 +1031,10 @@ void ensure_krylov(Handle& H, int restart) {
   if (H.restart_alloc >= restart) return;
   H.V.alloc((size_t)(restart + 1) * n);
   H.Z.alloc((size_t)restart * n);
+  H.lds = (n + 1) / 2 * 2;  // even: 16-byte aligned columns of float pairs
+  H.Vs.alloc((size_t)(restart + 1) * H.lds);
+  H.gs_shift.alloc(2);
+  GB_CUDA(cudaMemsetAsync(H.gs_shift.p, 0, 2 * sizeof(int), H.st));
   H.coef_d.alloc(restart + 2);
   H.hcol_d.alloc(restart + 2);
   H.arn_d.alloc(3);
@@ -1054,6 +1063,7 @@ int gmres(Handle& H, double* x, const double* b, double tol, int maxit, int rest
           double& final_res) {
   const long n = H.n_top();
   ensure_krylov(H, restart);
+  const bool float_pair = !P || P->orthogonalization == GB_GMG_GS_FLOAT_PAIR;
   double* V = H.V.p;
   double* Z = H.Z.p;
   double* w = H.wv.p;
@@ -1074,8 +1084,12 @@ int gmres(Handle& H, double* x, const double* b, double tol, int maxit, int rest
     GB_CHECK(std::isfinite(beta), GB_GMG_NAN_DETECTED, "NaN or Inf in the Stokes residual");
     if (beta <= tol) { converged = true; return it; }
     if (it >= maxit) return it;
-    v_copy<double>(n, r, V, H.st);
-    v_scale<double>(n, 1.0 / beta, V, H.st);
+    if (float_pair) {
+      v_basis_df(n, nullptr, 1.0 / beta, r, V, H.Vs.p, H.st);
+    } else {
+      v_copy<double>(n, r, V, H.st);
+      v_scale<double>(n, 1.0 / beta, V, H.st);
+    }
     std::vector<std::vector<double>> Hc;
     std::vector<double> cs, sn, g(1, beta);
     int j = 0;
@@ -1093,12 +1107,25 @@ int gmres(Handle& H, double* x, const double* b, double tol, int maxit, int rest
       double* arn = H.arn_d.p;
       int* need2 = H.arn_flag.p;
       double* vnext = V + (size_t)(j + 1) * n;
-      v_multidot(n, w, V, n, j + 1, true, H.dots_d.p, H.partial.p, H.st);
-      v_cgs_update(n, j, 0, H.dots_d.p, V, n, w, hcol, arn, need2, H.partial.p, H.st);
-      v_multidot(n, w, V, n, j + 1, false, H.dots_d.p, H.partial.p, H.st, need2);
-      v_cgs_update(n, j, 1, H.dots_d.p, V, n, w, hcol, arn, need2, H.partial.p, H.st);
-      k_next_basis<<<ceil_div(n, 256), 256, 0, H.st>>>(n, arn, w, vnext);
-      VecCounter::launches() += 1;
+      int* shift = H.gs_shift.p;
+      if (float_pair && j >= 1 && j + 1 <= kGsMaxK) {
+        v_arnoldi_step_df(n, j, H.Vs.p, H.lds, w, vnext, H.Vs.p + (size_t)(j + 1) * H.lds, hcol, arn, need2,
+                          shift + (j & 1), shift + ((j + 1) & 1), H.partial.p, H.st);
+      } else {
+        // FP64 passes (also the first step of a float-pair solve: it sets the
+        // scale exponent of the next step)
+        v_multidot(n, w, V, n, j + 1, true, H.dots_d.p, H.partial.p, H.st);
+        v_cgs_update(n, j, 0, H.dots_d.p, V, n, w, hcol, arn, need2, H.partial.p, H.st,
+                     float_pair ? shift + ((j + 1) & 1) : nullptr);
+        v_multidot(n, w, V, n, j + 1, false, H.dots_d.p, H.partial.p, H.st, need2);
+        v_cgs_update(n, j, 1, H.dots_d.p, V, n, w, hcol, arn, need2, H.partial.p, H.st);
+        if (float_pair) {
+          v_basis_df(n, arn + 2, 0.0, w, vnext, H.Vs.p + (size_t)(j + 1) * H.lds, H.st);
+        } else {
+          k_next_basis<<<ceil_div(n, 256), 256, 0, H.st>>>(n, arn, w, vnext);
+          VecCounter::launches() += 1;
+        }
+      }
       GB_CUDA(cudaMemcpyAsync(H.dots_h, hcol, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, H.st));
       GB_CUDA(cudaStreamSynchronize(H.st));
       std::vector<double> h(H.dots_h, H.dots_h + j + 2);
@@ -1700,6 +1727,7 @@ void gb_gmg_default_solve_params(gb_gmg_solve_params* p) {
   p->idr_s = 2;
   p->solve_newton_system = 0;
   p->ir_inner_tolerance = 1e-3;
+  p->orthogonalization = GB_GMG_GS_FLOAT_PAIR;
 }
 
 int gb_gmg_create(const gb_gmg_options* opt, int dim, int degree_v, int n_levels, gb_gmg** out) {
@@ -2355,6 +2383,8 @@ int gb_gmg_solve_device(gb_gmg* g, const double* d_rhs, double* d_sol, const gb_
     gb_gmg_solve_params P;
     if (prm) P = *prm; else gb_gmg_default_solve_params(&P);
     GB_CHECK(P.restart >= 1, 1, "restart must be >= 1");
+    GB_CHECK(P.orthogonalization == GB_GMG_GS_FLOAT_PAIR || P.orthogonalization == GB_GMG_GS_FP64, 1,
+             "orthogonalization must be GB_GMG_GS_FLOAT_PAIR or GB_GMG_GS_FP64");
     const int top = H.n_levels - 1;
     gb::to_internal(H, top, d_rhs, H.bv.p, true, true);
     gb::to_internal(H, top, d_sol, H.cg_x.p, true, true);
@@ -2510,7 +2540,7 @@ int gb_gmg_memory_consumption(const gb_gmg* g, size_t* bytes) {
                                       &H.rv, &H.bv, &H.tv, &H.t2v, &H.coef_d, &H.cg_r, &H.cg_z, &H.cg_p, &H.cg_q,
                                       &H.cg_x})
     b += x->bytes();
-  b += H.f32_a.bytes() + H.f32_b.bytes();
+  b += H.f32_a.bytes() + H.f32_b.bytes() + H.Vs.bytes();
   *bytes = b;
   return GB_GMG_OK;
 }

@@ -67,9 +67,26 @@ void v_spmv_set(long rows, long n, const int* ptr, const int* col, const T* val,
 // partial: the reduction workspace (kDotWorkspaceDoubles, zeroed once)
 void v_multidot(long n, const double* w, const double* V, long ld, int k, bool with_norm, double* out_dev,
                 double* partial, cudaStream_t s, const int* active = nullptr);
-// one classical Gram-Schmidt pass of an Arnoldi step after its multi-dot (see vec.cu)
+// one classical Gram-Schmidt pass of an Arnoldi step after its multi-dot (see vec.cu);
+// pass 0 also sets *shift (when given) for the float-pair passes of the next step
 void v_cgs_update(long n, int j, int pass, const double* dots, const double* V, long ld, double* w, double* h,
-                  double* arn, int* need2, double* partial, cudaStream_t s);
+                  double* arn, int* need2, double* partial, cudaStream_t s, int* shift = nullptr);
+// One Arnoldi step (classical Gram-Schmidt with the conditional second pass,
+// the next basis vector and the Hessenberg column h[0..j+1]) on the float-pair
+// copy Vs of the basis (entries (h, l) with h + l the FP64 entry; column stride
+// lds even, 16-byte aligned columns): five launches, the partial sums of each
+// reduced by the next (see vec.cu). w is scaled by 2^-(*shift) while it is split;
+// the step writes the next step's exponent to *shift_next (another address) and
+// whether the second pass ran to *need2. j + 1 <= 128.
+constexpr int kDfChunk = 16;     // vectors per block of the dots launch
+constexpr int kDfMaxChunks = 8;  // chunks of one step
+constexpr int kGsMaxK = kDfMaxChunks * kDfChunk;  // basis vectors of one float-pair step, at most (128)
+void v_arnoldi_step_df(long n, int j, const float2* Vs, long lds, double* w, double* vnext, float2* vsnext,
+                       double* h, double* arn, int* need2, const int* shift, int* shift_next, double* workspace,
+                       cudaStream_t s);
+// v = sc w canonicalised to its float pair, the pair into vs (sc = *sc_dev if given)
+void v_basis_df(long n, const double* sc_dev, double sc_host, const double* w, double* v, float2* vs,
+                cudaStream_t s);
 template <typename T>
 void v_dot(long n, const T* a, const T* b, double* out_dev, double* partial, cudaStream_t s,
            const int* active = nullptr);

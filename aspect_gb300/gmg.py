@@ -58,7 +58,7 @@ class SolveParams(ctypes.Structure):
                 ("restart", ctypes.c_int), ("tol_A", ctypes.c_double), ("tol_S", ctypes.c_double),
                 ("mg_precision", ctypes.c_int), ("krylov", ctypes.c_int),
                 ("ir_inner_tolerance", ctypes.c_double), ("idr_s", ctypes.c_int),
-                ("solve_newton_system", ctypes.c_int)]
+                ("solve_newton_system", ctypes.c_int), ("orthogonalization", ctypes.c_int)]
 
 
 class NewtonTerms(ctypes.Structure):

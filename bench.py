@@ -352,6 +352,8 @@ def run_gpu(args):
     log("gmres-ir solve", tir, oir)
     tidr, oidr, xidr = timed_solve(linear_solver_tolerance=TOL, mg_precision=gmg.FP32, krylov=gmg.IDR, idr_s=2)
     log("idr(2) solve", tidr, oidr)
+    tgs, ogs, xgs = timed_solve(**dict(params, orthogonalization=1))
+    log("mixed solve, FP64 Gram-Schmidt passes", tgs, ogs)
     _, _, x32 = timed_solve(**params)
     rel = lambda a, b: float(torch.linalg.norm(a[: f.n_u] - b[: f.n_u]) / torch.linalg.norm(b[: f.n_u]))
 
@@ -406,6 +408,7 @@ def run_gpu(args):
         "data": f"synthetic: 8 sinkers seeded SplitMix64({P.extra['seed']})",
         "config": {"workload": WORKLOAD, "cells": f.n_cells, "n_u": f.n_u, "n_p": f.n_p, "levels": len(P.levels),
                    "tolerance": TOL, "krylov": "FGMRES(100), FP64", "mg": "FP32 V-cycle, Chebyshev(4)",
+                   "gram_schmidt": "classical, conditional second pass; float-pair products (~46 bits)",
                    "l2": "flushed between timed solves (256 MiB write)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "MDoF/s", "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": n * 8,
                 "solves": len(e2e_s), "seconds_per_solve": e2e_s},
@@ -452,6 +455,8 @@ def run_gpu(args):
                             "A_preconditioner_applications": oidr["A_preconditioner_applications"],
                             "fp64_stokes_applications": oidr["fp64_stokes_applications"],
                             "speedup_vs_fp64_mg": t64 / tidr},
+            "mixed_fp64_gram_schmidt": {"solve_s": tgs, "iterations": ogs["cheap_iterations"],
+                                        "velocity_rel_l2_vs_float_pair": rel(xgs, x32)},
             "velocity_rel_l2_vs_fp64_mg": {"mixed": rel(x32, x64), "gmres_ir": rel(xir, x64),
                                            "idr2": rel(xidr, x64)},
             "operator_seconds": ops, "operator_gdofs": gdofs,

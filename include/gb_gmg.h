@@ -140,6 +140,19 @@ enum gb_gmg_coarse_solver {
                                    null spaces such as the rotations of a free-slip shell) */
 };
 
+/* Arithmetic of the classical Gram-Schmidt passes (with the conditional second
+   pass) of the GMRES / FGMRES Arnoldi steps; the basis, the Hessenberg matrix, the
+   operator and the residuals stay FP64 either way. */
+enum gb_gmg_orthogonalization {
+  GB_GMG_GS_FLOAT_PAIR = 0,  /* the k n multiply-adds of a step as unevaluated pairs of
+                                floats (about 46 significant bits; Hessenberg entries
+                                within a few 1e-15 |w| of the FP64 passes), on the FP32
+                                pipe at the HBM rate of the basis; steps with more than
+                                128 basis vectors and the first step after a (re)start
+                                run the FP64 passes */
+  GB_GMG_GS_FP64 = 1         /* FP64 passes (bound by the FP64 pipe on this GPU)      */
+};
+
 typedef struct gb_gmg_solve_params {
   double linear_solver_tolerance;  /* relative (1e-7); tolerance rule of :977-1041   */
   double absolute_tolerance;       /* > 0: use this absolute tolerance instead        */
@@ -157,6 +170,8 @@ typedef struct gb_gmg_solve_params {
                                       so the solve starts from zero and the tolerance and
                                       initial_nonlinear_residual use |rhs| alone
                                       (stokes_matrix_free_local_smoothing.cc:952-1041)   */
+  int orthogonalization;           /* gb_gmg_orthogonalization of the GMRES / FGMRES
+                                      Arnoldi steps (float pairs)                       */
 } gb_gmg_solve_params;
 
 /* StokesSolver::SolverOutputs plus the counters the reference prints. */
