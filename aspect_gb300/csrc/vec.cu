@@ -243,8 +243,9 @@ __device__ __forceinline__ void block_reduce_store(double (&acc)[K], int nk, dou
 }
 
 // The block of a reduction that arrives last (a counter per chunk, reset by
-// that block) sums the per-block partials itself, in a fixed order, so the
-// result is deterministic in one launch.
+// that block) sums the per-block partials itself, in the same fixed order a
+// separate finishing launch would: lane l of a warp adds blocks l, l+32, ...,
+// then lane 0 adds the 32 lane sums in lane order. Deterministic, one launch.
 __device__ __forceinline__ bool arrive_last(unsigned* counter) {
   __shared__ bool last;
   __threadfence();  // this block's partials are visible before its arrival counts
@@ -254,54 +255,35 @@ __device__ __forceinline__ bool arrive_last(unsigned* counter) {
   if (last) __threadfence();
   return last;
 }
-// out[j] = sum over blocks b of part[j * nb + b], j < nk <= K: thread t adds
-// blocks t, t + kDotThreads, ... of every value with all of its loads issued
-// before the additions (one L2 round trip for nb <= kDotThreads instead of a
-// chain of dependent loads, which made this single block the tail of every
-// reduction launch), then each warp's 32 sums in a fixed shuffle tree and the 8
-// warp sums in order.
-template <int K>
 __device__ __forceinline__ void finish_partials(const double* part, int nk, double* out, unsigned* counter,
                                                 int nb = kDotBlocks) {
-  __shared__ double seg[K][kDotThreads / 32];
+  __shared__ double sh[kDotThreads / 32][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double v[K];
-#pragma unroll
-  for (int j = 0; j < K; ++j) {
+  for (int j = wid; j < nk; j += kDotThreads / 32) {
+    // lane l adds blocks l, l + 32, ... in that order; eight loads are issued
+    // before they are added, so the finishing block does not wait on one load
+    // at a time
     double t = 0;
-    if (j < nk) {
-      const double* pj = part + (size_t)j * nb;
-      int b = threadIdx.x;
-      for (; b + 3 * kDotThreads < nb; b += 4 * kDotThreads) {
-        const double a0 = __ldcg(pj + b), a1 = __ldcg(pj + b + kDotThreads);
-        const double a2 = __ldcg(pj + b + 2 * kDotThreads), a3 = __ldcg(pj + b + 3 * kDotThreads);
-        t += a0;
-        t += a1;
-        t += a2;
-        t += a3;
-      }
-      for (; b < nb; b += kDotThreads) t += __ldcg(pj + b);
+    const double* pj = part + (size_t)j * nb;
+    int b = lane;
+    for (; b + 7 * 32 < nb; b += 8 * 32) {
+      double v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = __ldcg(pj + b + u * 32);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) t += v[u];
     }
-    v[j] = t;
-  }
-#pragma unroll
-  for (int j = 0; j < K; ++j) {
-    if (j < nk) {
-      double t = v[j];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-      if (lane == 0) seg[j][wid] = t;
+    for (; b < nb; b += 32) t += __ldcg(pj + b);
+    sh[wid][lane] = t;
+    __syncwarp();
+    if (lane == 0) {
+      double v = 0;
+      for (int l = 0; l < 32; ++l) v += sh[wid][l];
+      out[j] = v;
     }
-  }
-  __syncthreads();
-  if ((int)threadIdx.x < nk) {
-    double t = 0;
-#pragma unroll
-    for (int w = 0; w < kDotThreads / 32; ++w) t += seg[threadIdx.x][w];
-    out[threadIdx.x] = t;
+    __syncwarp();
   }
   if (threadIdx.x == 0) *counter = 0u;
-  __syncthreads();
 }
 
 // blockIdx.y = chunk of kDotChunk vectors; the chunk that ends at k also forms
@@ -358,7 +340,7 @@ __global__ void __launch_bounds__(kDotThreads, 3) k_multidot(long n, const doubl
   double* part = partial + (size_t)chunk * (kDotChunk + 1) * nb;
   block_reduce_store<kDotChunk + 1>(acc, kk + norm, part, nb, norm ? kk : -1);
   if (arrive_last(counters + chunk))
-    finish_partials<kDotChunk + 1>(part, kk + norm, out + j0, counters + chunk, nb);
+    finish_partials(part, kk + norm, out + j0, counters + chunk, nb);
 }
 
 // Blocks per chunk: all chunks together about 3 x kDotBlocks blocks (three
@@ -444,7 +426,7 @@ __global__ void __launch_bounds__(kDotThreads) k_cgs_update(long n, int j, int p
   }
   block_reduce_store<1>(acc, 1, partial, gridDim.x);
   if (!arrive_last(counter)) return;
-  finish_partials<1>(partial, 1, arn, counter, gridDim.x);  // arn[0] = <w, w>
+  finish_partials(partial, 1, arn, counter, gridDim.x);  // arn[0] = <w, w>
   for (int i = threadIdx.x; i < k; i += blockDim.x) h[i] = pass == 0 ? dots[i] : h[i] + dots[i];
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -994,7 +976,7 @@ __global__ void __launch_bounds__(kDotThreads) k_dot(long n, const T* __restrict
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     acc[0] += (double)a[i] * (double)b[i];
   block_reduce_store<1>(acc, 1, partial, kDotBlocks);
-  if (arrive_last(counter)) finish_partials<1>(partial, 1, out, counter);
+  if (arrive_last(counter)) finish_partials(partial, 1, out, counter);
 }
 template <typename T>
 void v_dot(long n, const T* a, const T* b, double* out_dev, double* partial, cudaStream_t s, const int* active) {
