@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgb_gmg.so")
-SOURCES = ["kernels_f32.cu", "kernels_f64.cu", "adjoint.cu", "vec.cu", "level_setup.cu", "gb_gmg.cu", "noalloc.cu", "mass_bottom.cu", "ablock_fused.cu", "newton.cu", "coefficients.cu", "free_surface.cu", "ho_kernels.cu", "a_bottom.cu"]
+SOURCES = ["kernels_f32.cu", "kernels_f64.cu", "adjoint.cu", "vec.cu", "level_setup.cu", "gb_gmg.cu", "noalloc.cu", "mass_bottom.cu", "ablock_fused.cu", "newton.cu", "coefficients.cu", "free_surface.cu", "ho_kernels.cu", "a_bottom.cu", "lattice_transfer.cu"]
 # measured FP64/FP32 FMA peaks for the benchmark's rooflines (not part of the solver)
 PROBE_LIB = os.path.join(HERE, "libgb_probe.so")
 PROBE_SOURCES = ["peak_probe.cu"]

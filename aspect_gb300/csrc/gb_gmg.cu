@@ -822,12 +822,14 @@ void vcycle_level(Handle& H, int lev, int block) {
   smoother_apply<T>(H, lev, block, sol, def);
   level_op_resid<T>(H, lev, block, sol, def, t);
   // restriction (zero fill and product in one launch)
-  if (block == 0) v_spmv_set<T>(L.PuT_rows, nc, L.PuT_ptr.p, L.PuT_col.p, D.PuT_val.p, t, cdef, H.st);
+  if (L.xfer_lattice[block]) lattice_restrict<T>(L.xfer[block], t, cdef, H.st);
+  else if (block == 0) v_spmv_set<T>(L.PuT_rows, nc, L.PuT_ptr.p, L.PuT_col.p, D.PuT_val.p, t, cdef, H.st);
   else v_spmv_set<T>(L.PpT_rows, nc, L.PpT_ptr.p, L.PpT_col.p, D.PpT_val.p, t, cdef, H.st);
   // the coarse solution needs no zero fill: every coarse solve (the smoother from
   // a zero start, the single-block bottom, the dense coarse solve) writes all of it
   vcycle_level<T>(H, lev - 1, block);
-  if (block == 0) v_spmv_add<T>(L.Pu_rows, L.Pu_ptr.p, L.Pu_col.p, D.Pu_val.p, csol, sol, H.st);
+  if (L.xfer_lattice[block]) lattice_prolong_add<T>(L.xfer[block], csol, sol, H.st);
+  else if (block == 0) v_spmv_add<T>(L.Pu_rows, L.Pu_ptr.p, L.Pu_col.p, D.Pu_val.p, csol, sol, H.st);
   else v_spmv_add<T>(L.Pp_rows, L.Pp_ptr.p, L.Pp_col.p, D.Pp_val.p, csol, sol, H.st);
   smoother_smooth<T>(H, lev, block, sol, def);
 }
@@ -1847,7 +1849,12 @@ int gb_gmg_finalize_setup(gb_gmg* g) {
     Handle& H = g->h;
     for (auto& L : H.levels) GB_CHECK(L.n_cells > 0, 2, "a level has no mesh");
     for (auto& L : H.levels) gb::setup_level(L, H.opt.force_indexed_layout != 0);
-    for (int l = 1; l < H.n_levels; ++l) gb::setup_transfer(H.levels[l], H.levels[l - 1]);
+    for (int l = 1; l < H.n_levels; ++l) {
+      gb::setup_transfer(H.levels[l], H.levels[l - 1]);
+      if (H.opt.verbose)
+        std::fprintf(stderr, "gb_gmg: transfer %d -> %d: velocity %s, pressure %s\n", l - 1, l,
+                     H.levels[l].xfer_lattice[0] ? "lattice" : "csr", H.levels[l].xfer_lattice[1] ? "lattice" : "csr");
+    }
     gb::setup_coefficient_maps(H.levels);
     for (auto& L : H.levels) {  // FP32 A-block applications of large lattice levels: fused kernel
       L.fused_tz = 0;
@@ -2324,10 +2331,12 @@ int gb_gmg_transfer(gb_gmg* g, int fine_level, int block, int precision, int res
         y = H.f32_b.p;
       }
       if (restrict_) {
-        if (block == 0) gb::v_spmv_add<T>(F.PuT_rows, F.PuT_ptr.p, F.PuT_col.p, D.PuT_val.p, x, y, H.st);
+        if (F.xfer_lattice[block]) gb::lattice_restrict<T>(F.xfer[block], x, y, H.st);
+        else if (block == 0) gb::v_spmv_add<T>(F.PuT_rows, F.PuT_ptr.p, F.PuT_col.p, D.PuT_val.p, x, y, H.st);
         else gb::v_spmv_add<T>(F.PpT_rows, F.PpT_ptr.p, F.PpT_col.p, D.PpT_val.p, x, y, H.st);
       } else {
-        if (block == 0) gb::v_spmv_add<T>(F.Pu_rows, F.Pu_ptr.p, F.Pu_col.p, D.Pu_val.p, x, y, H.st);
+        if (F.xfer_lattice[block]) gb::lattice_prolong_add<T>(F.xfer[block], x, y, H.st);
+        else if (block == 0) gb::v_spmv_add<T>(F.Pu_rows, F.Pu_ptr.p, F.Pu_col.p, D.Pu_val.p, x, y, H.st);
         else gb::v_spmv_add<T>(F.Pp_rows, F.Pp_ptr.p, F.Pp_col.p, D.Pp_val.p, x, y, H.st);
       }
       if constexpr (!std::is_same<T, double>::value) gb::v_cast<float, double>(nout, H.f32_b.p, H.stage_a.p, H.st);

@@ -5,6 +5,7 @@
 #include <set>
 #include <vector>
 
+#include "lattice_transfer.cuh"
 #include "ops.cuh"
 #include "vec.cuh"
 
@@ -111,6 +112,11 @@ struct Level {
   DevBuf<int> pprobe_ptr, pprobe_g, pprobe_eptr, pprobe_li;
   DevBuf<int> Pu_ptr, Pu_col, PuT_ptr, PuT_col, Pp_ptr, Pp_col, PpT_ptr, PpT_col;
   long Pu_rows = 0, PuT_rows = 0, Pp_rows = 0, PpT_rows = 0;
+  // both this level and the next coarser one structured, and the transfer
+  // matrices equal to the lattice stencils (checked entry by entry at set-up):
+  // the V-cycle applies them matrix-free ([0] velocity, [1] pressure)
+  bool xfer_lattice[2] = {false, false};
+  LatticeTransfer xfer[2] = {};
   // pass-2 gather lists of general levels (caller numbering = internal numbering)
   DevBuf<int> gu_ptr, gu_slot, gp_ptr, gp_slot;
   DevBuf<unsigned char> cmask_u, cmask_p;

@@ -529,6 +529,58 @@ void setup_level(Level& L, bool force_indexed) {
 // columns: coarse internal DoFs): the coarse FE function, with its constraints
 // resolved, evaluated at the fine support points (reference coordinates of the
 // child inside its parent). Restriction is the transpose.
+// The lattice description of the transfer between two structured levels, if
+// the CSR matrix P (rows: fine internal DoFs, columns sorted by coarse internal
+// DoF) holds exactly the lattice stencils' entries: the same columns in the
+// same order and the same values. Then the matrix-free kernels form the same
+// sums as the CSR products.
+static bool lattice_transfer_of(const Level& F, const Level& C, int block, const Csr& P, LatticeTransfer& X) {
+  if (!F.structured || !C.structured || F.degree != 2 || C.degree != 2 || F.dim != C.dim) return false;
+  const int d = F.dim;
+  X = LatticeTransfer{};
+  X.q2 = block == 0 ? 1 : 0;
+  X.ncomp = block == 0 ? d : 1;
+  for (int e = 0; e < 3; ++e) {
+    if (e < d && F.nc[e] != 2 * C.nc[e]) return false;
+    X.Nf[e] = e < d ? (block == 0 ? 2 * F.nc[e] + 1 : F.nc[e] + 1) : 1;
+    X.Nc[e] = e < d ? (block == 0 ? 2 * C.nc[e] + 1 : C.nc[e] + 1) : 1;
+  }
+  X.nf_nodes = (long)X.Nf[0] * X.Nf[1] * X.Nf[2];
+  X.nc_nodes = (long)X.Nc[0] * X.Nc[1] * X.Nc[2];
+  X.zf_f = block == 0 ? F.zero_faces : 0u;
+  X.zf_c = block == 0 ? C.zero_faces : 0u;
+  const long nf = X.ncomp * X.nf_nodes;
+  if (P.rows() != nf || nf != (block == 0 ? F.n_u : F.n_p) || X.ncomp * X.nc_nodes != (block == 0 ? C.n_u : C.n_p))
+    return false;
+  for (long r = 0; r < nf; ++r) {
+    const int comp = (int)(r / X.nf_nodes);
+    const long node = r - (long)comp * X.nf_nodes;
+    const int f[3] = {(int)(node % X.Nf[0]), (int)((node / X.Nf[0]) % X.Nf[1]), (int)(node / ((long)X.Nf[0] * X.Nf[1]))};
+    int k = P.ptr[r];
+    const int e = P.ptr[r + 1];
+    if (!(X.q2 && lattice_zero(X.zf_f, X.Nf, comp, f[0], f[1], f[2]))) {
+      int c[3][3];
+      double w[3][3];
+      int m[3];
+      for (int a = 0; a < 3; ++a) {
+        if (X.Nf[a] > 1) m[a] = lattice_p1d(X.q2, f[a], c[a], w[a]);
+        else { m[a] = 1; c[a][0] = 0; w[a][0] = 1.0; }
+      }
+      for (int z = 0; z < m[2]; ++z)
+        for (int y = 0; y < m[1]; ++y)
+          for (int x = 0; x < m[0]; ++x) {
+            if (X.q2 && lattice_zero(X.zf_c, X.Nc, comp, c[0][x], c[1][y], c[2][z])) continue;
+            const long col = (long)comp * X.nc_nodes + ((long)c[2][z] * X.Nc[1] + c[1][y]) * X.Nc[0] + c[0][x];
+            const double val = w[0][x] * w[1][y] * w[2][z];
+            if (k >= e || P.col[k] != col || P.val[k] != val) return false;
+            ++k;
+          }
+    }
+    if (k != e) return false;
+  }
+  return true;
+}
+
 void setup_transfer(Level& F, const Level& C) {
   const int d = F.dim, nv = nv_of(F), np = np_of(F), nu = d * nv;
   GB_CHECK(F.has_transfer, 2, "missing child/parent data for a level");
@@ -634,6 +686,7 @@ void setup_transfer(Level& F, const Level& C) {
       }
       P.ptr.push_back((int)P.col.size());
     }
+    F.xfer_lattice[block] = lattice_transfer_of(F, C, block, P, F.xfer[block]);
     Csr PT = P.transpose(block == 0 ? C.n_u : C.n_p);
     if (block == 0) {
       F.Pu_ptr.upload(P.ptr); F.Pu_col.upload(P.col); F.Pu_rows = P.rows();
