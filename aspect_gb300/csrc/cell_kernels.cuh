@@ -848,6 +848,10 @@ template <bool eta_per_q>
 __global__ void __launch_bounds__(kSmallCellThreads) lattice_cell_kernel_small(LevelView<float> L,
                                                                                const float* __restrict__ src_u,
                                                                                float* __restrict__ Eu) {
+  // the cell's viscosity (fixed over a V-cycle) before pdl_wait, overlapping the
+  // preceding kernel in the V-cycle graphs' programmatic edges
+  const float eta_pre = threadIdx.x < 27 ? (eta_per_q ? L.eta[(size_t)blockIdx.x * 27 + threadIdx.x] : L.eta[blockIdx.x])
+                                         : 0.0f;
   pdl_wait();
   __shared__ float A[2][81];   // nodal / Gauss-point values, ping-pong between sweeps
   __shared__ float G[9][27];   // G[c*3+d][q] = d u_c / d x_d, then the fluxes R in place
@@ -891,7 +895,7 @@ __global__ void __launch_bounds__(kSmallCellThreads) lattice_cell_kernel_small(L
   if (t < 27) {
     const int q = t;
     const float jxw = L.det * K.W[q];
-    const float eta = eta_per_q ? L.eta[(size_t)cell * 27 + q] : L.eta[cell];
+    const float eta = eta_pre;
     float g[3][3];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
@@ -1034,7 +1038,8 @@ struct GatherCsr {
 };
 
 template <typename T, int epi>
-__device__ __forceinline__ void gather_epilogue(const GatherArgs<T>& a, long g, T sum, bool constrained) {
+__device__ __forceinline__ void gather_epilogue_dinv(const GatherArgs<T>& a, long g, T sum, bool constrained,
+                                                    T dinv_g) {
   if (epi == EPI_STORE) {
     a.y[g] = constrained ? a.x[g] : sum;
   } else if (epi == EPI_BT) {
@@ -1044,11 +1049,16 @@ __device__ __forceinline__ void gather_epilogue(const GatherArgs<T>& a, long g, 
   } else {
     const T xg = a.x[g];
     const T t = constrained ? xg : sum;
-    const T dn = a.f1 * a.d[g] + a.f2 * a.dinv[g] * (a.b[g] - t);
+    const T dn = a.f1 * a.d[g] + a.f2 * dinv_g * (a.b[g] - t);
     a.d[g] = dn;
     if (epi == EPI_CHEB) a.x[g] = xg + dn;
     else a.y[g] = xg + dn;
   }
+}
+template <typename T, int epi>
+__device__ __forceinline__ void gather_epilogue(const GatherArgs<T>& a, long g, T sum, bool constrained) {
+  gather_epilogue_dinv<T, epi>(a, g, sum, constrained,
+                               (epi == EPI_CHEB || epi == EPI_CHEB_OUT) ? a.dinv[g] : T(0));
 }
 
 // Velocity DoFs of a lattice level: a node's cells follow from its coordinates.
@@ -1097,7 +1107,8 @@ __global__ void __launch_bounds__(256) velocity_gather_structured(LevelView<T> L
 // summed in the same order as velocity_gather_structured (z, y, x; the lower
 // cell along a direction first), so the two give bit-identical sums.
 template <typename T, int epi>
-__device__ __forceinline__ void velocity_lattice_node(const LevelView<T>& L, const GatherArgs<T>& a, int node) {
+__device__ __forceinline__ void velocity_lattice_node_d(const LevelView<T>& L, const GatherArgs<T>& a, int node,
+                                                        const T (&dv)[3]) {
   const int nxy = L.Nn[0] * L.Nn[1];
   const int gz = node / nxy;
   const int rem = node - gz * nxy;
@@ -1145,14 +1156,33 @@ __device__ __forceinline__ void velocity_lattice_node(const LevelView<T>& L, con
           if (!cons[c]) sum[c] += a.E[(size_t)cell * a.cs + (size_t)(c * 27 + l) * a.ss];
       }
 #pragma unroll
-  for (int c = 0; c < 3; ++c) gather_epilogue<T, epi>(a, (long)c * L.n_nodes + node, sum[c], cons[c]);
+  for (int c = 0; c < 3; ++c) gather_epilogue_dinv<T, epi>(a, (long)c * L.n_nodes + node, sum[c], cons[c], dv[c]);
+}
+// the diagonal inverse of the node's three DoFs (Chebyshev epilogues only)
+template <typename T, int epi>
+__device__ __forceinline__ void velocity_lattice_dinv(const LevelView<T>& L, const GatherArgs<T>& a, int node,
+                                                      T (&dv)[3]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    dv[c] = (epi == EPI_CHEB || epi == EPI_CHEB_OUT) ? a.dinv[(long)c * L.n_nodes + node] : T(0);
 }
 template <typename T, int epi>
+__device__ __forceinline__ void velocity_lattice_node(const LevelView<T>& L, const GatherArgs<T>& a, int node) {
+  T dv[3];
+  velocity_lattice_dinv<T, epi>(L, a, node, dv);
+  velocity_lattice_node_d<T, epi>(L, a, node, dv);
+}
+// The diagonal inverse (fixed over a V-cycle, written only by the preconditioner
+// set-up) is loaded before pdl_wait, overlapping the preceding kernel in the
+// V-cycle graphs' programmatic edges.
+template <typename T, int epi>
 __global__ void __launch_bounds__(256) velocity_gather_lattice3(LevelView<T> L, GatherArgs<T> a) {
-  pdl_wait();
   const int node = blockIdx.x * blockDim.x + threadIdx.x;
+  T dv[3] = {T(0), T(0), T(0)};
+  if (node < L.n_nodes) velocity_lattice_dinv<T, epi>(L, a, node, dv);
+  pdl_wait();
   if (node >= L.n_nodes) return;
-  velocity_lattice_node<T, epi>(L, a, node);
+  velocity_lattice_node_d<T, epi>(L, a, node, dv);
 }
 
 // Pressure DoFs of a lattice level (never constrained there).
@@ -1198,46 +1228,78 @@ constexpr int kMassLatticeThreads = 256;
 
 // Task t = (node t / 2^dim, cell slot t % 2^dim). All 32 lanes of a warp must
 // call it together (the lanes of a node are summed with shuffles); tasks past
-// the last node only take part in the shuffles.
+// the last node only take part in the shuffles. In two parts: the operands that
+// stay fixed over a whole V-cycle (the cell's mass-matrix row, the node's
+// diagonal inverse) and then the dot with the iterate and the epilogue.
+template <typename T, int dim>
+struct MassLatticeRow {
+  T r[Shape<dim>::np];
+  T dinv;
+  long g;
+  int s, p0;
+  bool ok, node_ok;
+};
 template <typename T, int dim, int epi>
-__device__ __forceinline__ void mass_lattice_task(const LevelView<T>& L, const T* __restrict__ Mc,
-                                                  const GatherArgs<T>& a, long t) {
+__device__ __forceinline__ void mass_lattice_row(const LevelView<T>& L, const T* __restrict__ Mc,
+                                                 const GatherArgs<T>& a, long t, MassLatticeRow<T, dim>& m) {
   constexpr int np = Shape<dim>::np;  // = lanes per node
-  const long g = t / np;
-  const int s = (int)(t % np);
-  const bool node_ok = g < L.n_p;
-  const int node = node_ok ? (int)g : 0;
+  m.g = t / np;
+  m.s = (int)(t % np);
+  m.node_ok = m.g < L.n_p;
+  const int node = m.node_ok ? (int)m.g : 0;
   const int gc[3] = {node % L.Np[0], (node / L.Np[0]) % L.Np[1], dim == 3 ? node / (L.Np[0] * L.Np[1]) : 0};
   // slot bit d = 0: the cell below the node along d (node at its local 1), 1: above (local 0)
   int c[3] = {0, 0, 0}, l = 0;
-  bool ok = node_ok;
+  bool ok = m.node_ok;
 #pragma unroll
   for (int d = 0; d < dim; ++d) {
-    const int bit = (s >> d) & 1;
+    const int bit = (m.s >> d) & 1;
     c[d] = gc[d] - 1 + bit;
     ok = ok && c[d] >= 0 && c[d] < L.nc[d];
     l += (bit ? 0 : 1) << d;
   }
-  T sum = T(0);
+  m.ok = ok;
+  m.p0 = (c[2] * L.Np[1] + c[1]) * L.Np[0] + c[0];
   if (ok) {
     const int cell = (c[2] * L.nc[1] + c[1]) * L.nc[0] + c[0];
-    T r[np];
-    load_row<T, np>(Mc + ((size_t)cell * np + l) * np, r);
-    const int p0 = (c[2] * L.Np[1] + c[1]) * L.Np[0] + c[0];
+    load_row<T, np>(Mc + ((size_t)cell * np + l) * np, m.r);
+  }
+  m.dinv = T(0);
+  if ((epi == EPI_CHEB || epi == EPI_CHEB_OUT) && m.node_ok && m.s == 0) m.dinv = a.dinv[m.g];
+}
+template <typename T, int dim, int epi>
+__device__ __forceinline__ void mass_lattice_dot(const LevelView<T>& L, const GatherArgs<T>& a,
+                                                 const MassLatticeRow<T, dim>& m) {
+  constexpr int np = Shape<dim>::np;
+  T sum = T(0);
+  if (m.ok) {
     const T* __restrict__ xin = a.x;
 #pragma unroll
-    for (int j = 0; j < np; ++j) sum += r[j] * xin[p0 + structured_pnode_offset<dim>(L.Np, j)];
+    for (int j = 0; j < np; ++j) sum += m.r[j] * xin[m.p0 + structured_pnode_offset<dim>(L.Np, j)];
   }
 #pragma unroll
   for (int o = 1; o < np; o <<= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-  if (node_ok && s == 0) gather_epilogue<T, epi>(a, g, sum, false);
+  if (m.node_ok && m.s == 0) gather_epilogue_dinv<T, epi>(a, m.g, sum, false, m.dinv);
+}
+template <typename T, int dim, int epi>
+__device__ __forceinline__ void mass_lattice_task(const LevelView<T>& L, const T* __restrict__ Mc,
+                                                  const GatherArgs<T>& a, long t) {
+  MassLatticeRow<T, dim> m;
+  mass_lattice_row<T, dim, epi>(L, Mc, a, t, m);
+  mass_lattice_dot<T, dim, epi>(L, a, m);
 }
 
+// The fixed operands are loaded before pdl_wait: in the V-cycle graphs, whose
+// kernel edges are programmatic, that load overlaps the preceding kernel (the
+// mass matrices and diagonals are written only by the preconditioner set-up,
+// before any V-cycle runs).
 template <typename T, int dim, int epi>
 __global__ void __launch_bounds__(kMassLatticeThreads) mass_apply_lattice(LevelView<T> L, const T* __restrict__ Mc,
                                                                           GatherArgs<T> a) {
+  MassLatticeRow<T, dim> m;
+  mass_lattice_row<T, dim, epi>(L, Mc, a, blockIdx.x * (long)blockDim.x + threadIdx.x, m);
   pdl_wait();
-  mass_lattice_task<T, dim, epi>(L, Mc, a, blockIdx.x * (long)blockDim.x + threadIdx.x);
+  mass_lattice_dot<T, dim, epi>(L, a, m);
 }
 
 template <typename T, int epi>
