@@ -521,7 +521,7 @@ __device__ __forceinline__ void mass_cell_op(const LevelView<T>& L, int cell, co
 template <int op, bool eta_per_q>
 __device__ __forceinline__ void lattice_cell_f32(const LevelView<float>& L, const float* __restrict__ src_u,
                                                  const float* __restrict__ src_p, int cell, float (&V)[3][27],
-                                                 float (&YP)[8]) {
+                                                 float (&YP)[8], const float* eta_q = nullptr, int eta_stride = 1) {
   constexpr bool need_u = (op == OPK_STOKES || op == OPK_A);
   constexpr bool need_p = (op == OPK_STOKES || op == OPK_BT);
   using T = float;
@@ -552,11 +552,13 @@ __device__ __forceinline__ void lattice_cell_f32(const LevelView<float>& L, cons
   const T ih0 = L.inv_h[0], ih1 = L.inv_h[1], ih2 = L.inv_h[2];
   const T s = L.s;
   const T eta_cell = eta_per_q ? T(0) : L.eta[cell];
-  const T* __restrict__ eq = L.eta + (size_t)cell * 27;
+  // per-point viscosity: the level table, or the caller's copy (eta_q[q * eta_stride])
+  const T* eq = eta_q ? eta_q : L.eta + (size_t)cell * 27;
+  const int es = eta_q ? eta_stride : 1;
   static_for<27>([&](auto qc) {
     constexpr int q = decltype(qc)::value;
     const T jxw = L.det * T(qweight<3, q>());
-    const T eta = eta_per_q ? eq[q] : eta_cell;
+    const T eta = eta_per_q ? eq[q * es] : eta_cell;
     T G[3][3] = {{T(0)}};
     if constexpr (need_u) {
 #pragma unroll
@@ -616,11 +618,27 @@ template <int op, bool eta_per_q>
 __global__ void __launch_bounds__(128) lattice_cell_kernel_f32(LevelView<float> L, const float* __restrict__ src_u,
                                                                 const float* __restrict__ src_p,
                                                                 float* __restrict__ Eu, float* __restrict__ Ep) {
-  pdl_wait();
+  // per-point viscosity (fixed over a V-cycle) copied to shared memory before
+  // pdl_wait, so that under the V-cycle graphs' programmatic edges its latency
+  // overlaps the preceding kernel; each thread reads back only its own column
+  // after waiting for its own copies
+  __shared__ float eta_s[eta_per_q ? 27 : 1][128];
   const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-  if (cell >= L.n_cells) return;
+  const bool live = cell < L.n_cells;
+  if (eta_per_q && live) {
+    const float* src = L.eta + (size_t)cell * 27;
+#pragma unroll
+    for (int q = 0; q < 27; ++q) {
+      const unsigned sa = (unsigned)__cvta_generic_to_shared(&eta_s[q][threadIdx.x]);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(src + q) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  }
+  pdl_wait();
+  if (!live) return;
+  if (eta_per_q) asm volatile("cp.async.wait_all;\n" ::: "memory");
   float V[3][27], YP[8];
-  lattice_cell_f32<op, eta_per_q>(L, src_u, src_p, cell, V, YP);
+  lattice_cell_f32<op, eta_per_q>(L, src_u, src_p, cell, V, YP, eta_per_q ? &eta_s[0][threadIdx.x] : nullptr, 128);
 #pragma unroll
   for (int c = 0; c < 3; ++c)
 #pragma unroll

@@ -70,11 +70,21 @@ void v_cast(long n, const Ts* x, Td* y, cudaStream_t s) {
   count();
 }
 
+// The diagonal inverse (fixed over a V-cycle, written only by the
+// preconditioner set-up) of the thread's first entry is loaded before pdl_wait,
+// overlapping the preceding kernel under the V-cycle graphs' programmatic edges.
 template <typename T>
 __global__ void k_cheb_first(long n, const T* __restrict__ b, const T* __restrict__ dinv, T f2, T* __restrict__ d,
                              T* __restrict__ x) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const T d0 = i < n ? dinv[i] : T(0);
   pdl_wait();
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+  if (i < n) {
+    const T v = f2 * d0 * b[i];
+    d[i] = v;
+    x[i] = v;
+  }
+  for (i += (long)gridDim.x * blockDim.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const T v = f2 * dinv[i] * b[i];
     d[i] = v;
     x[i] = v;
