@@ -200,18 +200,42 @@ namespace {
 // 32 rows per block, the columns split over 16 warps: lane = row, warp = slice of
 // columns; the 16 partial sums of a row are added in slice order
 constexpr int kGemvSlices = 16;
+constexpr int kGemvBatch = 16;
 __global__ void __launch_bounds__(32 * kGemvSlices) dense_gemv_colmajor(int n, const float* __restrict__ B,
                                                                        const float* __restrict__ x,
                                                                        float* __restrict__ y) {
-  pdl_wait();
   __shared__ float part[kGemvSlices][32];
   const int lane = threadIdx.x & 31, slice = threadIdx.x >> 5;
   const int row = blockIdx.x * 32 + lane;
   const int chunk = (n + kGemvSlices - 1) / kGemvSlices;
   const int j0 = slice * chunk, j1 = min(n, j0 + chunk);
+  // The matrix entries are loaded kGemvBatch at a time before they are added
+  // (in column order, as one at a time would), so a thread keeps kGemvBatch
+  // loads in flight; the matrix is fixed over a V-cycle, so the first batch is
+  // loaded before pdl_wait and overlaps the preceding kernel.
+  float bv[kGemvBatch];
+  const bool first = row < n && j0 + kGemvBatch <= j1;
+  if (first) {
+#pragma unroll
+    for (int u = 0; u < kGemvBatch; ++u) bv[u] = B[(size_t)(j0 + u) * n + row];
+  }
+  pdl_wait();
   float acc = 0.0f;
-  if (row < n)
-    for (int j = j0; j < j1; ++j) acc += B[(size_t)j * n + row] * x[j];
+  if (row < n) {
+    int j = j0;
+    if (first) {
+#pragma unroll
+      for (int u = 0; u < kGemvBatch; ++u) acc += bv[u] * x[j0 + u];
+      j += kGemvBatch;
+    }
+    for (; j + kGemvBatch <= j1; j += kGemvBatch) {
+#pragma unroll
+      for (int u = 0; u < kGemvBatch; ++u) bv[u] = B[(size_t)(j + u) * n + row];
+#pragma unroll
+      for (int u = 0; u < kGemvBatch; ++u) acc += bv[u] * x[j + u];
+    }
+    for (; j < j1; ++j) acc += B[(size_t)j * n + row] * x[j];
+  }
   part[slice][lane] = acc;
   __syncthreads();
   if (slice == 0 && row < n) {
