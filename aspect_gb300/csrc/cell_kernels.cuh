@@ -1082,9 +1082,11 @@ __device__ __forceinline__ void gather_epilogue(const GatherArgs<T>& a, long g, 
 // Velocity DoFs of a lattice level: a node's cells follow from its coordinates.
 template <typename T, int dim, int epi>
 __global__ void __launch_bounds__(256) velocity_gather_structured(LevelView<T> L, GatherArgs<T> a) {
-  pdl_wait();
   constexpr int nv = Shape<dim>::nv;
   const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  // the diagonal inverse (fixed over a V-cycle) before pdl_wait
+  const T dg = ((epi == EPI_CHEB || epi == EPI_CHEB_OUT) && g < L.n_u) ? a.dinv[g] : T(0);
+  pdl_wait();
   if (g >= L.n_u) return;
   const int comp = (int)(g / L.n_nodes);
   const int node = (int)(g - (long)comp * L.n_nodes);
@@ -1115,7 +1117,7 @@ __global__ void __launch_bounds__(256) velocity_gather_structured(LevelView<T> L
           sum += a.E[(size_t)cell * a.cs + (size_t)(comp * nv + l) * a.ss];
         }
   }
-  gather_epilogue<T, epi>(a, g, sum, constrained);
+  gather_epilogue_dinv<T, epi>(a, g, sum, constrained, dg);
 }
 
 // Velocity DoFs of a 3D lattice level, one thread per Q2 node for all three

@@ -10,6 +10,11 @@ constexpr int kCellThreads = 128;
 // lattice kernel vs lattice_cell_kernel_small: 8 cells 10.3 vs 4.1 us, 64 cells
 // 10.3 vs 5.1, 512 cells 10.3 vs 6.2, 4096 cells 10.3 vs 14.4, 32768 cells 12.3 vs 86.
 constexpr int kSmallLatticeMaxCells = 512;
+// 3D lattice velocity gathers: one thread per node (three components) above
+// this many nodes, one thread per DoF at or below it (the two form the same
+// sums). Measured A-block V-cycle levels: per DoF 8 us faster at 16^3 (33^3
+// nodes) and 3 us at 8^3, per node 65 us faster at 32^3.
+constexpr int kGatherPerNodeMinNodes = 33 * 33 * 33;
 constexpr int kGatherThreads = 256;
 template <int dim>
 int cell_grid(int count) {
@@ -50,7 +55,7 @@ void gather_dim_epi(const LevelView<GB_T>& L, int block, const GatherCsr<GB_T>* 
   const long n = block == 0 ? L.n_u : L.n_p;
   const int g = ceil_div(n, kGatherThreads);
   if (csr) gather_csr<GB_T, epi><<<g, kGatherThreads, 0, s>>>(n, *csr, a);
-  else if (block == 0 && dim == 3)
+  else if (block == 0 && dim == 3 && L.n_nodes > kGatherPerNodeMinNodes)
     velocity_gather_lattice3<GB_T, epi><<<ceil_div(L.n_nodes, kGatherThreads), kGatherThreads, 0, s>>>(L, a);
   else if (block == 0) velocity_gather_structured<GB_T, dim, epi><<<g, kGatherThreads, 0, s>>>(L, a);
   else pressure_gather_structured<GB_T, dim, epi><<<g, kGatherThreads, 0, s>>>(L, a);
