@@ -862,31 +862,18 @@ __constant__ SmallLatticeTables c_small_tables = {
 
 constexpr int kSmallCellThreads = 96;  // 81 active: (component, node)
 
+// The cell pass of the small-level kernel once A[0] holds the cell's 81 nodal
+// values (zero at constrained DoFs) and all threads have passed a barrier.
 template <bool eta_per_q>
-__global__ void __launch_bounds__(kSmallCellThreads) lattice_cell_kernel_small(LevelView<float> L,
-                                                                               const float* __restrict__ src_u,
-                                                                               float* __restrict__ Eu) {
-  // the cell's viscosity (fixed over a V-cycle) before pdl_wait, overlapping the
-  // preceding kernel in the V-cycle graphs' programmatic edges
-  const float eta_pre = threadIdx.x < 27 ? (eta_per_q ? L.eta[(size_t)blockIdx.x * 27 + threadIdx.x] : L.eta[blockIdx.x])
-                                         : 0.0f;
-  pdl_wait();
-  __shared__ float A[2][81];   // nodal / Gauss-point values, ping-pong between sweeps
-  __shared__ float G[9][27];   // G[c*3+d][q] = d u_c / d x_d, then the fluxes R in place
+__device__ __forceinline__ void small_cell_pass(const LevelView<float>& L, int cell, float eta_pre,
+                                                float (&A)[2][81], float (&G)[9][27], float* __restrict__ Eu) {
   const SmallLatticeTables& K = c_small_tables;
-  const int cell = blockIdx.x;
   const int t = threadIdx.x;
   const bool act = t < 81;
   const int c = act ? t / 27 : 0;
   const int n = act ? t - 27 * c : 0;
   const int dig[3] = {n % 3, (n / 3) % 3, n / 9};
   const int st[3] = {1, 3, 9};
-  StructuredCell<float, 3> sc;
-  structured_cell_lex<float, 3>(L, cell, sc);
-  if (act)
-    A[0][t] = structured_zero<float, 3>(L, sc, c, n) ? 0.0f
-                                                     : src_u[c * L.n_nodes + sc.node0 + structured_node_offset<3>(L.Nn, n)];
-  __syncthreads();
   // nodes -> Gauss points, directions 0, 1, 2
   int cur = 0;
 #pragma unroll
@@ -960,6 +947,101 @@ __global__ void __launch_bounds__(kSmallCellThreads) lattice_cell_kernel_small(L
     __syncthreads();
   }
   if (act) Eu[(size_t)(c * 27 + n) * L.n_cells + cell] = A[cur][t];
+}
+
+
+template <bool eta_per_q>
+__global__ void __launch_bounds__(kSmallCellThreads) lattice_cell_kernel_small(LevelView<float> L,
+                                                                               const float* __restrict__ src_u,
+                                                                               float* __restrict__ Eu) {
+  // the cell's viscosity (fixed over a V-cycle) before pdl_wait, overlapping the
+  // preceding kernel in the V-cycle graphs' programmatic edges
+  const float eta_pre = threadIdx.x < 27 ? (eta_per_q ? L.eta[(size_t)blockIdx.x * 27 + threadIdx.x] : L.eta[blockIdx.x])
+                                         : 0.0f;
+  pdl_wait();
+  __shared__ float A[2][81];   // nodal / Gauss-point values, ping-pong between sweeps
+  __shared__ float G[9][27];   // G[c*3+d][q] = d u_c / d x_d, then the fluxes R in place
+  const int cell = blockIdx.x;
+  const int t = threadIdx.x;
+  const bool act = t < 81;
+  const int c = act ? t / 27 : 0;
+  const int n = act ? t - 27 * c : 0;
+  StructuredCell<float, 3> sc;
+  structured_cell_lex<float, 3>(L, cell, sc);
+  if (act)
+    A[0][t] = structured_zero<float, 3>(L, sc, c, n) ? 0.0f
+                                                     : src_u[c * L.n_nodes + sc.node0 + structured_node_offset<3>(L.Nn, n)];
+  __syncthreads();
+  small_cell_pass<eta_per_q>(L, cell, eta_pre, A, G, Eu);
+}
+
+// One Chebyshev step of the FP32 A-block smoother of a small lattice level with
+// the next step's cell pass fused in (one launch instead of a gather and a cell
+// pass): each block gathers its cell's 81 DoFs from the previous cell pass's
+// contributions E (the sum of structured_dof_sum, as the gathers form it), runs
+// the Chebyshev update of the gathers' epilogue (first: the zero-start step
+// d = f2 dinv b, x = d), writes the DoFs whose owner it is (a node belongs to
+// the cell holding it at local coordinate 0 or 1 along every direction, or 2
+// on the level's upper faces) to the other buffers of a ping-pong pair, and
+// runs the cell pass on the new values into E_out. Shared nodes are updated by
+// up to eight blocks with the same arithmetic; only the owner stores.
+template <typename T, int dim>
+__device__ __forceinline__ T structured_dof_sum(const LevelView<T>& L, const T* __restrict__ E, int cs, int ss,
+                                                int comp, int node, bool& constrained);
+struct ChebSmallArgs {
+  const float* E;      // slot-major contributions of the previous cell pass (not read when first)
+  float* E_out;        // slot-major contributions of this step's cell pass
+  const float* x_in;
+  const float* d_in;
+  float* x_out;
+  float* d_out;
+  const float* b;
+  const float* dinv;
+  float f1, f2;
+};
+template <bool first, bool eta_per_q>
+__global__ void __launch_bounds__(kSmallCellThreads) lattice_cheb_small(LevelView<float> L, ChebSmallArgs a) {
+  const int cell = blockIdx.x;
+  const int t = threadIdx.x;
+  const bool act = t < 81;
+  const int c = act ? t / 27 : 0;
+  const int n = act ? t - 27 * c : 0;
+  StructuredCell<float, 3> sc;
+  structured_cell_lex<float, 3>(L, cell, sc);
+  const int node = sc.node0 + structured_node_offset<3>(L.Nn, n);
+  const long g = (long)c * L.n_nodes + node;
+  // fixed over a V-cycle: viscosity and diagonal before pdl_wait
+  const float eta_pre = t < 27 ? (eta_per_q ? L.eta[(size_t)cell * 27 + t] : L.eta[cell]) : 0.0f;
+  const float dg = act ? a.dinv[g] : 0.0f;
+  pdl_wait();
+  __shared__ float A[2][81];
+  __shared__ float G[9][27];
+  if (act) {
+    float xn, dn;
+    if (first) {
+      dn = a.f2 * dg * a.b[g];
+      xn = dn;
+    } else {
+      bool cons = false;
+      const float sum = structured_dof_sum<float, 3>(L, a.E, 1, L.n_cells, c, node, cons);
+      const float xg = a.x_in[g];
+      const float tt = cons ? xg : sum;
+      dn = a.f1 * a.d_in[g] + a.f2 * dg * (a.b[g] - tt);
+      xn = xg + dn;
+    }
+    const int gi[3] = {2 * sc.i + n % 3, 2 * sc.j + (n / 3) % 3, 2 * sc.k + n / 9};
+    const int ci[3] = {sc.i, sc.j, sc.k};
+    bool owner = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) owner = owner && ci[d] == min(gi[d] >> 1, L.nc[d] - 1);
+    if (owner) {
+      a.x_out[g] = xn;
+      a.d_out[g] = dn;
+    }
+    A[0][t] = structured_zero<float, 3>(L, sc, c, n) ? 0.0f : xn;
+  }
+  __syncthreads();
+  small_cell_pass<eta_per_q>(L, cell, eta_pre, A, G, a.E_out);
 }
 
 // (generic loads: the rows may live in global or in shared memory)
@@ -1080,19 +1162,16 @@ __device__ __forceinline__ void gather_epilogue(const GatherArgs<T>& a, long g, 
 }
 
 // Velocity DoFs of a lattice level: a node's cells follow from its coordinates.
-template <typename T, int dim, int epi>
-__global__ void __launch_bounds__(256) velocity_gather_structured(LevelView<T> L, GatherArgs<T> a) {
+// Sum of the per-cell contributions E (cell stride cs, slot stride ss) of
+// velocity DoF (comp, node) of a lattice level, lower cell first along z, y, x;
+// constrained: the DoF is on a zero face (the sum is then 0).
+template <typename T, int dim>
+__device__ __forceinline__ T structured_dof_sum(const LevelView<T>& L, const T* __restrict__ E, int cs, int ss,
+                                                int comp, int node, bool& constrained) {
   constexpr int nv = Shape<dim>::nv;
-  const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  // the diagonal inverse (fixed over a V-cycle) before pdl_wait
-  const T dg = ((epi == EPI_CHEB || epi == EPI_CHEB_OUT) && g < L.n_u) ? a.dinv[g] : T(0);
-  pdl_wait();
-  if (g >= L.n_u) return;
-  const int comp = (int)(g / L.n_nodes);
-  const int node = (int)(g - (long)comp * L.n_nodes);
   const int gc[3] = {node % L.Nn[0], (node / L.Nn[0]) % L.Nn[1], dim == 3 ? node / (L.Nn[0] * L.Nn[1]) : 0};
   int cidx[3][2], loc[3][2], cnt[3];
-  bool constrained = false;
+  constrained = false;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     cnt[d] = 0;
@@ -1114,9 +1193,23 @@ __global__ void __launch_bounds__(256) velocity_gather_structured(LevelView<T> L
         for (int kx = 0; kx < cnt[0]; ++kx) {
           const int cell = (cidx[2][kz] * L.nc[1] + cidx[1][ky]) * L.nc[0] + cidx[0][kx];
           const int l = loc[0][kx] + 3 * loc[1][ky] + 9 * loc[2][kz];
-          sum += a.E[(size_t)cell * a.cs + (size_t)(comp * nv + l) * a.ss];
+          sum += E[(size_t)cell * cs + (size_t)(comp * nv + l) * ss];
         }
   }
+  return sum;
+}
+
+template <typename T, int dim, int epi>
+__global__ void __launch_bounds__(256) velocity_gather_structured(LevelView<T> L, GatherArgs<T> a) {
+  const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  // the diagonal inverse (fixed over a V-cycle) before pdl_wait
+  const T dg = ((epi == EPI_CHEB || epi == EPI_CHEB_OUT) && g < L.n_u) ? a.dinv[g] : T(0);
+  pdl_wait();
+  if (g >= L.n_u) return;
+  const int comp = (int)(g / L.n_nodes);
+  const int node = (int)(g - (long)comp * L.n_nodes);
+  bool constrained = false;
+  const T sum = structured_dof_sum<T, dim>(L, a.E, a.cs, a.ss, comp, node, constrained);
   gather_epilogue_dinv<T, epi>(a, g, sum, constrained, dg);
 }
 

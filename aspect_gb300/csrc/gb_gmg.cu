@@ -783,6 +783,119 @@ void build_a_dense(Handle& H) {
   H.a_dense_top = K;
 }
 
+// FP32 A-block smoothing of small lattice levels with fused steps
+// (lattice_cheb_small): each Chebyshev step's gather and the next step's cell
+// pass in one launch, the iterate, direction and contributions in ping-pong
+// pairs (sol/xalt, dA/dalt, Eu/Ealt). The same steps, coefficients, sums and
+// residual as chebyshev() + level_op_resid(); pre-smoothing and residual in
+// degree + 1 launches instead of 2 degree + 1, post-smoothing in degree + 1
+// instead of 2 degree.
+bool small_fused_level(Handle& H, int lev, int block) {
+  Level& L = H.levels[lev];
+  return block == 0 && H.opt.fused_small_smoother && L.f32.xalt.p && L.fused_tz == 0 &&
+         small_lattice_a_level(L.view<float>(H.s, H.compressible));
+}
+// Chebyshev step coefficients (f1, f2) of a level, step 0 first (chebyshev())
+std::vector<std::pair<float, float>> cheb_steps(Handle& H, int lev, int block) {
+  const ChebParams cp = cheb_params(H, lev);
+  double theta, delta;
+  chebyshev_bounds<float>(H, lev, block, theta, delta);
+  std::vector<std::pair<float, float>> c;
+  c.push_back({0.0f, (float)(1.0 / theta)});
+  double rhok = delta / theta;
+  const double sigma = theta / delta;
+  for (int k = 1; k < cp.degree; ++k) {
+    const double rhokp = 1.0 / (2.0 * sigma - rhok);
+    c.push_back({(float)(rhokp * rhok), (float)(2.0 * rhokp / delta)});
+    rhok = rhokp;
+  }
+  return c;
+}
+// pre-smoothing from a zero start, then t = b - A sol
+void small_presmooth_resid(Handle& H, int lev, float* sol, const float* b, float* t) {
+  Level& L = H.levels[lev];
+  LevelDev<float>& D = L.f32;
+  const LevelView<float> v = L.view<float>(H.s, H.compressible);
+  const std::vector<std::pair<float, float>> c = cheb_steps(H, lev, 0);
+  float* X[2] = {sol, D.xalt.p};
+  float* Dv[2] = {D.dA.p, D.dalt.p};
+  float* E[2] = {D.Eu.p, D.Ealt.p};
+  ChebSmallArgs a{};
+  a.b = b;
+  a.dinv = D.dinvA.p;
+  a.x_out = X[1];
+  a.d_out = Dv[1];
+  a.E_out = E[0];
+  a.f1 = 0.0f;
+  a.f2 = c[0].second;
+  launch_cheb_small(v, true, a, H.st);
+  ++H.cell_launches;
+  int cx = 1, ce = 0;
+  for (size_t k = 1; k < c.size(); ++k) {
+    a.E = E[ce];
+    a.x_in = X[cx];
+    a.d_in = Dv[cx];
+    a.x_out = X[cx ^ 1];
+    a.d_out = Dv[cx ^ 1];
+    a.E_out = E[ce ^ 1];
+    a.f1 = c[k].first;
+    a.f2 = c[k].second;
+    launch_cheb_small(v, false, a, H.st);
+    ++H.cell_launches;
+    cx ^= 1;
+    ce ^= 1;
+  }
+  GatherArgs<float> g{};
+  g.E = E[ce];
+  g.x = X[cx];
+  g.b = b;
+  g.y = t;
+  gather<float>(H, L, v, 0, EPI_RESID, g, OPK_A);
+  if (X[cx] != sol) v_copy<float>(L.n_u, X[cx], sol, H.st);
+}
+// post-smoothing from sol
+void small_postsmooth(Handle& H, int lev, float* sol, const float* b) {
+  Level& L = H.levels[lev];
+  LevelDev<float>& D = L.f32;
+  const LevelView<float> v = L.view<float>(H.s, H.compressible);
+  const std::vector<std::pair<float, float>> c = cheb_steps(H, lev, 0);
+  float* X[2] = {sol, D.xalt.p};
+  float* Dv[2] = {D.dA.p, D.dalt.p};
+  float* E[2] = {D.Eu.p, D.Ealt.p};
+  launch_cell_pass<float>(v, OPK_A, sol, sol, E[0], D.Ep.p, H.st);
+  ++H.cell_launches;
+  int cx = 0, ce = 0;
+  ChebSmallArgs a{};
+  a.b = b;
+  a.dinv = D.dinvA.p;
+  for (size_t k = 0; k + 1 < c.size(); ++k) {
+    a.E = E[ce];
+    a.x_in = X[cx];
+    a.d_in = Dv[cx];
+    a.x_out = X[cx ^ 1];
+    a.d_out = Dv[cx ^ 1];
+    a.E_out = E[ce ^ 1];
+    a.f1 = c[k].first;
+    a.f2 = c[k].second;
+    launch_cheb_small(v, false, a, H.st);
+    ++H.cell_launches;
+    cx ^= 1;
+    ce ^= 1;
+  }
+  GatherArgs<float> g{};
+  g.E = E[ce];
+  g.x = X[cx];
+  g.y = X[cx ^ 1];
+  g.b = b;
+  g.dinv = D.dinvA.p;
+  g.d = Dv[cx];
+  g.f1 = c.back().first;
+  g.f2 = c.back().second;
+  gather<float>(H, L, v, 0, EPI_CHEB_OUT, g, OPK_A);
+  cx ^= 1;
+  if (X[cx] != sol) v_copy<float>(L.n_u, X[cx], sol, H.st);
+}
+
 template <typename T>
 void vcycle_level(Handle& H, int lev, int block) {
   if constexpr (std::is_same<T, float>::value) {
@@ -819,8 +932,15 @@ void vcycle_level(Handle& H, int lev, int block) {
   T* csol = block == 0 ? DC.solA.p : DC.solM.p;
   T* cdef = block == 0 ? DC.defA.p : DC.defM.p;
   const long nc = block == 0 ? C.n_u : C.n_p;
-  smoother_apply<T>(H, lev, block, sol, def);
-  level_op_resid<T>(H, lev, block, sol, def, t);
+  bool fused = false;
+  if constexpr (std::is_same<T, float>::value) fused = small_fused_level(H, lev, block);
+  if constexpr (std::is_same<T, float>::value) {
+    if (fused) small_presmooth_resid(H, lev, sol, def, t);
+  }
+  if (!fused) {
+    smoother_apply<T>(H, lev, block, sol, def);
+    level_op_resid<T>(H, lev, block, sol, def, t);
+  }
   // restriction (zero fill and product in one launch)
   if (L.xfer_lattice[block]) lattice_restrict<T>(L.xfer[block], t, cdef, H.st);
   else if (block == 0) v_spmv_set<T>(L.PuT_rows, nc, L.PuT_ptr.p, L.PuT_col.p, D.PuT_val.p, t, cdef, H.st);
@@ -831,6 +951,12 @@ void vcycle_level(Handle& H, int lev, int block) {
   if (L.xfer_lattice[block]) lattice_prolong_add<T>(L.xfer[block], csol, sol, H.st);
   else if (block == 0) v_spmv_add<T>(L.Pu_rows, L.Pu_ptr.p, L.Pu_col.p, D.Pu_val.p, csol, sol, H.st);
   else v_spmv_add<T>(L.Pp_rows, L.Pp_ptr.p, L.Pp_col.p, D.Pp_val.p, csol, sol, H.st);
+  if constexpr (std::is_same<T, float>::value) {
+    if (fused) {
+      small_postsmooth(H, lev, sol, def);
+      return;
+    }
+  }
   smoother_smooth<T>(H, lev, block, sol, def);
 }
 
@@ -1714,6 +1840,7 @@ void gb_gmg_default_options(gb_gmg_options* o) {
   // worth it only when several solves share one build.
   o->dense_mass_cycle_nodes = gb::kMaxDenseBottomNodes;
   o->dense_a_cycle_dofs = gb::kMaxDenseANodes;
+  o->fused_small_smoother = 1;
 }
 
 void gb_gmg_default_solve_params(gb_gmg_solve_params* p) {
@@ -1856,6 +1983,18 @@ int gb_gmg_finalize_setup(gb_gmg* g) {
                      H.levels[l].xfer_lattice[0] ? "lattice" : "csr", H.levels[l].xfer_lattice[1] ? "lattice" : "csr");
     }
     gb::setup_coefficient_maps(H.levels);
+    for (auto& L : H.levels) {  // ping-pong halves of the fused small-level smoother
+      L.f32.xalt.release();
+      L.f32.dalt.release();
+      L.f32.Ealt.release();
+      if (!gb::small_lattice_a_level(L.view<float>(1.0, 0))) continue;
+      L.f32.xalt.alloc(L.n_u);
+      L.f32.dalt.alloc(L.n_u);
+      L.f32.Ealt.alloc((size_t)L.n_cells * 81);
+      GB_CUDA(cudaMemsetAsync(L.f32.xalt.p, 0, L.n_u * sizeof(float), H.st));
+      GB_CUDA(cudaMemsetAsync(L.f32.dalt.p, 0, L.n_u * sizeof(float), H.st));
+      GB_CUDA(cudaMemsetAsync(L.f32.Ealt.p, 0, (size_t)L.n_cells * 81 * sizeof(float), H.st));
+    }
     for (auto& L : H.levels) {  // FP32 A-block applications of large lattice levels: fused kernel
       L.fused_tz = 0;
       L.f32.Fa.release();

@@ -189,4 +189,22 @@ void launch_mass_diag<GB_T>(const LevelView<GB_T>& L, int colour, int begin, int
   else mass_diag_kernel<GB_T, 2><<<g, kCellThreads, 0, s>>>(L, colour, begin, count, pr.ptr, pr.g, pr.eptr, pr.li, pr.w, diag);
 }
 
+#if defined(GB_T_IS_FLOAT)
+bool small_lattice_a_level(const LevelView<float>& L) {
+  return cell_pass_slot_major<float>(L, OPK_A) && L.n_cells <= kSmallLatticeMaxCells && L.deg == 2;
+}
+void launch_cheb_small(const LevelView<float>& L, bool first, const ChebSmallArgs& a, cudaStream_t s) {
+  if (L.n_cells <= 0) return;
+  const bool pq = L.eta_n != 1;
+  if (first) {
+    if (pq) lattice_cheb_small<true, true><<<L.n_cells, kSmallCellThreads, 0, s>>>(L, a);
+    else lattice_cheb_small<true, false><<<L.n_cells, kSmallCellThreads, 0, s>>>(L, a);
+  } else {
+    if (pq) lattice_cheb_small<false, true><<<L.n_cells, kSmallCellThreads, 0, s>>>(L, a);
+    else lattice_cheb_small<false, false><<<L.n_cells, kSmallCellThreads, 0, s>>>(L, a);
+  }
+  GB_CUDA(cudaGetLastError());
+}
+#endif
+
 }  // namespace gb

@@ -61,6 +61,9 @@ struct LevelDev {
   DevBuf<T> eta_active;  // finest level without averaging: per-point table of the outer operators
   // V-cycle work vectors (A block: n_u, Schur block: n_p)
   DevBuf<T> solA, defA, tA, dA, solM, defM, tM, dM;
+  // the other halves of the iterate, direction and contribution ping-pong pairs
+  // of the fused small-level A-block smoother (FP32 small lattice levels only)
+  DevBuf<T> xalt, dalt, Ealt;
   double eigA[2] = {0, 0}, eigM[2] = {0, 0};
   bool eig_given[2] = {false, false};
 };

@@ -25,6 +25,11 @@ void launch_cell_pass(const LevelView<T>& L, int op, const T* src_u, const T* sr
 template <typename T>
 void launch_gather(const LevelView<T>& L, int block, int epi, const GatherCsr<T>* csr, const GatherArgs<T>& a,
                    cudaStream_t s);
+// FP32 A-block levels whose cell pass is the one-cell-per-block small-level
+// kernel (the levels lattice_cheb_small serves)
+bool small_lattice_a_level(const LevelView<float>& L);
+// one fused Chebyshev step (gather, update, next cell pass) of such a level
+void launch_cheb_small(const LevelView<float>& L, bool first, const ChebSmallArgs& a, cudaStream_t s);
 // one-pass pressure mass operator of a lattice level (Mc: per-cell local matrices)
 template <typename T>
 void launch_mass_lattice(const LevelView<T>& L, const T* Mc, int epi, const GatherArgs<T>& a, cudaStream_t s);

@@ -49,7 +49,7 @@ class Options(ctypes.Structure):
                 ("coarse_eig_cg_iterations", ctypes.c_int), ("schur_smoothing_steps", ctypes.c_int),
                 ("force_indexed_layout", ctypes.c_int), ("coarse_solver", ctypes.c_int),
                 ("fused_a_min_cells", ctypes.c_int), ("dense_mass_cycle_nodes", ctypes.c_int),
-                ("dense_a_cycle_dofs", ctypes.c_int)]
+                ("dense_a_cycle_dofs", ctypes.c_int), ("fused_small_smoother", ctypes.c_int)]
 
 
 class SolveParams(ctypes.Structure):

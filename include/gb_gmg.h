@@ -132,6 +132,10 @@ typedef struct gb_gmg_options {
   int dense_a_cycle_dofs;       /* the same for the FP32 A-block V-cycle: lattice levels
                                    up to the highest one with at most this many velocity
                                    DoFs (<= 2200; 2200; 0: off)                        */
+  int fused_small_smoother;     /* 1: the FP32 A-block smoother of small lattice levels
+                                   (one-cell-per-block cell pass) runs each Chebyshev
+                                   step's gather and the next step's cell pass as one
+                                   launch (the same arithmetic; 1); 0: two launches  */
 } gb_gmg_options;
 
 enum gb_gmg_coarse_solver {
