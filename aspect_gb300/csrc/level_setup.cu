@@ -758,7 +758,8 @@ size_t Level::device_bytes() const {
          D.pprobe_w.bytes() + D.Pu_val.bytes() + D.PuT_val.bytes() + D.Pp_val.bytes() + D.PpT_val.bytes() +
          D.dinvA.bytes() + D.dinvM.bytes() + D.solA.bytes() + D.defA.bytes() + D.tA.bytes() + D.dA.bytes() +
          D.solM.bytes() + D.defM.bytes() + D.tM.bytes() + D.dM.bytes() + D.gu_w.bytes() + D.gp_w.bytes() +
-         D.Eu.bytes() + D.Ep.bytes() + D.Mp.bytes() + D.Fa.bytes() + D.eta_active.bytes();
+         D.Eu.bytes() + D.Ep.bytes() + D.Mp.bytes() + D.Fa.bytes() + D.eta_active.bytes() + D.xalt.bytes() +
+         D.dalt.bytes() + D.Ealt.bytes();
   };
   b += ioc_d.bytes() + kid_ptr_d.bytes() + kid_d.bytes() + child_d.bytes() + jxw_d.bytes() + eta_in_d.bytes() +
        dg_d.bytes();
