@@ -5,9 +5,10 @@ counts and solutions within 1e-10 relative (the passes differ in the last
 ~10 bits of each Hessenberg entry, far below the 1e-8 solver tolerance), for
 FP64 and FP32 V-cycles, odd and even system sizes, short restarts (every
 restart begins with an FP64 step that sets the scale of the next one), the
-flexible and the non-flexible cheap solver and GMRES-IR; and the float-pair
+flexible and the non-flexible cheap solver and GMRES-IR; the float-pair
 FP64-MG solve against the oracle's solve within 1e-8 with its FP64 residual
-under the tolerance."""
+under the tolerance; and a restart cycle longer than 128 steps (FP64 passes
+after the 128th basis vector)."""
 import numpy as np
 import pytest
 
@@ -74,3 +75,24 @@ def test_orthogonalization_value_is_checked():
     g = gmg.from_problem(P)
     with pytest.raises(gmg.GmgError):
         g.solve(P.rhs, orthogonalization=2)
+
+
+def test_float_pair_beyond_128_basis_vectors():
+    """Spherical shell (about 190 iterations) with restart 200: the Arnoldi steps
+    past 128 basis vectors run the FP64 passes inside a float-pair solve, the
+    float-pair steps before them; the solution's FP64 residual, measured by the
+    oracle, meets the tolerance and the iteration count matches the FP64
+    passes' within one."""
+    P = problems.spherical_shell(2)
+    g = gmg.from_problem(P, options={"coarse_solver": gmg.COARSE_DENSE_FP64})
+    xa, oa = g.solve(P.rhs, linear_solver_tolerance=1e-8, mg_precision=gmg.FP32, restart=200,
+                     orthogonalization=GS_FLOAT_PAIR)
+    xb, ob = g.solve(P.rhs, linear_solver_tolerance=1e-8, mg_precision=gmg.FP32, restart=200,
+                     orthogonalization=GS_FP64)
+    assert oa["status"] == 0 and ob["status"] == 0
+    assert oa["cheap_iterations"] > 130, oa
+    assert abs(oa["cheap_iterations"] - ob["cheap_iterations"]) <= 1, (oa, ob)
+    o = Oracle(P.levels)
+    o.set_viscosity(P.eta, P.projection, P.pressure_scaling)
+    r = P.rhs - o.vmult(0, len(P.levels) - 1, xa)
+    assert np.linalg.norm(r) <= 1.01 * oa["solver_tolerance"]
