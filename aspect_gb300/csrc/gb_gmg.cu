@@ -98,6 +98,9 @@ struct Handle {
   double eta_min = 0, eta_max = 0;
   bool setup_done = false, visc_done = false;
   bool prec_done[2] = {false, false};  // per precision (0 fp64, 1 fp32)
+  // build_preconditioner ran but left the FP64 levels (diagonals, eigenvalue
+  // estimates) to their first use: a solve with FP32 V-cycles never needs them
+  bool fp64_pending = false;
   long long cell_launches = 0;
   // staging and FP64 active-level workspace
   DevBuf<double> stage_a, stage_b, partial, dots_d;
@@ -112,6 +115,9 @@ struct Handle {
   DevBuf<float2> Vs;
   long lds = 0;
   DevBuf<int> gs_shift;
+  // eigenvalue-estimate CG: device scalars and alpha/beta history, flags
+  DevBuf<double> eig_s;
+  DevBuf<int> eig_f;
   DevBuf<double> cg_r, cg_z, cg_p, cg_q, cg_x;
   DevBuf<float> f32_a, f32_b;
   int restart_alloc = -1;
@@ -465,26 +471,35 @@ void estimate_eigenvalues(Handle& H, int lev, int block) {
   T* Ap = block == 0 ? D.tA.p : D.tM.p;
   const T* dinv = block == 0 ? D.dinvA.p : D.dinvM.p;
   GB_CUDA(cudaMemcpyAsync(r, b.data(), n * sizeof(T), cudaMemcpyHostToDevice, H.st));
-  // z = D^-1 r ; p = z
-  v_cheb_first<T>(n, r, dinv, T(1), p, z, H.st);
-  double rz = dot_host_T<T>(H, n, r, z);
-  std::vector<double> alphas, betas;
-  for (int it = 0; it < cp.eig_its; ++it) {
+  // CG with the scalars on the device (v_eig_step): alpha = r.z / p.Ap, r -= alpha Ap,
+  // stop when |r| < 1e-2 (SolverControl(eig_cg_n_iterations, 1e-2), absolute),
+  // z = D^-1 r, beta = r.z new / r.z, p = z + beta p; the host looks at the
+  // running flag every kEigCheck steps and reads the alpha/beta history once
+  const int its = cp.eig_its;
+  if (H.eig_s.n < (size_t)(kEigHist + 2 * its)) H.eig_s.alloc(kEigHist + 2 * its);
+  if (H.eig_f.n < 3) H.eig_f.alloc(3);
+  double* sd = H.eig_s.p;
+  int* fd = H.eig_f.p;
+  v_eig_start(fd, H.st);
+  v_cheb_first<T>(n, r, dinv, T(1), p, z, H.st);  // z = D^-1 r ; p = z
+  v_dot<T>(n, r, z, sd, H.partial.p, H.st);       // s[0] = r.z
+  constexpr int kEigCheck = 8;
+  int flags[3] = {1, 0, 0};
+  for (int it = 0; it < its; ++it) {
     level_op<T>(H, lev, block, p, Ap);
-    const double pAp = dot_host_T<T>(H, n, p, Ap);
-    if (!(pAp > 0)) break;
-    const double alpha = rz / pAp;
-    alphas.push_back(alpha);
-    v_axpby<T>(n, (T)(-alpha), Ap, T(1), r, H.st);  // r -= alpha Ap
-    // SolverControl(eig_cg_n_iterations, eig_cg_residual = 1e-2), absolute
-    if (std::sqrt(dot_host_T<T>(H, n, r, r)) < 1e-2) break;
-    v_cheb_first<T>(n, r, dinv, T(1), Ap, z, H.st);  // z = D^-1 r (Ap used as scratch)
-    const double rz_new = dot_host_T<T>(H, n, r, z);
-    const double beta = rz_new / rz;
-    betas.push_back(beta);
-    rz = rz_new;
-    v_axpby<T>(n, T(1), z, (T)beta, p, H.st);  // p = z + beta p
+    v_eig_step<T>(n, p, Ap, r, z, dinv, sd, fd, its, H.partial.p, H.st);
+    if ((it + 1) % kEigCheck == 0 && it + 1 < its) {
+      GB_CUDA(cudaMemcpyAsync(flags, fd, sizeof(int), cudaMemcpyDeviceToHost, H.st));
+      GB_CUDA(cudaStreamSynchronize(H.st));
+      if (flags[0] == 0) break;
+    }
   }
+  std::vector<double> hist(kEigHist + 2 * its);
+  GB_CUDA(cudaMemcpyAsync(flags, fd, 3 * sizeof(int), cudaMemcpyDeviceToHost, H.st));
+  GB_CUDA(cudaMemcpyAsync(hist.data(), sd, hist.size() * sizeof(double), cudaMemcpyDeviceToHost, H.st));
+  GB_CUDA(cudaStreamSynchronize(H.st));
+  const std::vector<double> alphas(hist.begin() + kEigHist, hist.begin() + kEigHist + flags[1]);
+  const std::vector<double> betas(hist.begin() + kEigHist + its, hist.begin() + kEigHist + its + flags[2]);
   const int k = (int)alphas.size();
   std::vector<double> dd(k), ee(k, 0.0);
   for (int i = 0; i < k; ++i) {
@@ -1682,6 +1697,18 @@ void build_preconditioner_T(Handle& H) {
   GB_CUDA(cudaStreamSynchronize(H.st));
 }
 
+// The FP64 levels of the last build_preconditioner, built on their first use.
+void ensure_fp64(Handle& H) {
+  if (H.prec_done[0] || !H.fp64_pending) return;
+  build_preconditioner_T<double>(H);
+  H.prec_done[0] = true;
+  H.fp64_pending = false;
+}
+// ensure_fp64 when `precision` is FP64
+void ensure_precision(Handle& H, int precision) {
+  if (precision != GB_GMG_FP32) ensure_fp64(H);
+}
+
 void to_internal(Handle& H, int lev, const double* d_caller, double* d_internal, bool with_u, bool with_p) {
   Level& L = H.levels[lev];
   if (with_u) v_permute_scatter<double, double>(L.n_u, L.perm_u_d.p, d_caller, d_internal, H.st);
@@ -1703,6 +1730,7 @@ void solve_internal(Handle& H, const gb_gmg_solve_params* P, gb_gmg_outputs* out
   double* x = H.cg_x.p;   // solution (internal)
   double* b = H.bv.p;     // rhs (internal)
   const int prec = P->mg_precision;
+  ensure_precision(H, prec);
   GB_CHECK(H.prec_done[prec == GB_GMG_FP32 ? 1 : 0], GB_GMG_NOT_READY, "build_preconditioner has not been called");
   // constrained entries of the initial guess are zero during the solve
   v_zero_indexed<double>((long)F.cons_u.size(), F.cons_u_d.p, x, H.st);
@@ -2021,6 +2049,7 @@ int gb_gmg_finalize_setup(gb_gmg* g) {
     H.setup_done = true;
     H.visc_done = false;
     H.prec_done[0] = H.prec_done[1] = false;
+    H.fp64_pending = false;
   })
 }
 
@@ -2044,6 +2073,7 @@ int gb_gmg_set_viscosity(gb_gmg* g, const double* eta, int n_per_cell, int proje
     H.reset_graphs();
     H.visc_done = true;
     H.prec_done[0] = H.prec_done[1] = false;
+    H.fp64_pending = false;
   })
 }
 
@@ -2057,6 +2087,9 @@ int gb_gmg_update_viscosity(gb_gmg* g, const double* eta, int n_per_cell) {
     // V-cycles all assume the layout of the last set_viscosity: a different one
     // is rejected before anything changes.
     GB_CHECK(n_per_cell == H.visc_n_per_cell, 1, "viscosity layout differs from the last set_viscosity");
+    // the kept preconditioner is the one of the old tables in both precisions:
+    // FP64 levels left to their first use are built now
+    gb::ensure_fp64(H);
     // the values are checked before any table changes; the tables keep their
     // sizes, so device addresses (and captured graphs) stay valid
     double mn, mx;
@@ -2212,9 +2245,15 @@ int gb_gmg_build_preconditioner(gb_gmg* g) {
     Handle& H = g->h;
     GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
     H.reset_graphs();
-    gb::build_preconditioner_T<double>(H);
-    if (H.opt.coarse_solver == GB_GMG_COARSE_DENSE_FP64) gb::build_dense_coarse(H);
-    H.prec_done[0] = true;
+    H.prec_done[0] = H.prec_done[1] = false;
+    H.fp64_pending = false;
+    if (H.opt.coarse_solver == GB_GMG_COARSE_DENSE_FP64) {
+      gb::build_preconditioner_T<double>(H);
+      gb::build_dense_coarse(H);
+      H.prec_done[0] = true;
+    } else {
+      H.fp64_pending = true;  // gb::ensure_fp64 builds them on first use
+    }
     gb::build_preconditioner_T<float>(H);
     H.mass_bottom_top = gb::plan_mass_bottom(H);
     H.prec_done[1] = true;
@@ -2390,6 +2429,7 @@ int gb_gmg_get_diagonal_inverse(gb_gmg* g, int level, int block, int precision, 
   ABI_TRY(g, {
     Handle& H = g->h;
     const int pi = precision == GB_GMG_FP32 ? 1 : 0;
+    gb::ensure_precision(H, precision);
     GB_CHECK(H.prec_done[pi], GB_GMG_NOT_READY, "build_preconditioner has not been called");
     gb::Level& L = H.levels.at(level);
     const std::vector<int>& perm = block == 0 ? L.perm_u : L.perm_p;
@@ -2407,6 +2447,7 @@ int gb_gmg_get_diagonal_inverse(gb_gmg* g, int level, int block, int precision, 
 int gb_gmg_get_eigenvalues(gb_gmg* g, int level, int block, int precision, double* mm) {
   if (!g) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
+    gb::ensure_precision(g->h, precision);
     gb::Level& L = g->h.levels.at(level);
     const double* e = precision == GB_GMG_FP32 ? (block == 0 ? L.f32.eigA : L.f32.eigM)
                                                : (block == 0 ? L.f64.eigA : L.f64.eigM);
@@ -2491,6 +2532,7 @@ int gb_gmg_vcycle(gb_gmg* g, int block, int precision, const double* src, double
   if (!g) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
     Handle& H = g->h;
+    gb::ensure_precision(H, precision);
     GB_CHECK(H.prec_done[precision == GB_GMG_FP32 ? 1 : 0], GB_GMG_NOT_READY, "build_preconditioner missing");
     const int top = H.n_levels - 1;
     gb::Level& F = H.levels[top];
@@ -2509,6 +2551,7 @@ int gb_gmg_block_preconditioner(gb_gmg* g, int precision, const double* src, dou
   if (!g) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
     Handle& H = g->h;
+    gb::ensure_precision(H, precision);
     GB_CHECK(H.prec_done[precision == GB_GMG_FP32 ? 1 : 0], GB_GMG_NOT_READY, "build_preconditioner missing");
     const int top = H.n_levels - 1;
     const long n = H.n_top();
@@ -2603,7 +2646,10 @@ int gb_gmg_time_operation(gb_gmg* g, int what, int precision, int repeats, doubl
     Handle& H = g->h;
     const int pi = precision == GB_GMG_FP32 ? 1 : 0;
     GB_CHECK(what >= 0 && what <= 7, 1, "unknown operation");
-    if (what >= 3 && what <= 5) GB_CHECK(H.prec_done[pi], GB_GMG_NOT_READY, "build_preconditioner has not been called");
+    if (what >= 3 && what <= 5) {
+      gb::ensure_precision(H, precision);
+      GB_CHECK(H.prec_done[pi], GB_GMG_NOT_READY, "build_preconditioner has not been called");
+    }
     else GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
     const int top = H.n_levels - 1;
     gb::Level& F = H.levels[top];

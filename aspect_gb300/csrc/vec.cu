@@ -995,6 +995,121 @@ void v_dot(long n, const T* a, const T* b, double* out_dev, double* partial, cud
   VecCounter::launches() += 1;
 }
 
+// ---------------------------------------------------------------- eigenvalue-estimate CG
+// The CG of PreconditionChebyshev's eigenvalue estimate with every scalar on the
+// device: per step, besides the level operator, four launches, each fusing a
+// vector update, a reduction with k_dot's grid and order and the step's scalar
+// bookkeeping in the block that finishes the reduction. The vector updates are
+// written as k_axpby and k_cheb_first write theirs (runtime coefficients), so
+// the iterates, dots and alpha/beta history equal those of the host-driven loop.
+//   s: [0] r.z, [1] p.Ap, [2] r.r, [3] new r.z, [4] alpha, [5] beta,
+//      [kEigHist ..) alphas, [kEigHist + its ..) betas
+//   f: [0] running, [1] alphas stored, [2] betas stored
+// A step that finds p.Ap <= 0 stops before storing alpha, one that finds
+// |r| < 1e-2 after storing alpha (SolverControl(its, 1e-2), absolute); later
+// launches see f[0] = 0 and return.
+template <typename T>
+__global__ void __launch_bounds__(kDotThreads) k_eig_pap(long n, const T* __restrict__ p, const T* __restrict__ Ap,
+                                                         double* s, int* f, double* partial, unsigned* counter) {
+  pdl_wait();
+  if (f[0] == 0) return;
+  double acc[1] = {0};
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    acc[0] += (double)p[i] * (double)Ap[i];
+  block_reduce_store<1>(acc, 1, partial, kDotBlocks);
+  if (!arrive_last(counter)) return;
+  finish_partials(partial, 1, s + 1, counter);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double pAp = s[1];
+    if (!(pAp > 0)) {
+      f[0] = 0;
+    } else {
+      const double alpha = s[0] / pAp;
+      s[4] = alpha;
+      s[kEigHist + f[1]] = alpha;
+      f[1] += 1;
+    }
+  }
+}
+// r = (-alpha) Ap + b r (b = 1) and r.r
+template <typename T>
+__global__ void __launch_bounds__(kDotThreads) k_eig_r(long n, const T* __restrict__ Ap, T* __restrict__ r, T b,
+                                                       double* s, int* f, double* partial, unsigned* counter) {
+  pdl_wait();
+  if (f[0] == 0) return;
+  const T a = (T)(-s[4]);
+  double acc[1] = {0};
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const T v = a * Ap[i] + b * r[i];
+    r[i] = v;
+    acc[0] += (double)v * (double)v;
+  }
+  block_reduce_store<1>(acc, 1, partial, kDotBlocks);
+  if (!arrive_last(counter)) return;
+  finish_partials(partial, 1, s + 2, counter);
+  __syncthreads();
+  if (threadIdx.x == 0 && sqrt(s[2]) < 1e-2) f[0] = 0;
+}
+// z = f2 dinv r (f2 = 1) and r.z; beta = new r.z / r.z
+template <typename T>
+__global__ void __launch_bounds__(kDotThreads) k_eig_z(long n, const T* __restrict__ r, const T* __restrict__ dinv,
+                                                       T f2, T* __restrict__ z, double* s, int* f, int its,
+                                                       double* partial, unsigned* counter) {
+  pdl_wait();
+  if (f[0] == 0) return;
+  double acc[1] = {0};
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const T v = f2 * dinv[i] * r[i];
+    z[i] = v;
+    acc[0] += (double)r[i] * (double)v;
+  }
+  block_reduce_store<1>(acc, 1, partial, kDotBlocks);
+  if (!arrive_last(counter)) return;
+  finish_partials(partial, 1, s + 3, counter);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double beta = s[3] / s[0];
+    s[5] = beta;
+    s[kEigHist + its + f[2]] = beta;
+    f[2] += 1;
+    s[0] = s[3];
+  }
+}
+// p = a z + beta p (a = 1)
+template <typename T>
+__global__ void k_eig_p(long n, T a, const T* __restrict__ z, T* __restrict__ p, const double* s, const int* f) {
+  pdl_wait();
+  if (f[0] == 0) return;
+  const T b = (T)s[5];
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    p[i] = a * z[i] + b * p[i];
+}
+__global__ void k_eig_start(int* f) {
+  f[0] = 1;
+  f[1] = 0;
+  f[2] = 0;
+}
+
+void v_eig_start(int* f, cudaStream_t st) {
+  k_eig_start<<<1, 1, 0, st>>>(f);
+  count();
+}
+template <typename T>
+void v_eig_step(long n, T* p, const T* Ap, T* r, T* z, const T* dinv, double* s, int* f, int its,
+                double* partial, cudaStream_t st) {
+  unsigned* counter = reinterpret_cast<unsigned*>(partial + kDotPartialDoubles) + kDotMaxChunks;
+  k_eig_pap<T><<<kDotBlocks, kDotThreads, 0, st>>>(n, p, Ap, s, f, partial, counter);
+  k_eig_r<T><<<kDotBlocks, kDotThreads, 0, st>>>(n, Ap, r, T(1), s, f, partial, counter);
+  k_eig_z<T><<<kDotBlocks, kDotThreads, 0, st>>>(n, r, dinv, T(1), z, s, f, its, partial, counter);
+  k_eig_p<T><<<grid_for(n), kThreads, 0, st>>>(n, T(1), z, p, s, f);
+  VecCounter::launches() += 4;
+}
+template void v_eig_step<float>(long, float*, const float*, float*, float*, const float*, double*, int*, int,
+                                double*, cudaStream_t);
+template void v_eig_step<double>(long, double*, const double*, double*, double*, const double*, double*, int*, int,
+                                 double*, cudaStream_t);
+
 // w += V coef. The basis entries of a row are loaded eight at a time before
 // they are summed (in order j = 0, 1, ...), so eight independent loads per
 // thread are in flight instead of one dependent load per step; the sums are

@@ -90,6 +90,14 @@ void v_basis_df(long n, const double* sc_dev, double sc_host, const double* w, d
 template <typename T>
 void v_dot(long n, const T* a, const T* b, double* out_dev, double* partial, cudaStream_t s,
            const int* active = nullptr);
+// Eigenvalue-estimate CG with device scalars (see vec.cu): s holds kEigHist +
+// 2 its doubles (r.z in s[0] before the first step), f three ints.
+constexpr int kEigHist = 8;
+void v_eig_start(int* f, cudaStream_t st);
+// one step after Ap = A p: alpha, r, |r|, z = D^-1 r, beta, p
+template <typename T>
+void v_eig_step(long n, T* p, const T* Ap, T* r, T* z, const T* dinv, double* s, int* f, int its,
+                double* partial, cudaStream_t st);
 // w += sum_j coef[j] V_j  (coef on the device)
 void v_multiaxpy(long n, int k, const double* coef_dev, const double* V, long ld, double* w, cudaStream_t s,
                  const int* active = nullptr);

@@ -271,7 +271,10 @@ typedef struct gb_gmg_newton_terms {
 int gb_gmg_set_newton_terms(gb_gmg* h, const gb_gmg_newton_terms* terms);
 
 /* build_preconditioner (:1856-1867): level diagonals for both blocks and both
- * precisions, eigenvalue estimates (:834-849) and the captured V-cycles. */
+ * precisions and eigenvalue estimates (:834-849); the V-cycle graphs are
+ * captured on their first use. The FP64 levels are built on their first use (an FP64 V-cycle or solve, an FP64
+ * diagonal or eigenvalue query, gb_gmg_update_viscosity), from the tables of this
+ * call; with GB_GMG_COARSE_DENSE_FP64 they are built here. */
 int gb_gmg_build_preconditioner(gb_gmg* h);
 
 /* One operator application on one level (host arrays, caller numbering).

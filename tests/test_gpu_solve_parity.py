@@ -159,6 +159,36 @@ def test_rejected_viscosity_update_changes_nothing():
     assert np.array_equal(g.vmult(gmg.OP_STOKES, top, x, gmg.FP64), before[0])
 
 
+def test_fp64_levels_follow_the_tables_of_the_build():
+    """gb_gmg_build_preconditioner leaves the FP64 levels (diagonals, eigenvalue
+    estimates) to their first use, built from the tables of that call all the
+    same: after gb_gmg_update_viscosity the FP64 V-cycles and an FP64 solve of a
+    handle that first used its FP64 levels after the update equal, bit for bit,
+    those of a handle that used them before it; a mixed solve right after the
+    build, which never needs them, equals one that follows an FP64 query."""
+    P = problems.sinkers_3d(8, projection=1)
+    f = P.fine
+    early, late = gmg.from_problem(P), gmg.from_problem(P)
+    early.diagonal_inverse(0, 0, gmg.FP64)
+    x_early, o_early = early.solve(P.rhs, linear_solver_tolerance=1e-8, mg_precision=gmg.FP32)
+    x_late, o_late = late.solve(P.rhs, linear_solver_tolerance=1e-8, mg_precision=gmg.FP32)
+    assert o_early["cheap_iterations"] == o_late["cheap_iterations"]
+    assert np.array_equal(x_early, x_late)
+    eta2 = P.eta * np.exp(0.5 * np.random.default_rng(3).uniform(-1, 1, size=P.eta.shape))
+    early.update_viscosity(eta2)
+    late.update_viscosity(eta2)
+    rng = np.random.default_rng(4)
+    for block, n in ((0, f.n_u), (1, f.n_p)):
+        r = rng.normal(size=n)
+        assert np.array_equal(early.vcycle(block, r, gmg.FP64), late.vcycle(block, r, gmg.FP64)), block
+    for lev in range(len(P.levels)):
+        assert np.array_equal(early.eigenvalues(lev, 0, gmg.FP64), late.eigenvalues(lev, 0, gmg.FP64))
+    xa, oa = early.solve(P.rhs, linear_solver_tolerance=1e-8, mg_precision=gmg.FP64)
+    xb, ob = late.solve(P.rhs, linear_solver_tolerance=1e-8, mg_precision=gmg.FP64)
+    assert oa["status"] == 0 and oa["cheap_iterations"] == ob["cheap_iterations"]
+    assert np.array_equal(xa, xb)
+
+
 def test_nsinker_without_averaging_reference_arrangement_on_gpu():
     """tests/nsinker_gmg_no_avg: "Material averaging = none" with the library's
     GB_GMG_VISC_NONE -- per-point viscosity for the outer FGMRES product, the
