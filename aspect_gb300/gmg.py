@@ -280,6 +280,8 @@ class StokesMatrixFreeGPU:
                                                  None if nj is None else _p(nj)))
 
     def build_preconditioner(self):
+        """Diagonals and Chebyshev eigenvalue estimates of every level; the FP64
+        levels are built on their first use (gb_gmg_build_preconditioner)."""
         self._chk(self.L.gb_gmg_build_preconditioner(self.h))
 
     # ---------------------------------------------------------------- solve

@@ -254,8 +254,9 @@ def run_gpu(args):
     log("problem built", n)
     # set-up in the handler's phases: setup_dofs (once per mesh), assemble (set
     # the viscosity: once per nonlinear iteration in ASPECT) and
-    # build_preconditioner (diagonals, eigenvalue estimates, captured V-cycles:
-    # also once per nonlinear iteration)
+    # build_preconditioner (diagonals and eigenvalue estimates of the FP32
+    # levels and the explicit coarse sub-cycles; the FP64 levels and the V-cycle
+    # graphs follow on first use: also once per nonlinear iteration)
     t0 = time.perf_counter()
     g = gmg.StokesMatrixFreeGPU(3, len(P.levels))
     g.setup_dofs(P.levels)
