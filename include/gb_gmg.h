@@ -376,7 +376,8 @@ enum gb_gmg_timed_operation {
  * after one warm-up call, measured with CUDA events on the library's stream. */
 int gb_gmg_time_operation(gb_gmg* h, int what, int precision, int repeats, double* seconds_per_call);
 
-/* Device memory held by the handle (get_*_memory_consumption of stokes_matrix_free.h:80-97). */
+/* Device memory held by the handle (get_*_memory_consumption of stokes_matrix_free.h:80-97);
+ * the FP64 levels' work vectors count from their first use. */
 int gb_gmg_memory_consumption(const gb_gmg* h, size_t* bytes);
 
 /* Number of kernel launches issued by this handle since creation. */
