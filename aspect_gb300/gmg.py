@@ -164,11 +164,20 @@ def _i(a):
     return np.ascontiguousarray(a, dtype=np.int32)
 
 
+def _assign_fields(struct: ctypes.Structure, values: dict, what: str) -> None:
+    """Sets the named fields of a ctypes mirror of a header struct; a name that
+    is not a field raises instead of becoming a plain (ignored) attribute."""
+    names = [f for f, _ in type(struct)._fields_]
+    for k, v in values.items():
+        if k not in names:
+            raise TypeError(f"unknown {what} {k!r}; known: {', '.join(names)}")
+        setattr(struct, k, v)
+
+
 def default_solve_params(**kw) -> SolveParams:
     p = SolveParams()
     load_library().gb_gmg_default_solve_params(ctypes.byref(p))
-    for k, v in kw.items():
-        setattr(p, k, v)
+    _assign_fields(p, kw, "solve parameter")
     return p
 
 
@@ -181,8 +190,7 @@ class StokesMatrixFreeGPU:
         self.L = load_library()
         opt = Options()
         self.L.gb_gmg_default_options(ctypes.byref(opt))
-        for k, v in (options or {}).items():
-            setattr(opt, k, v)
+        _assign_fields(opt, options or {}, "option")
         h = ctypes.c_void_p()
         rc = self.L.gb_gmg_create(ctypes.byref(opt), dim, degree, n_levels, ctypes.byref(h))
         if rc != 0:

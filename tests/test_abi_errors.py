@@ -29,6 +29,18 @@ def test_solve_parameter_defaults_follow_the_reference(L):
     assert p.absolute_tolerance == 0.0
 
 
+def test_misspelled_parameter_names_are_rejected(L):
+    """The Python front end sets only fields the header declares: a misspelled
+    solve parameter or option raises (ctypes would otherwise keep it as a plain
+    attribute and the library would never see it); known names still set."""
+    with pytest.raises(TypeError, match="linear_solver_tolerence"):
+        gmg.default_solve_params(linear_solver_tolerence=1e-8)
+    with pytest.raises(TypeError, match="smoother_degre"):
+        gmg.StokesMatrixFreeGPU(3, 2, {"smoother_degre": 6})  # raises before any CUDA call
+    p = gmg.default_solve_params(linear_solver_tolerance=1e-8, restart=50, orthogonalization=1)
+    assert (p.linear_solver_tolerance, p.restart, p.orthogonalization) == (1e-8, 50, 1)
+
+
 def test_create_rejects_invalid_shapes(L):
     h = ctypes.c_void_p(1)
     for dim, deg, nl in [(1, 2, 3), (4, 2, 3), (3, 1, 3), (3, 4, 3), (3, 2, 0)]:
