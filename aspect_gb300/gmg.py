@@ -164,6 +164,14 @@ def _i(a):
     return np.ascontiguousarray(a, dtype=np.int32)
 
 
+def _at_least(a: np.ndarray, n: int, what: str) -> np.ndarray:
+    """The library reads (or writes) n entries through the array's pointer: a
+    shorter array is rejected with its INVALID_ARGUMENT status before the call."""
+    if a.size < n:
+        raise GmgError(1, f"{what} has {a.size} entries; the library uses {n}")
+    return a
+
+
 def _assign_fields(struct: ctypes.Structure, values: dict, what: str) -> None:
     """Sets the named fields of a ctypes mirror of a header struct; a name that
     is not a field raises instead of becoming a plain (ignored) attribute."""
@@ -247,14 +255,14 @@ class StokesMatrixFreeGPU:
 
     def assemble(self, eta, projection: int, pressure_scaling: float, compressible: int = 0):
         """evaluate_material_model: finest-level viscosity (per cell or per quadrature point)."""
-        eta = _d(eta)
+        eta = _at_least(_d(eta), self.levels[-1].n_cells, "viscosity")
         n_per_cell = eta.size // self.levels[-1].n_cells
         self._chk(self.L.gb_gmg_set_viscosity(self.h, _p(eta), n_per_cell, projection,
                                               ctypes.c_double(pressure_scaling), compressible))
 
     def update_viscosity(self, eta):
         """New viscosity for the operators; keeps the last-built preconditioner."""
-        eta = _d(eta)
+        eta = _at_least(_d(eta), self.levels[-1].n_cells, "viscosity")
         self._chk(self.L.gb_gmg_update_viscosity(self.h, _p(eta), eta.size // self.levels[-1].n_cells))
 
     def set_newton_terms(self, newton=False, symmetrize=False, average=False, dilation=False, strain_rate=None,
@@ -297,6 +305,9 @@ class StokesMatrixFreeGPU:
         """Returns (solution [u; p/s], outputs dict). Raises NoConvergence on failure."""
         rhs = _d(rhs)
         sol = _d(np.zeros_like(rhs) if x0 is None else x0).copy()
+        if self.levels is not None:
+            _at_least(rhs, self._n_top(), "rhs")
+            _at_least(sol, self._n_top(), "x0")
         prm = default_solve_params(**params)
         out = Outputs()
         self._chk(self.L.gb_gmg_solve(self.h, _p(rhs), _p(sol), ctypes.byref(prm), ctypes.byref(out)))
@@ -313,7 +324,8 @@ class StokesMatrixFreeGPU:
     def vmult(self, op: int, level: int, src, precision: int = FP64):
         m = self.levels[level]
         n_out = m.n_u + m.n_p if op == OP_STOKES else (m.n_p if op == OP_MASS else m.n_u)
-        src = _d(src)
+        n_in = m.n_u + m.n_p if op == OP_STOKES else (m.n_u if op == OP_A else m.n_p)
+        src = _at_least(_d(src), n_in, "src")
         out = np.zeros(n_out)
         self._chk(self.L.gb_gmg_vmult(self.h, op, level, precision, _p(src), _p(out)))
         return out
@@ -321,8 +333,8 @@ class StokesMatrixFreeGPU:
     def correct_stokes_rhs(self, u0, rhs):
         """rhs - K u0 (plain reads of u0, which holds the inhomogeneous constraint
         values), as StokesMatrixFreeHandler::correct_stokes_rhs; returns a new array."""
-        u0 = _d(u0)
-        out = _d(rhs).copy()
+        u0 = _at_least(_d(u0), self._n_top(), "u0")
+        out = _at_least(_d(rhs).copy(), self._n_top(), "rhs")
         self._chk(self.L.gb_gmg_correct_stokes_rhs(self.h, _p(u0), _p(out)))
         return out
 
@@ -330,6 +342,8 @@ class StokesMatrixFreeGPU:
         """Body-force right-hand side int f . phi_u of the finest level on the device,
         condensed with the velocity constraints; force_q: (n_cells, 3**dim, dim)."""
         f = _d(force_q)
+        if self.degree == 2:  # other degrees: the library's own rejection
+            _at_least(f, self.levels[-1].n_cells * 3 ** self.dim * self.dim, "force_q")
         out = np.zeros(self.levels[-1].n_u + self.levels[-1].n_p)
         self._chk(self.L.gb_gmg_assemble_rhs(self.h, _p(f), _p(out)))
         return out
@@ -350,30 +364,36 @@ class StokesMatrixFreeGPU:
         return out
 
     def set_eigenvalues(self, level: int, block: int, precision: int, minmax):
-        v = _d(minmax)
+        v = _at_least(_d(minmax), 2, "minmax")
         self._chk(self.L.gb_gmg_set_eigenvalues(self.h, level, block, precision, _p(v)))
 
     def transfer(self, fine_level: int, block: int, restrict: bool, src, precision: int = FP64):
         tgt = self.levels[fine_level - 1 if restrict else fine_level]
         out = np.zeros(tgt.n_u if block == 0 else tgt.n_p)
         src = _d(src)
+        if 1 <= fine_level < len(self.levels):  # other levels: the library's own rejection
+            srcl = self.levels[fine_level if restrict else fine_level - 1]
+            _at_least(src, srcl.n_u if block == 0 else srcl.n_p, "src")
         self._chk(self.L.gb_gmg_transfer(self.h, fine_level, block, precision, int(restrict), _p(src), _p(out)))
         return out
 
     def vcycle(self, block: int, src, precision: int = FP64):
         src = _d(src)
+        if block in (0, 1):
+            _at_least(src, self.levels[-1].n_u if block == 0 else self.levels[-1].n_p, "src")
         out = np.zeros_like(src)
         self._chk(self.L.gb_gmg_vcycle(self.h, block, precision, _p(src), _p(out)))
         return out
 
     def block_preconditioner(self, src, precision: int = FP64):
-        src = _d(src)
+        src = _at_least(_d(src), self._n_top(), "src")
         out = np.zeros_like(src)
         self._chk(self.L.gb_gmg_block_preconditioner(self.h, precision, _p(src), _p(out)))
         return out
 
     def adjoint_gradient(self, u, lam):
-        u, lam = _d(u), _d(lam)
+        u = _at_least(_d(u), self.levels[-1].n_u, "u")
+        lam = _at_least(_d(lam), self.levels[-1].n_u, "lam")
         out = np.zeros(self.levels[-1].n_cells)
         self._chk(self.L.gb_gmg_adjoint_gradient(self.h, _p(u), _p(lam), _p(out)))
         return out
@@ -388,6 +408,9 @@ class StokesMatrixFreeGPU:
         sec = ctypes.c_double()
         self._chk(self.L.gb_gmg_time_operation(self.h, what, precision, repeats, ctypes.byref(sec)))
         return sec.value
+
+    def _n_top(self) -> int:
+        return self.levels[-1].n_u + self.levels[-1].n_p
 
     def kernel_launches(self) -> int:
         return int(self.L.gb_gmg_kernel_launches(self.h))

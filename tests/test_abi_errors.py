@@ -97,3 +97,69 @@ def test_no_gpu_means_no_solver():
     with pytest.raises(gmg.GmgError) as e:
         gmg.StokesMatrixFreeGPU(3, 2)
     assert e.value.code == CUDA_ERROR
+
+
+class _RecordingLibrary:
+    """Stands in for the loaded library behind a front-end object: every entry
+    point records its name and returns OK."""
+
+    def __init__(self):
+        self.calls = []
+
+    def __getattr__(self, name):
+        def entry(*args):
+            self.calls.append(name)
+            return OK
+        return entry
+
+
+def _front_end(degree=2):
+    from types import SimpleNamespace
+
+    g = object.__new__(gmg.StokesMatrixFreeGPU)  # no handle: nothing reaches a GPU
+    g.L, g.h, g.dim, g.degree = _RecordingLibrary(), None, 3, degree
+    g.levels = [SimpleNamespace(n_u=24, n_p=8, n_cells=1), SimpleNamespace(n_u=375, n_p=27, n_cells=8)]
+    return g
+
+
+def test_short_arrays_are_rejected_before_the_library_reads_them():
+    """The library reads a fixed number of entries through each host pointer (the
+    finest level's n_u + n_p for a solve, the operator's source size for a vmult,
+    ...): the front end rejects a shorter array with INVALID_ARGUMENT before the
+    call, and hands arrays of the used length (or longer) through."""
+    g = _front_end()
+    nu, npr, n = 375, 27, 402
+    short = [
+        lambda: g.solve(np.zeros(n - 1)),
+        lambda: g.solve(np.zeros(n), x0=np.zeros(n - 1)),
+        lambda: g.vmult(gmg.OP_STOKES, 1, np.zeros(n - 1)),
+        lambda: g.vmult(gmg.OP_A, 0, np.zeros(23)),
+        lambda: g.vmult(gmg.OP_BT, 1, np.zeros(npr - 1)),
+        lambda: g.vcycle(0, np.zeros(nu - 1)),
+        lambda: g.vcycle(1, np.zeros(npr - 1)),
+        lambda: g.block_preconditioner(np.zeros(n - 1)),
+        lambda: g.transfer(1, 0, True, np.zeros(nu - 1)),
+        lambda: g.transfer(1, 1, False, np.zeros(7)),
+        lambda: g.correct_stokes_rhs(np.zeros(n - 1), np.zeros(n)),
+        lambda: g.adjoint_gradient(np.zeros(nu), np.zeros(nu - 1)),
+        lambda: g.assemble_rhs(np.zeros((8, 27, 2))),
+        lambda: g.set_eigenvalues(0, 0, gmg.FP64, [1.0]),
+        lambda: g.assemble(np.ones(7), gmg.VISC_DGQ0, 1.0),
+    ]
+    for call in short:
+        with pytest.raises(gmg.GmgError) as e:
+            call()
+        assert e.value.code == INVALID
+    assert g.L.calls == []
+    g.solve(np.zeros(n))
+    g.vmult(gmg.OP_MASS, 1, np.zeros(npr))
+    g.vcycle(0, np.zeros(nu))
+    g.transfer(1, 0, False, np.zeros(24))
+    g.adjoint_gradient(np.zeros(n), np.zeros(n))  # [u; p] vectors: the velocity part is read
+    g.assemble_rhs(np.zeros((8, 27, 3)))
+    assert g.L.calls == ["gb_gmg_solve", "gb_gmg_vmult", "gb_gmg_vcycle", "gb_gmg_transfer",
+                         "gb_gmg_adjoint_gradient", "gb_gmg_assemble_rhs"]
+    # degree 3: the body force is the library's to reject (it is built for degree 2)
+    g3 = _front_end(degree=3)
+    g3.assemble_rhs(np.zeros((8, 16, 3)))
+    assert g3.L.calls == ["gb_gmg_assemble_rhs"]
