@@ -2428,6 +2428,8 @@ int gb_gmg_get_diagonal_inverse(gb_gmg* g, int level, int block, int precision, 
   if (!g) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
     Handle& H = g->h;
+    GB_CHECK(block == 0 || block == 1, 1, "block must be 0 (velocity) or 1 (pressure)");
+    GB_CHECK(out, 1, "null output");
     const int pi = precision == GB_GMG_FP32 ? 1 : 0;
     gb::ensure_precision(H, precision);
     GB_CHECK(H.prec_done[pi], GB_GMG_NOT_READY, "build_preconditioner has not been called");
@@ -2447,6 +2449,8 @@ int gb_gmg_get_diagonal_inverse(gb_gmg* g, int level, int block, int precision, 
 int gb_gmg_get_eigenvalues(gb_gmg* g, int level, int block, int precision, double* mm) {
   if (!g) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
+    GB_CHECK(block == 0 || block == 1, 1, "block must be 0 (velocity) or 1 (pressure)");
+    GB_CHECK(mm, 1, "null output");
     gb::ensure_precision(g->h, precision);
     gb::Level& L = g->h.levels.at(level);
     const double* e = precision == GB_GMG_FP32 ? (block == 0 ? L.f32.eigA : L.f32.eigM)
@@ -2459,6 +2463,8 @@ int gb_gmg_get_eigenvalues(gb_gmg* g, int level, int block, int precision, doubl
 int gb_gmg_set_eigenvalues(gb_gmg* g, int level, int block, int precision, const double* mm) {
   if (!g) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
+    GB_CHECK(block == 0 || block == 1, 1, "block must be 0 (velocity) or 1 (pressure)");
+    GB_CHECK(mm, 1, "null interval");
     gb::Level& L = g->h.levels.at(level);
     double* e;
     bool* given;
@@ -2485,6 +2491,7 @@ int gb_gmg_transfer(gb_gmg* g, int fine_level, int block, int precision, int res
   ABI_TRY(g, {
     Handle& H = g->h;
     GB_CHECK(H.setup_done && fine_level >= 1 && fine_level < H.n_levels, 1, "bad transfer level");
+    GB_CHECK(block == 0 || block == 1, 1, "block must be 0 (velocity) or 1 (pressure)");
     gb::Level& F = H.levels[fine_level];
     gb::Level& C = H.levels[fine_level - 1];
     const long nf = block == 0 ? F.n_u : F.n_p, nc = block == 0 ? C.n_u : C.n_p;
@@ -2532,6 +2539,7 @@ int gb_gmg_vcycle(gb_gmg* g, int block, int precision, const double* src, double
   if (!g) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
     Handle& H = g->h;
+    GB_CHECK(block == 0 || block == 1, 1, "block must be 0 (velocity) or 1 (pressure)");
     gb::ensure_precision(H, precision);
     GB_CHECK(H.prec_done[precision == GB_GMG_FP32 ? 1 : 0], GB_GMG_NOT_READY, "build_preconditioner missing");
     const int top = H.n_levels - 1;
