@@ -2362,7 +2362,7 @@ int gb_gmg_assemble_rhs(gb_gmg* g, const double* force, double* rhs) {
 }
 
 int gb_gmg_vmult(gb_gmg* g, int op, int level, int precision, const double* src, double* dst) {
-  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  if (!g || !src || !dst) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
     Handle& H = g->h;
     GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
@@ -2487,7 +2487,7 @@ int gb_gmg_set_eigenvalues(gb_gmg* g, int level, int block, int precision, const
 
 int gb_gmg_transfer(gb_gmg* g, int fine_level, int block, int precision, int restrict_, const double* src,
                     double* dst) {
-  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  if (!g || !src || !dst) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
     Handle& H = g->h;
     GB_CHECK(H.setup_done && fine_level >= 1 && fine_level < H.n_levels, 1, "bad transfer level");
@@ -2536,7 +2536,7 @@ int gb_gmg_transfer(gb_gmg* g, int fine_level, int block, int precision, int res
 }
 
 int gb_gmg_vcycle(gb_gmg* g, int block, int precision, const double* src, double* dst) {
-  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  if (!g || !src || !dst) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
     Handle& H = g->h;
     GB_CHECK(block == 0 || block == 1, 1, "block must be 0 (velocity) or 1 (pressure)");
@@ -2556,7 +2556,7 @@ int gb_gmg_vcycle(gb_gmg* g, int block, int precision, const double* src, double
 }
 
 int gb_gmg_block_preconditioner(gb_gmg* g, int precision, const double* src, double* dst) {
-  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  if (!g || !src || !dst) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
     Handle& H = g->h;
     gb::ensure_precision(H, precision);
@@ -2599,7 +2599,7 @@ int gb_gmg_solve_device(gb_gmg* g, const double* d_rhs, double* d_sol, const gb_
 }
 
 int gb_gmg_solve(gb_gmg* g, const double* rhs, double* sol, const gb_gmg_solve_params* prm, gb_gmg_outputs* out) {
-  if (!g || !out) return GB_GMG_INVALID_ARGUMENT;
+  if (!g || !rhs || !sol || !out) return GB_GMG_INVALID_ARGUMENT;
   Handle& H = g->h;
   const long n = H.setup_done ? H.n_top() : 0;
   if (!n) { H.err = "finalize_setup has not been called"; return GB_GMG_NOT_READY; }
@@ -2620,7 +2620,7 @@ int gb_gmg_solve(gb_gmg* g, const double* rhs, double* sol, const gb_gmg_solve_p
 }
 
 int gb_gmg_adjoint_gradient(gb_gmg* g, const double* u, const double* lambda, double* grad) {
-  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  if (!g || !u || !lambda || !grad) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
     Handle& H = g->h;
     GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");

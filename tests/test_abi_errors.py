@@ -41,6 +41,26 @@ def test_misspelled_parameter_names_are_rejected(L):
     assert (p.linear_solver_tolerance, p.restart, p.orthogonalization) == (1e-8, 50, 1)
 
 
+def test_null_arrays_are_rejected_before_the_handle_is_used(L):
+    """A null host array returns INVALID_ARGUMENT from the entry point's first
+    line, before the handle is read (here a placeholder that is never one)."""
+    fake = ctypes.create_string_buffer(64)
+    h = ctypes.cast(fake, ctypes.c_void_p)
+    x = np.zeros(8)
+    p = x.ctypes.data_as(ctypes.c_void_p)
+    out = gmg.Outputs()
+    assert L.gb_gmg_vmult(h, 0, 0, 0, None, p) == INVALID
+    assert L.gb_gmg_vmult(h, 0, 0, 0, p, None) == INVALID
+    assert L.gb_gmg_vcycle(h, 0, 0, None, p) == INVALID
+    assert L.gb_gmg_block_preconditioner(h, 0, p, None) == INVALID
+    assert L.gb_gmg_transfer(h, 1, 0, 0, 1, None, p) == INVALID
+    assert L.gb_gmg_solve(h, None, p, None, ctypes.byref(out)) == INVALID
+    assert L.gb_gmg_solve(h, p, None, None, ctypes.byref(out)) == INVALID
+    assert L.gb_gmg_adjoint_gradient(h, p, p, None) == INVALID
+    assert L.gb_gmg_correct_stokes_rhs(h, None, p) == INVALID
+    assert L.gb_gmg_assemble_rhs(h, p, None) == INVALID
+
+
 def test_create_rejects_invalid_shapes(L):
     h = ctypes.c_void_p(1)
     for dim, deg, nl in [(1, 2, 3), (4, 2, 3), (3, 1, 3), (3, 4, 3), (3, 2, 0)]:
