@@ -2406,7 +2406,7 @@ int gb_gmg_vmult(gb_gmg* g, int op, int level, int precision, const double* src,
 }
 
 int gb_gmg_vmult_device(gb_gmg* g, int op, int precision, const double* d_src, double* d_dst) {
-  if (!g) return GB_GMG_INVALID_ARGUMENT;
+  if (!g || !d_src || !d_dst) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
     Handle& H = g->h;
     GB_CHECK(H.visc_done, GB_GMG_NOT_READY, "set_viscosity has not been called");
@@ -2576,9 +2576,11 @@ int gb_gmg_block_preconditioner(gb_gmg* g, int precision, const double* src, dou
 
 int gb_gmg_solve_device(gb_gmg* g, const double* d_rhs, double* d_sol, const gb_gmg_solve_params* prm,
                         gb_gmg_outputs* out) {
-  if (!g || !out) return GB_GMG_INVALID_ARGUMENT;
+  if (!g || !d_rhs || !d_sol || !out) return GB_GMG_INVALID_ARGUMENT;
   ABI_TRY(g, {
     Handle& H = g->h;
+    // before the permutation kernels below read the level tables
+    GB_CHECK(H.prec_done[0] || H.prec_done[1], GB_GMG_NOT_READY, "build_preconditioner has not been called");
     gb_gmg_solve_params P;
     if (prm) P = *prm; else gb_gmg_default_solve_params(&P);
     GB_CHECK(P.restart >= 1, 1, "restart must be >= 1");

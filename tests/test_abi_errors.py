@@ -59,6 +59,10 @@ def test_null_arrays_are_rejected_before_the_handle_is_used(L):
     assert L.gb_gmg_adjoint_gradient(h, p, p, None) == INVALID
     assert L.gb_gmg_correct_stokes_rhs(h, None, p) == INVALID
     assert L.gb_gmg_assemble_rhs(h, p, None) == INVALID
+    assert L.gb_gmg_solve_device(h, None, p, None, ctypes.byref(out)) == INVALID
+    assert L.gb_gmg_solve_device(h, p, None, None, ctypes.byref(out)) == INVALID
+    assert L.gb_gmg_vmult_device(h, 0, 0, None, p) == INVALID
+    assert L.gb_gmg_vmult_device(h, 0, 0, p, None) == INVALID
 
 
 def test_create_rejects_invalid_shapes(L):
