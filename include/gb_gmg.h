@@ -14,6 +14,10 @@
  * Conventions
  *  - Every function returns GB_GMG_OK (0) or an error code; nothing throws
  *    across the ABI. gb_gmg_last_error() gives the message of the last error.
+ *    A null array, a block other than 0 (velocity) / 1 (pressure) or a level out
+ *    of range returns GB_GMG_INVALID_ARGUMENT, a missing set-up step
+ *    GB_GMG_NOT_READY, before any device work. Array lengths are the caller's to
+ *    get right: the library reads and writes the sizes each entry states.
  *  - The caller owns every host array; the library copies what it needs into
  *    GB300 device memory (HBM). The handle owns all device memory. Set-up calls
  *    allocate; operator, transfer and V-cycle calls do not. A solve allocates
